@@ -1,0 +1,362 @@
+"""Benchmark: D3Q19 CHT lattice throughput (MLUPS) on one GB300.
+
+Workload (default): the pin-fin heat sink, 256x128x128 cells (4,194,304), base
+plate + 16x8 jittered cylinders of radius 3.5 and height 80, interpolated
+bounce-back with analytic link fractions, MRT collision, FP16 shifted
+populations with FP32 collision, velocity inlet u = 0.08, pressure outlet,
+walls at +-z, periodic in y, outlet sponge of 40 cells.  One step = one fused
+pass + the inlet/outlet plane kernels.  The same case with FP32 populations
+is timed as the plain-precision comparison, and the thermal MG-Krylov solve
+time to a 1e-8 FP64 residual is reported beside it when available.
+
+The populations (2 x 159 MB at FP16) exceed the 129 MB L2, so no L2 flush is
+inserted between steps.
+
+--impl reference times the oracle's C restatement of the reference's CUDA-path
+step (collide, sponge, stream, bounce-back, plane BCs) on the host cores.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "D3Q19 CHT MLUPS + thermal ms to 1e-8 residual, mixed/learned vs plain, 1 GB300"
+WORKLOAD = "pin-fin heat sink 256x128x128, MRT + Bouzidi IBB, FP16 shifted populations"
+
+
+def peaks():
+    p = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(p):
+        with open(p) as fh:
+            d = json.load(fh)
+        return float(d["hbm_gbs"]), float(d.get("bf16_tflops", 1924.8)), "measured"
+    return 6800.0, 1900.0, "fallback"
+
+
+class ClockSampler:
+    """nvidia-smi clocks / throttle reasons sampled every 200 ms during the timed region."""
+
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+         "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+         "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu_index: int):
+        self.idx = gpu_index
+        self.proc = None
+        self.lines = []
+        self.thread = None
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", f"--id={self.idx}", f"--query-gpu={self.Q}", "--format=csv,noheader,nounits",
+                 "-lms", "200"], stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+        except (OSError, FileNotFoundError):
+            self.proc = None
+            return
+        self.thread = threading.Thread(target=self._read, daemon=True)
+        self.thread.start()
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def stop(self):
+        if self.proc is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.proc.kill()
+        sm, smax, reasons = [], None, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            parts = [p.strip() for p in ln.split(",")]
+            if len(parts) < 9:
+                continue
+            try:
+                sm.append(float(parts[1]))
+                smax = float(parts[2])
+            except ValueError:
+                continue
+            for n, v in zip(names, parts[5:9]):
+                if v.lower().startswith("active"):
+                    reasons.add(n)
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": smax,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def dist_env():
+    ws = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return ws, rank, local
+
+
+def make_case(device, storage, args):
+    from fluxcore3d_gb300 import case as cases
+    sim = cases.pin_fin(device=device, collision=args.collision, storage=storage, nx=args.nx, ny=args.ny,
+                        nz=args.nz)
+    sim.cfg.macro_stride = args.macro_stride
+    return sim
+
+
+def lbm_traffic(sim, fc, storage_bytes):
+    """Algorithmic bytes of one fused launch: every fluid cell reads and writes its 19
+    populations once, every cell's flag byte is read, and link cells read their link
+    offset plus 9 bytes per link (w1, w2, meta)."""
+    import torch
+    N = sim.nx * sim.ny * sim.nz
+    deferred = int(((fc.flags & 4) != 0).sum())
+    fluid = int((fc.flags & 1 == 0).sum()) - deferred
+    link_cells = int(((fc.flags & 2) != 0).sum())
+    return fluid * 38 * storage_bytes + N + link_cells * 4 + fc.n_links * 9, fluid
+
+
+def time_steps(sim, steps, per_kernel=True):
+    """Returns (total_ms, fused_kernel_ms_list) timed with CUDA events on the current stream."""
+    import torch
+    st = torch.cuda.current_stream()
+    evs = []
+    t0 = torch.cuda.Event(enable_timing=True)
+    t1 = torch.cuda.Event(enable_timing=True)
+    torch.cuda.synchronize()
+    t0.record(st)
+    for _ in range(steps):
+        if per_kernel:
+            a = torch.cuda.Event(enable_timing=True)
+            b = torch.cuda.Event(enable_timing=True)
+            a.record(st)
+            sim._fc.step(phase_event=b)
+            evs.append((a, b))
+        else:
+            sim._fc.step()
+    t1.record(st)
+    torch.cuda.synchronize()
+    total = t0.elapsed_time(t1)
+    ks = [a.elapsed_time(b) for a, b in evs]
+    return total, ks
+
+
+def run_reference(args):
+    """CPU baseline: the oracle's C restatement of the reference step on all host cores."""
+    ws, rank, _ = dist_env()
+    if rank != 0:
+        return
+    import numpy as np
+    import torch
+    from oracle.lbm import OracleLBM
+    sim = make_case("cpu", "fp32", args)
+    d = sim.ibb_data
+    links = {k: getattr(d, k).numpy() for k in
+             ("fluid_flat", "dir_i", "dir_opp", "w_i", "w_second", "q_ge_half", "ff_flat", "ff_valid")}
+    cores = os.cpu_count() or 1
+    os.environ.setdefault("OMP_NUM_THREADS", str(cores))
+    orc = OracleLBM(sim.nx, sim.ny, sim.nz, sim.f.numpy(), sim.solid_flow.numpy(), collision=args.collision,
+                    omega=float(sim.omega_plus), S=sim._mrt_S.numpy() if hasattr(sim, "_mrt_S") else None,
+                    sigma=sim._sponge_sigma.numpy() if sim.cfg.sponge_length > 0 else None, links=links,
+                    domain_walls=sim.cfg.domain_walls, u_in_lat=sim.u_in_lat, real="f32")
+    orc.step(args.warmup)
+    t = time.perf_counter()
+    orc.step(args.steps)
+    dt = time.perf_counter() - t
+    N = sim.nx * sim.ny * sim.nz
+    v = N * args.steps / dt / 1e6
+    line = {
+        "impl": "reference", "metric": METRIC, "value": round(v, 3), "unit": "MLUPS", "n_gpus": ws,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(dt * 1e3 / args.steps, 3),
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+        "data": "synthetic", "config": {"workload": WORKLOAD.replace("FP16 shifted", "FP32"),
+                                        "cells": N, "l2_flush": "inputs larger than L2"},
+        "cpu_baseline": {"value": round(v, 3), "unit": "MLUPS", "cores": cores, "kind": "port",
+                         "sample": f"{args.steps} full steps of the 256x128x128 workload (oracle C, OpenMP)"},
+        "e2e": {"value": round(v, 3), "unit": "MLUPS", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+
+
+def cpu_baseline_sample(args):
+    """A bounded sample of the same workload on the host cores (oracle, FP32)."""
+    import numpy as np
+    from oracle.lbm import OracleLBM
+    sim = make_case("cpu", "fp32", args)
+    d = sim.ibb_data
+    links = {k: getattr(d, k).numpy() for k in
+             ("fluid_flat", "dir_i", "dir_opp", "w_i", "w_second", "q_ge_half", "ff_flat", "ff_valid")}
+    orc = OracleLBM(sim.nx, sim.ny, sim.nz, sim.f.numpy(), sim.solid_flow.numpy(), collision=args.collision,
+                    omega=float(sim.omega_plus), S=sim._mrt_S.numpy() if hasattr(sim, "_mrt_S") else None,
+                    sigma=sim._sponge_sigma.numpy() if sim.cfg.sponge_length > 0 else None, links=links,
+                    domain_walls=sim.cfg.domain_walls, u_in_lat=sim.u_in_lat, real="f32")
+    orc.step(1)
+    n = args.cpu_steps
+    t = time.perf_counter()
+    orc.step(n)
+    dt = time.perf_counter() - t
+    N = sim.nx * sim.ny * sim.nz
+    return {"value": round(N * n / dt / 1e6, 3), "unit": "MLUPS", "cores": os.cpu_count() or 1, "kind": "port",
+            "sample": f"{n} steps of the same 256x128x128 MRT+IBB workload, FP32 oracle C (OpenMP)"}
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=400)
+    ap.add_argument("--warmup", type=int, default=20)
+    ap.add_argument("--impl", default="fluxcore3d_gb300")
+    ap.add_argument("--collision", default="mrt")
+    ap.add_argument("--nx", type=int, default=256)
+    ap.add_argument("--ny", type=int, default=128)
+    ap.add_argument("--nz", type=int, default=128)
+    ap.add_argument("--macro-stride", type=int, default=100)
+    ap.add_argument("--cpu-steps", type=int, default=3)
+    ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--no-thermal", action="store_true")
+    args = ap.parse_args()
+    args.warmup = max(3, args.warmup)
+    if args.impl == "reference":
+        run_reference(args)
+        return
+
+    import torch
+    ws, rank, local = dist_env()
+    if ws > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl")
+    torch.cuda.set_device(local)
+    dev = torch.device("cuda", local)
+    from fluxcore3d_gb300 import _build
+    _build.build()
+    from fluxcore3d_gb300.solver.lbm_cuda_ext import LBMCUDAUpgrade
+
+    hbm_peak, _, peak_kind = peaks()
+    results = {}
+    for storage in ("fp16", "fp32"):
+        sim = make_case(dev, storage, args)
+        LBMCUDAUpgrade.patch(sim)
+        for _ in range(args.warmup):
+            sim.step(do_thermal=False)
+        torch.cuda.synchronize()
+        sampler = ClockSampler(local) if storage == "fp16" else None
+        if sampler:
+            sampler.start()
+        if ws > 1:
+            torch.distributed.barrier()
+        total_ms, ks = time_steps(sim, args.steps)
+        if ws > 1:
+            tt = torch.tensor([total_ms], device=dev)
+            torch.distributed.all_reduce(tt, op=torch.distributed.ReduceOp.MAX)
+            total_ms = float(tt)
+        clocks = sampler.stop() if sampler else None
+        sbytes = 2 if storage == "fp16" else 4
+        alg, n_fluid = lbm_traffic(sim, sim._fc, sbytes)
+        kmean = statistics.mean(ks)
+        results[storage] = dict(total_ms=total_ms, kernel_ms=kmean, alg=alg, clocks=clocks,
+                                N=sim.nx * sim.ny * sim.nz, n_fluid=n_fluid, planes=len(sim._fc.planes),
+                                links=sim._fc.n_links, err=sim._fc.check_device_error())
+        if storage == "fp16":
+            keep = sim
+        else:
+            del sim
+    r = results["fp16"]
+    N = r["N"]
+    mlups = N * args.steps / (r["total_ms"] / 1e3) / 1e6 * ws
+    achieved = r["alg"] / (r["kernel_ms"] / 1e3) / 1e9
+    launches_per_step = 1 + 2 * r["planes"] + (1 if any(True for _ in []) else 0)
+
+    # end to end through the public API with host buffers
+    e2e = None
+    if not args.no_e2e:
+        e2e = e2e_run(args, dev)
+
+    line = {
+        "metric": METRIC,
+        "value": round(mlups, 1),
+        "unit": "MLUPS",
+        "n_gpus": ws,
+        "steps": args.steps,
+        "warmup": args.warmup,
+        "ms_per_step": round(r["total_ms"] / args.steps, 5),
+        "higher_is_better": True,
+        "scaling": "weak",
+        "vs_baseline": None,
+        "dtype": "f16-storage/f32-compute",
+        "data": "synthetic",
+        "config": {"workload": WORKLOAD, "cells": N, "fluid_cells": r["n_fluid"], "links": r["links"],
+                   "collision": args.collision, "macro_stride": args.macro_stride,
+                   "l2_flush": "inputs larger than L2 (2 x 159 MB populations)", "parallelism": "replicas"},
+        "roofline": {"bound": "hbm", "achieved": round(achieved, 1), "peak": hbm_peak, "unit": "GB/s",
+                     "frac": round(achieved / hbm_peak, 4), "traffic": None,
+                     "kernel": "k_fused_step<F16S,MRT>", "kernel_ms": round(r["kernel_ms"], 5),
+                     "peak_kind": peak_kind},
+        "fp32": {"mlups": round(results["fp32"]["N"] * args.steps / (results["fp32"]["total_ms"] / 1e3) / 1e6, 1),
+                 "kernel_ms": round(results["fp32"]["kernel_ms"], 5),
+                 "achieved_gbs": round(results["fp32"]["alg"] / (results["fp32"]["kernel_ms"] / 1e3) / 1e9, 1)},
+        "clocks": r["clocks"],
+        "gpu_launches": args.steps * launches_per_step,
+        "device_error": r["err"],
+    }
+    line["fp16_over_fp32"] = round(line["value"] / max(line["fp32"]["mlups"], 1e-9), 3)
+    if e2e:
+        line["e2e"] = e2e
+    if not args.no_thermal:
+        try:
+            th = thermal_run(args, dev)
+            if th:
+                line["thermal"] = th
+        except ImportError:
+            pass
+    if rank == 0 and not args.no_cpu:
+        line["cpu_baseline"] = cpu_baseline_sample(args)
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+    if ws > 1:
+        torch.distributed.destroy_process_group()
+
+
+def e2e_run(args, dev):
+    """Public API end to end: initial populations uploaded from pinned host memory, K steps
+    through sim.step(), final macro fields read back; bytes are reported per step."""
+    import torch
+    from fluxcore3d_gb300.solver.lbm_cuda_ext import LBMCUDAUpgrade
+    sim = make_case(dev, "fp16", args)
+    host_f = sim.f.cpu().pin_memory()
+    out = torch.empty((4,) + tuple(sim.rho.shape), dtype=torch.float32).pin_memory()
+    LBMCUDAUpgrade.patch(sim)
+    for _ in range(args.warmup):
+        sim.step(do_thermal=False)
+    torch.cuda.synchronize()
+    t = time.perf_counter()
+    sim.f.copy_(host_f, non_blocking=True)
+    sim._fc.invalidate()
+    for _ in range(args.steps):
+        sim.step(do_thermal=False)
+    out[0].copy_(sim.rho, non_blocking=True)
+    out[1].copy_(sim.u, non_blocking=True)
+    out[2].copy_(sim.v, non_blocking=True)
+    out[3].copy_(sim.wv, non_blocking=True)
+    torch.cuda.synchronize()
+    dt = time.perf_counter() - t
+    N = sim.nx * sim.ny * sim.nz
+    return {"value": round(N * args.steps / dt / 1e6, 1), "unit": "MLUPS",
+            "h2d_bytes_per_step": int(host_f.numel() * 4 // args.steps),
+            "d2h_bytes_per_step": int(out.numel() * 4 // args.steps)}
+
+
+def thermal_run(args, dev):
+    from fluxcore3d_gb300 import thermal_bench
+    return thermal_bench.run(dev)
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,160 @@
+"""ctypes binding of libfluxcore3d_gb300.so.
+
+The library is the only compute backend.  `lib()` raises when it is missing or
+when CUDA is unavailable; there is no CPU or torch fallback behind it.
+Tensors cross the boundary as raw device pointers (`tensor.data_ptr()`) and
+the launching stream as `torch.cuda.current_stream().cuda_stream`.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+
+from . import _build
+
+_LIB = None
+_LOAD_ERROR: str | None = None
+
+c_float_p = C.POINTER(C.c_float)
+vp = C.c_void_p
+i32 = C.c_int
+i64 = C.c_longlong
+f32 = C.c_float
+f64 = C.c_double
+
+
+class StepArgs(C.Structure):
+    """Mirror of fc_lbm_step_args (include/fluxcore3d_gb300.h)."""
+
+    _fields_ = [
+        ("storage", C.c_int32),
+        ("collision", C.c_int32),
+        ("nx", C.c_int32),
+        ("ny", C.c_int32),
+        ("nz", C.c_int32),
+        ("periodic", C.c_int32 * 3),
+        ("pop_in", vp),
+        ("pop_out", vp),
+        ("f32", vp),
+        ("rho", vp),
+        ("u", vp),
+        ("v", vp),
+        ("w", vp),
+        ("cell_flags", vp),
+        ("link_off", vp),
+        ("link_meta", vp),
+        ("link_w", vp),
+        ("n_links", i64),
+        ("sponge", vp),
+        ("sponge_axis", C.c_int32),
+        ("has_links", C.c_int32),
+        ("omega", f32),
+        ("omega_plus", f32),
+        ("omega_minus", f32),
+        ("S", f32 * 19),
+        ("Cs_dx2", f32),
+        ("omega0", f32),
+        ("dev_err", vp),
+    ]
+
+
+# name -> (restype, argtypes)
+SIGNATURES: dict[str, tuple] = {
+    "fc_abi_version": (i32, []),
+    # lattice, per-operation
+    "fc_lbm_macro_collide_bgk": (i32, [vp, vp, vp, vp, vp, vp, vp, f32, i64, vp]),
+    "fc_lbm_macro_collide_trt": (i32, [vp, vp, vp, vp, vp, vp, vp, f32, f32, i64, vp]),
+    "fc_lbm_macro_collide_mrt": (i32, [vp, vp, vp, vp, vp, vp, vp, vp, i64, vp]),
+    "fc_lbm_macro_collide_mrt_smag": (i32, [vp, vp, vp, vp, vp, vp, vp, vp, f32, f32, i64, vp]),
+    "fc_lbm_stream_pull": (i32, [vp, vp, i32, i32, i32, i32, i32, i32, vp]),
+    "fc_lbm_sponge": (i32, [vp, vp, vp, vp, vp, vp, i64, vp]),
+    "fc_lbm_ibb": (i32, [vp, vp, vp, vp, vp, vp, vp, vp, vp, vp, i64, i64, vp, vp]),
+    "fc_lbm_reset_solid": (i32, [vp, vp, i64, vp]),
+    "fc_lbm_zou_he_bc": (i32, [vp, vp, i32, i32, i32, i32, i32, i32, i32, f32, f32, i32, vp]),
+    "fc_lbm_convective_workspace_bytes": (i64, [i32, i32]),
+    "fc_lbm_convective_bc": (i32, [vp, vp, i32, i32, i32, i32, i32, i32, i32, f32, i32, i32, vp, i64, vp]),
+    # lattice, fused
+    "fc_lbm_fused_step": (i32, [C.POINTER(StepArgs), vp]),
+    "fc_lbm_collide_from_f32": (i32, [C.POINTER(StepArgs), i32, i32, vp]),
+    "fc_lbm_materialize": (i32, [C.POINTER(StepArgs), vp]),
+    "fc_lbm_pin_solid": (i32, [C.POINTER(StepArgs), vp]),
+    # multigrid
+    "fc_mg_mop": (i32, [vp] * 9 + [f32, i32, i32, i32, i32, i32, vp]),
+    "fc_mg_jacobi": (i32, [vp, vp, vp, vp, i64, vp]),
+    "fc_mg_apply_L": (i32, [vp] * 9 + [f32, i32, i32, i32, i32, i32, vp]),
+    "fc_mg_smooth": (i32, [vp] * 11 + [f32, i32, i32, i32, i32, i32, vp]),
+    "fc_mg_smooth_from_zero": (i32, [vp, vp, vp, i64, vp]),
+    "fc_mg_residual_restrict": (i32, [vp] * 10 + [f32, i32, i32, i32, i32, i32, vp, i32, i32, i32, vp]),
+    "fc_mg_prolong_correct": (i32, [vp, vp, vp, i32, i32, i32, i32, i32, i32, f32, vp]),
+    "fc_mg_reduce_workspace_bytes": (i64, [i64]),
+    "fc_mg_residual_norm2": (i32, [vp] * 10 + [f32, i32, i32, i32, i32, i32, vp, vp, i64, vp, vp]),
+    "fc_mg_build_coeffs": (i32, [vp] * 5 + [i32, i32, i32, i32, i32, f32, f32] + [vp] * 7 + [vp]),
+    "fc_mg_restrict_mean": (i32, [vp, i32, i32, i32, vp, i32, vp]),
+    "fc_mg_inv_diag": (i32, [vp, vp, vp, f32, f32, i64, vp]),
+    # krylov
+    "fc_vec_workspace_bytes": (i64, [i64]),
+    "fc_vec_dot": (i32, [i32, vp, vp, i64, vp, vp, i64, vp, vp]),
+    "fc_vec_axpby": (i32, [i32, vp, vp, i64, f64, vp, vp, f64, vp, vp]),
+    "fc_vec_convert": (i32, [i32, vp, vp, i64, vp, f64, vp]),
+    "fc_mg_mop_f64": (i32, [vp] * 8 + [f64, i32, i32, i32, i32, i32, vp, vp, vp, vp]),
+}
+
+STATUS_TEXT = {1: "bad argument", 2: "CUDA launch failure", 3: "unsupported combination"}
+
+
+def lib_path() -> str:
+    return _build.LIB_PATH
+
+
+def _load():
+    global _LIB, _LOAD_ERROR
+    if _LIB is not None or _LOAD_ERROR is not None:
+        return
+    path = lib_path()
+    if not os.path.exists(path):
+        _LOAD_ERROR = f"{path} is not built (run fluxcore3d_gb300._build.build())"
+        return
+    try:
+        L = C.CDLL(path)
+    except OSError as e:  # pragma: no cover - depends on the machine
+        _LOAD_ERROR = f"cannot load {path}: {e}"
+        return
+    for name, (res, args) in SIGNATURES.items():
+        fn = getattr(L, name, None)
+        if fn is None:
+            continue
+        fn.restype = res
+        fn.argtypes = args
+    _LIB = L
+
+
+def load_error() -> str | None:
+    _load()
+    return _LOAD_ERROR
+
+
+def lib():
+    """The loaded library; raises RuntimeError if it cannot be used."""
+    _load()
+    if _LIB is None:
+        raise RuntimeError(f"fluxcore3d_gb300 native library unavailable: {_LOAD_ERROR}")
+    return _LIB
+
+
+def exported_symbols() -> list[str]:
+    """Names from SIGNATURES that the loaded library actually exports."""
+    L = lib()
+    return [n for n in SIGNATURES if hasattr(L, n)]
+
+
+def check(rc: int, what: str) -> None:
+    if rc != 0:
+        raise RuntimeError(f"{what} failed: {STATUS_TEXT.get(rc, f'status {rc}')}")
+
+
+def call(name: str, *args) -> int:
+    fn = getattr(lib(), name)
+    rc = fn(*args)
+    if fn.restype is i32:
+        check(rc, name)
+    return rc

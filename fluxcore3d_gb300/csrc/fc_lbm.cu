@@ -1,0 +1,828 @@
+// fc_lbm.cu -- D3Q19 lattice-Boltzmann kernels for sm_103a behind a C ABI.
+//
+// Two families live here.
+//
+// 1. The per-operation kernels with the reference module's call surface
+//    (LBM_CUDA.* in solver/lbm_kernels.cu:1347-1386): macro_collide_{bgk,trt,
+//    mrt,mrt_smag}, stream_pull, sponge, ibb, reset_solid, zou_he_bc and
+//    convective_bc.  They operate on FP32 [19][N] tensors with the reference's
+//    semantics and are what a caller that drives single operations binds.
+//
+// 2. The fused step used by the drop-in solver object: one pass per time step
+//    that pulls post-collision populations from the previous step (periodic /
+//    copy-self edges as stream_pull), applies interpolated bounce-back from a
+//    per-cell link table, collides (BGK/TRT/MRT/MRT-Smagorinsky), applies the
+//    outlet sponge and stores the next post-collision populations in FP32 or in
+//    FP16/BF16 shifted (f - w_q) form.  Solid cells are never touched: their
+//    populations are pinned to w_q in both ping-pong buffers, which is what
+//    collide-then-reset produces in the reference every step.  Cells on
+//    inlet/outlet planes export their post-stream populations to an FP32 [19][N]
+//    tensor so the plane BC kernels can run on it in the reference order, after
+//    which plane_collide finishes them.
+#include "fc_common.cuh"
+#include "fc_collide.cuh"
+#include "../../include/fluxcore3d_gb300.h"
+
+using namespace fc;
+
+namespace {
+
+constexpr int BLOCK = 256;
+
+__constant__ int c_CX[19] = {0, 1, -1, 0, 0, 0, 0, 1, 1, -1, -1, 1, 1, -1, -1, 0, 0, 0, 0};
+__constant__ int c_CY[19] = {0, 0, 0, 1, -1, 0, 0, 1, -1, 1, -1, 0, 0, 0, 0, 1, 1, -1, -1};
+__constant__ int c_CZ[19] = {0, 0, 0, 0, 0, 1, -1, 0, 0, 0, 0, 1, -1, 1, -1, 1, -1, 1, -1};
+__constant__ int c_OPP[19] = {0, 2, 1, 4, 3, 6, 5, 10, 9, 8, 7, 14, 13, 12, 11, 18, 17, 16, 15};
+
+inline unsigned grid_for(long long n) { return (unsigned)((n + BLOCK - 1) / BLOCK); }
+
+// ============================================================================
+//  Family 1: per-operation kernels (reference call surface)
+// ============================================================================
+
+template <int MODE>
+__global__ void __launch_bounds__(BLOCK) k_macro_collide(
+    const float* __restrict__ f, float* __restrict__ f_post, float* __restrict__ rho,
+    float* __restrict__ u, float* __restrict__ v, float* __restrict__ w,
+    const uint8_t* __restrict__ solid, CollideParams p, const float* __restrict__ S_dev, long long N) {
+    const long long idx = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (idx >= N) return;
+    if (S_dev) {
+#pragma unroll
+        for (int q = 0; q < 19; ++q) p.S[q] = __ldg(S_dev + q);
+    }
+    if (solid[idx]) {
+#pragma unroll
+        for (int q = 0; q < 19; ++q) f_post[q * N + idx] = wq(q);
+        rho[idx] = 1.f; u[idx] = 0.f; v[idx] = 0.f; w[idx] = 0.f;
+        return;
+    }
+    float fi[19], feq[19];
+#pragma unroll
+    for (int q = 0; q < 19; ++q) fi[q] = __ldg(f + q * N + idx);
+    const Macro m = collide<MODE>(fi, feq, p);
+    rho[idx] = m.rho; u[idx] = m.ux; v[idx] = m.uy; w[idx] = m.uz;
+#pragma unroll
+    for (int q = 0; q < 19; ++q) f_post[q * N + idx] = fi[q];
+}
+
+__global__ void __launch_bounds__(BLOCK) k_stream_pull(
+    const float* __restrict__ fin, float* __restrict__ fout, int nx, int ny, int nz,
+    int px, int py, int pz) {
+    const long long N = (long long)nx * ny * nz;
+    const long long idx = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (idx >= N) return;
+    const int nynz = ny * nz;
+    const int i = (int)(idx / nynz);
+    const int rem = (int)(idx - (long long)i * nynz);
+    const int j = rem / nz;
+    const int k = rem - j * nz;
+#pragma unroll
+    for (int q = 0; q < 19; ++q) {
+        int si = i - cx(q), sj = j - cy(q), sk = k - cz(q);
+        bool self = false;
+        if (si < 0 || si >= nx) { if (px) si = (si + nx) % nx; else self = true; }
+        if (sj < 0 || sj >= ny) { if (py) sj = (sj + ny) % ny; else self = true; }
+        if (sk < 0 || sk >= nz) { if (pz) sk = (sk + nz) % nz; else self = true; }
+        const long long src = self ? idx : ((long long)si * nynz + (long long)sj * nz + sk);
+        fout[q * N + idx] = fin[q * N + src];
+    }
+}
+
+__global__ void __launch_bounds__(BLOCK) k_sponge(
+    float* __restrict__ f, const float* __restrict__ rho, const float* __restrict__ u,
+    const float* __restrict__ v, const float* __restrict__ w, const float* __restrict__ sigma,
+    long long N) {
+    const long long idx = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (idx >= N) return;
+    const float sg = sigma[idx];
+    if (sg <= 0.f) return;
+    float feq[19];
+    equilibrium(rho[idx], u[idx], v[idx], w[idx], feq);
+#pragma unroll
+    for (int q = 0; q < 19; ++q) {
+        const long long a = q * N + idx;
+        f[a] = f[a] - sg * (f[a] - feq[q]);
+    }
+}
+
+__global__ void __launch_bounds__(BLOCK) k_ibb_links(
+    const float* __restrict__ fpost, float* __restrict__ fstream,
+    const int* __restrict__ fluid_flat, const int* __restrict__ dir_i,
+    const int* __restrict__ dir_opp, const float* __restrict__ w1,
+    const float* __restrict__ w2, const uint8_t* __restrict__ q_ge_half,
+    const int* __restrict__ ff_flat, const uint8_t* __restrict__ ff_valid,
+    long long n_links, long long N, unsigned* __restrict__ dev_err) {
+    const long long l = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (l >= n_links) return;
+    const long long xf = fluid_flat[l];
+    const int qi = dir_i[l], qo = dir_opp[l];
+    if (xf < 0 || xf >= N || qi < 0 || qi > 18 || qo < 0 || qo > 18) {
+        if (dev_err) atomicOr(dev_err, DEV_ERR_INDEX);
+        return;
+    }
+    const float a = fpost[qo * N + xf];
+    float bb;
+    if (q_ge_half[l]) {
+        bb = w1[l] * a + w2[l] * fpost[qi * N + xf];
+    } else if (ff_valid[l]) {
+        const long long xff = ff_flat[l];
+        if (xff < 0 || xff >= N) {
+            if (dev_err) atomicOr(dev_err, DEV_ERR_INDEX);
+            return;
+        }
+        bb = w1[l] * a + w2[l] * fpost[qo * N + xff];
+    } else {
+        bb = a;
+    }
+    fstream[qi * N + xf] = bb;
+}
+
+__global__ void __launch_bounds__(BLOCK) k_reset_solid(float* __restrict__ f,
+                                                       const uint8_t* __restrict__ solid, long long N) {
+    const long long idx = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (idx >= N || !solid[idx]) return;
+#pragma unroll
+    for (int q = 0; q < 19; ++q) f[q * N + idx] = wq(q);
+}
+
+// plane node (a,b) -> flat index of plane `p` along `axis`
+__device__ __forceinline__ long long plane_flat(int axis, int p, int a, int b, int ny, int nz) {
+    if (axis == 0) return ((long long)p * ny + a) * nz + b;
+    if (axis == 1) return ((long long)a * ny + p) * nz + b;
+    return ((long long)a * ny + b) * nz + p;
+}
+
+// Regularized Zou/He on one plane (reference semantics: solver/lbm_kernels.cu:791-969).
+// Second-order Hermite tensors Q = c c - I/3 use the reference's 8-digit literals.
+__device__ __forceinline__ float q_diag(int c) { return c != 0 ? 0.66666667f : -0.33333333f; }
+
+__device__ void zou_he_node(float* __restrict__ f, long long N, long long flat_bc, long long flat_in,
+                            int axis, int plane_idx, int bc_type, float u_in, float rho_out, int sign) {
+    float fi[19];
+#pragma unroll
+    for (int q = 0; q < 19; ++q) fi[q] = f[q * N + flat_bc];
+    const int unknown = (plane_idx == 0) ? 1 : -1;
+    const int known = -unknown;
+    float s0 = 0.f, sk = 0.f;
+#pragma unroll
+    for (int q = 0; q < 19; ++q) {
+        const int c = axis == 0 ? cx(q) : (axis == 1 ? cy(q) : cz(q));
+        if (c == 0) s0 += fi[q];
+        if (c == known) sk += fi[q];
+    }
+    float rho_bc, uax, ub = 0.f, vb = 0.f, wb = 0.f;
+    if (bc_type == 0) {
+        uax = u_in;
+        rho_bc = (s0 + 2.f * sk) / (1.f - fabsf(u_in) + 1e-12f);
+        rho_bc = fminf(fmaxf(rho_bc, 0.2f), 5.0f);
+        if (axis == 0) ub = uax; else if (axis == 1) vb = uax; else wb = uax;
+    } else {
+        rho_bc = rho_out;
+        uax = (float)known * ((s0 + 2.f * sk) / (rho_bc + 1e-12f) - 1.f);
+        if (uax * (float)sign < 0.f) {
+#pragma unroll
+            for (int q = 0; q < 19; ++q) f[q * N + flat_bc] = f[q * N + flat_in];
+            return;
+        }
+        float fin[19];
+#pragma unroll
+        for (int q = 0; q < 19; ++q) fin[q] = f[q * N + flat_in];
+        const Macro mi = macros_of(fin);
+        if (axis == 0) { ub = uax; vb = mi.uy; wb = mi.uz; }
+        else if (axis == 1) { ub = mi.ux; vb = uax; wb = mi.uz; }
+        else { ub = mi.ux; vb = mi.uy; wb = uax; }
+    }
+    float feq[19];
+    equilibrium(rho_bc, ub, vb, wb, feq);
+    float g[19];
+#pragma unroll
+    for (int q = 0; q < 19; ++q) {
+        const int c = axis == 0 ? cx(q) : (axis == 1 ? cy(q) : cz(q));
+        g[q] = (c == unknown) ? fi[opp(q)] + feq[q] - feq[opp(q)] : fi[q];
+    }
+    float Pxx = 0.f, Pyy = 0.f, Pzz = 0.f, Pxy = 0.f, Pxz = 0.f, Pyz = 0.f;
+#pragma unroll
+    for (int q = 0; q < 19; ++q) {
+        const float fn = g[q] - feq[q];
+        Pxx += fn * q_diag(cx(q));
+        Pyy += fn * q_diag(cy(q));
+        Pzz += fn * q_diag(cz(q));
+        Pxy += fn * (float)(cx(q) * cy(q));
+        Pxz += fn * (float)(cx(q) * cz(q));
+        Pyz += fn * (float)(cy(q) * cz(q));
+    }
+#pragma unroll
+    for (int q = 0; q < 19; ++q) {
+        const float sq = q_diag(cx(q)) * Pxx + q_diag(cy(q)) * Pyy + q_diag(cz(q)) * Pzz +
+                         2.f * ((float)(cx(q) * cy(q)) * Pxy + (float)(cx(q) * cz(q)) * Pxz +
+                                (float)(cy(q) * cz(q)) * Pyz);
+        f[q * N + flat_bc] = feq[q] + wq(q) * sq * 4.5f;
+    }
+}
+
+__global__ void __launch_bounds__(BLOCK) k_zou_he(
+    float* __restrict__ f, const uint8_t* __restrict__ solid, int nx, int ny, int nz, int axis,
+    int plane_idx, int interior_idx, int bc_type, float u_in, float rho_out, int sign, int n1, int n2) {
+    const int t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= n1 * n2) return;
+    const int a = t / n2, b = t - (t / n2) * n2;
+    const long long N = (long long)nx * ny * nz;
+    const long long fb = plane_flat(axis, plane_idx, a, b, ny, nz);
+    const long long fi = plane_flat(axis, interior_idx, a, b, ny, nz);
+    if (solid[fb]) return;
+    zou_he_node(f, N, fb, fi, axis, plane_idx, bc_type, u_in, rho_out, sign);
+}
+
+// Convective outlet, pass 1: zero-gradient copy of the incoming populations
+// and per-block partial sums (FP64, fixed tree order => deterministic).
+__global__ void __launch_bounds__(BLOCK) k_convective_pass1(
+    float* __restrict__ f, const uint8_t* __restrict__ solid, int nx, int ny, int nz, int axis,
+    int outlet_idx, int interior_idx, int unknown_cax, int n1, int n2,
+    double* __restrict__ part_rho, int* __restrict__ part_cnt) {
+    __shared__ double s_rho[BLOCK];
+    __shared__ int s_cnt[BLOCK];
+    const int t = blockIdx.x * blockDim.x + threadIdx.x;
+    const long long N = (long long)nx * ny * nz;
+    double r = 0.0;
+    int c = 0;
+    if (t < n1 * n2) {
+        const int a = t / n2, b = t - (t / n2) * n2;
+        const long long fo = plane_flat(axis, outlet_idx, a, b, ny, nz);
+        const long long fi = plane_flat(axis, interior_idx, a, b, ny, nz);
+        if (!solid[fo]) {
+            float rn = 0.f;
+#pragma unroll
+            for (int q = 0; q < 19; ++q) {
+                const int cq = axis == 0 ? cx(q) : (axis == 1 ? cy(q) : cz(q));
+                float val = f[q * N + fo];
+                if (cq == unknown_cax) { val = f[q * N + fi]; f[q * N + fo] = val; }
+                rn += val;
+            }
+            r = (double)rn;
+            c = 1;
+        }
+    }
+    s_rho[threadIdx.x] = r;
+    s_cnt[threadIdx.x] = c;
+    __syncthreads();
+    for (int st = BLOCK / 2; st > 0; st >>= 1) {
+        if ((int)threadIdx.x < st) {
+            s_rho[threadIdx.x] += s_rho[threadIdx.x + st];
+            s_cnt[threadIdx.x] += s_cnt[threadIdx.x + st];
+        }
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) { part_rho[blockIdx.x] = s_rho[0]; part_cnt[blockIdx.x] = s_cnt[0]; }
+}
+
+// Convective outlet, pass 2: every block reduces the partials in the same
+// order, then rescales its fluid outlet nodes by rho_out * count / sum(rho).
+__global__ void __launch_bounds__(BLOCK) k_convective_pass2(
+    float* __restrict__ f, const uint8_t* __restrict__ solid, int nx, int ny, int nz, int axis,
+    int outlet_idx, float rho_out, int n1, int n2, const double* __restrict__ part_rho,
+    const int* __restrict__ part_cnt, int n_parts) {
+    __shared__ double s_rho[BLOCK];
+    __shared__ int s_cnt[BLOCK];
+    double r = 0.0;
+    int c = 0;
+    for (int p = threadIdx.x; p < n_parts; p += BLOCK) { r += part_rho[p]; c += part_cnt[p]; }
+    s_rho[threadIdx.x] = r;
+    s_cnt[threadIdx.x] = c;
+    __syncthreads();
+    for (int st = BLOCK / 2; st > 0; st >>= 1) {
+        if ((int)threadIdx.x < st) {
+            s_rho[threadIdx.x] += s_rho[threadIdx.x + st];
+            s_cnt[threadIdx.x] += s_cnt[threadIdx.x + st];
+        }
+        __syncthreads();
+    }
+    const double sum = s_rho[0];
+    const int cnt = s_cnt[0];
+    const int t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= n1 * n2) return;
+    if (cnt < 1 || sum < 1e-10) return;
+    const float corr = (float)((double)rho_out * (double)cnt / sum);
+    const int a = t / n2, b = t - (t / n2) * n2;
+    const long long N = (long long)nx * ny * nz;
+    const long long fo = plane_flat(axis, outlet_idx, a, b, ny, nz);
+    if (solid[fo]) return;
+#pragma unroll
+    for (int q = 0; q < 19; ++q) f[q * N + fo] *= corr;
+}
+
+// ============================================================================
+//  Family 2: fused step
+// ============================================================================
+
+struct Geo {
+    int nx, ny, nz;
+    int px, py, pz;
+    long long N;
+    int nynz;
+};
+
+__device__ __forceinline__ void cell_coords(const Geo& g, long long idx, int& i, int& j, int& k) {
+    i = (int)(idx / g.nynz);
+    const int rem = (int)(idx - (long long)i * g.nynz);
+    j = rem / g.nz;
+    k = rem - j * g.nz;
+}
+
+// Neighbour source index for population q at cell (i,j,k): x - c_q with
+// periodic wrap, or the cell itself when a non-periodic axis leaves the box.
+struct Nbr {
+    int im, ip, jm, jp, km, kp;  // -1 = leave the box on a non-periodic axis
+};
+__device__ __forceinline__ Nbr make_nbr(const Geo& g, int i, int j, int k) {
+    Nbr n;
+    n.im = i > 0 ? i - 1 : (g.px ? g.nx - 1 : -1);
+    n.ip = i < g.nx - 1 ? i + 1 : (g.px ? 0 : -1);
+    n.jm = j > 0 ? j - 1 : (g.py ? g.ny - 1 : -1);
+    n.jp = j < g.ny - 1 ? j + 1 : (g.py ? 0 : -1);
+    n.km = k > 0 ? k - 1 : (g.pz ? g.nz - 1 : -1);
+    n.kp = k < g.nz - 1 ? k + 1 : (g.pz ? 0 : -1);
+    return n;
+}
+template <int Q>
+__device__ __forceinline__ long long src_of(const Geo& g, const Nbr& n, int i, int j, int k, long long idx) {
+    const int si = cx(Q) == 1 ? n.im : (cx(Q) == -1 ? n.ip : i);
+    const int sj = cy(Q) == 1 ? n.jm : (cy(Q) == -1 ? n.jp : j);
+    const int sk = cz(Q) == 1 ? n.km : (cz(Q) == -1 ? n.kp : k);
+    if ((si | sj | sk) < 0) return idx;
+    return ((long long)si * g.ny + sj) * g.nz + sk;
+}
+
+template <int KIND, int Q>
+struct PullOne {
+    static __device__ __forceinline__ void run(const typename Store<KIND>::T* __restrict__ P, const Geo& g,
+                                               const Nbr& n, int i, int j, int k, long long idx, float f[19]) {
+        f[Q] = Store<KIND>::load(P + (long long)Q * g.N + src_of<Q>(g, n, i, j, k, idx), Q);
+        PullOne<KIND, Q + 1>::run(P, g, n, i, j, k, idx, f);
+    }
+};
+template <int KIND>
+struct PullOne<KIND, 19> {
+    static __device__ __forceinline__ void run(const typename Store<KIND>::T* __restrict__, const Geo&,
+                                               const Nbr&, int, int, int, long long, float*) {}
+};
+
+template <int KIND>
+__device__ __forceinline__ float load_dyn(const typename Store<KIND>::T* __restrict__ P, long long N,
+                                          int q, long long cell) {
+    float v = 0.f;
+    const auto raw = P + (long long)q * N + cell;
+    if (KIND == ST_F32) {
+        v = __ldg(reinterpret_cast<const float*>(raw));
+    } else if (KIND == ST_F16S) {
+        v = __half2float(__ldg(reinterpret_cast<const __half*>(raw)));
+    } else {
+        v = __bfloat162float(__ldg(reinterpret_cast<const __nv_bfloat16*>(raw)));
+    }
+    if (KIND != ST_F32) {
+        v += (q == 0) ? 0.33333333f : (q <= 6 ? 0.05555556f : 0.02777778f);
+    }
+    return v;
+}
+
+struct FusedArgs {
+    Geo g;
+    const void* pop_in;
+    void* pop_out;
+    float* f32;
+    float* rho;
+    float* u;
+    float* v;
+    float* w;
+    const uint8_t* flags;
+    const int* link_off;
+    const uint8_t* link_meta;
+    const float2* link_w;
+    long long n_links;
+    const float* sponge;
+    int sponge_axis;
+    int has_links;
+    CollideParams cp;
+    unsigned* dev_err;
+};
+
+// Post-stream populations of one cell from the previous post-collision buffer:
+// pull + interpolated bounce-back on the cell's own links.
+template <int KIND>
+__device__ __forceinline__ void gather_cell(const FusedArgs& a, long long idx, int i, int j, int k,
+                                            uint8_t fl, float f[19]) {
+    using T = typename Store<KIND>::T;
+    const T* __restrict__ P = reinterpret_cast<const T*>(a.pop_in);
+    const Nbr n = make_nbr(a.g, i, j, k);
+    PullOne<KIND, 0>::run(P, a.g, n, i, j, k, idx, f);
+    if (fl & CF_LINK) {
+        long long l = a.link_off[idx];
+        for (int guard = 0; guard < 18; ++guard) {
+            if (l < 0 || l >= a.n_links) {
+                if (a.dev_err) atomicOr(a.dev_err, DEV_ERR_INDEX);
+                break;
+            }
+            const uint8_t meta = a.link_meta[l];
+            const int dir = meta & 31;
+            const int mode = (meta >> 5) & 3;
+            const float2 wt = a.link_w[l];
+            const int o = c_OPP[dir];
+            const float popp = load_dyn<KIND>(P, a.g.N, o, idx);
+            float val;
+            if (mode == 0) {
+                val = wt.x * popp + wt.y * load_dyn<KIND>(P, a.g.N, dir, idx);
+            } else if (mode == 1) {
+                const long long xff = idx - ((long long)c_CX[dir] * a.g.nynz + (long long)c_CY[dir] * a.g.nz + c_CZ[dir]);
+                val = wt.x * popp + wt.y * load_dyn<KIND>(P, a.g.N, o, xff);
+            } else {
+                val = popp;
+            }
+#pragma unroll
+            for (int q = 1; q < 19; ++q)
+                if (q == dir) f[q] = val;
+            if (meta & 0x80) break;
+            ++l;
+        }
+    }
+}
+
+// Post-stream populations of a flow-solid cell as the reference leaves them:
+// w_q after reset_solid when links exist, else the in-cell direction swap of
+// the pulled values (LBM_CHT.py _bounce_back_post_stream).
+template <int KIND>
+__device__ __forceinline__ void solid_cell(const FusedArgs& a, long long idx, int i, int j, int k, float f[19]) {
+    if (a.has_links) {
+#pragma unroll
+        for (int q = 0; q < 19; ++q) f[q] = wq(q);
+    } else {
+        using T = typename Store<KIND>::T;
+        const Nbr n = make_nbr(a.g, i, j, k);
+        float t[19];
+        PullOne<KIND, 0>::run(reinterpret_cast<const T*>(a.pop_in), a.g, n, i, j, k, idx, t);
+#pragma unroll
+        for (int q = 0; q < 19; ++q) f[q] = t[opp(q)];
+    }
+}
+
+template <int KIND, int MODE>
+__device__ __forceinline__ void collide_store(const FusedArgs& a, long long idx, int i, int j, int k,
+                                              float f[19]) {
+    using T = typename Store<KIND>::T;
+    float feq[19];
+    const Macro m = collide<MODE>(f, feq, a.cp);
+    if (a.sponge) {
+        const int c = a.sponge_axis == 0 ? i : (a.sponge_axis == 1 ? j : k);
+        const float sg = a.sponge[c];
+        if (sg > 0.f) {
+#pragma unroll
+            for (int q = 0; q < 19; ++q) f[q] = f[q] - sg * (f[q] - feq[q]);
+        }
+    }
+    T* __restrict__ Po = reinterpret_cast<T*>(a.pop_out);
+#pragma unroll
+    for (int q = 0; q < 19; ++q) Store<KIND>::store(Po + (long long)q * a.g.N + idx, q, f[q]);
+    if (a.rho) {
+        a.rho[idx] = m.rho; a.u[idx] = m.ux; a.v[idx] = m.uy; a.w[idx] = m.uz;
+    }
+}
+
+template <int KIND, int MODE>
+__global__ void __launch_bounds__(BLOCK) k_fused_step(const FusedArgs a) {
+    const long long idx = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (idx >= a.g.N) return;
+    const uint8_t fl = a.flags[idx];
+    int i, j, k;
+    if (fl & CF_SOLID) {
+        if (fl & (CF_DEFER | CF_WRITE_S)) {
+            cell_coords(a.g, idx, i, j, k);
+            float f[19];
+            solid_cell<KIND>(a, idx, i, j, k, f);
+#pragma unroll
+            for (int q = 0; q < 19; ++q) a.f32[q * a.g.N + idx] = f[q];
+        }
+        return;
+    }
+    cell_coords(a.g, idx, i, j, k);
+    float f[19];
+    gather_cell<KIND>(a, idx, i, j, k, fl, f);
+    if (fl & (CF_DEFER | CF_WRITE_S)) {
+#pragma unroll
+        for (int q = 0; q < 19; ++q) a.f32[q * a.g.N + idx] = f[q];
+        if (fl & CF_DEFER) return;
+    }
+    collide_store<KIND, MODE>(a, idx, i, j, k, f);
+}
+
+// Rebuild the post-stream FP32 populations (the reference's sim.f) of every
+// cell not on a deferred plane from the previous post-collision buffer.
+template <int KIND>
+__global__ void __launch_bounds__(BLOCK) k_materialize(const FusedArgs a) {
+    const long long idx = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (idx >= a.g.N) return;
+    const uint8_t fl = a.flags[idx];
+    if (fl & CF_DEFER) return;
+    int i, j, k;
+    cell_coords(a.g, idx, i, j, k);
+    float f[19];
+    if (fl & CF_SOLID) solid_cell<KIND>(a, idx, i, j, k, f);
+    else gather_cell<KIND>(a, idx, i, j, k, fl, f);
+#pragma unroll
+    for (int q = 0; q < 19; ++q) a.f32[q * a.g.N + idx] = f[q];
+}
+
+// Collide cells straight from the FP32 post-stream tensor: the whole grid at
+// start-up (prologue) or one inlet/outlet plane after its BC (plane mode).
+template <int KIND, int MODE>
+__global__ void __launch_bounds__(BLOCK) k_collide_from_f32(const FusedArgs a, int axis, int plane,
+                                                            int n1, int n2) {
+    const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    long long idx;
+    if (axis < 0) {
+        if (t >= a.g.N) return;
+        idx = t;
+    } else {
+        if (t >= (long long)n1 * n2) return;
+        const int pa = (int)(t / n2), pb = (int)(t - (t / n2) * n2);
+        idx = plane_flat(axis, plane, pa, pb, a.g.ny, a.g.nz);
+    }
+    if (a.flags[idx] & CF_SOLID) return;
+    int i, j, k;
+    cell_coords(a.g, idx, i, j, k);
+    float f[19];
+#pragma unroll
+    for (int q = 0; q < 19; ++q) f[q] = a.f32[q * a.g.N + idx];
+    collide_store<KIND, MODE>(a, idx, i, j, k, f);
+}
+
+// Pin solid cells: populations w_q in the given buffer (shifted => 0), macros (1,0,0,0).
+template <int KIND>
+__global__ void __launch_bounds__(BLOCK) k_pin_solid(const FusedArgs a) {
+    const long long idx = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (idx >= a.g.N) return;
+    if (!(a.flags[idx] & CF_SOLID)) return;
+    using T = typename Store<KIND>::T;
+    T* Po = reinterpret_cast<T*>(a.pop_out);
+#pragma unroll
+    for (int q = 0; q < 19; ++q) Store<KIND>::store(Po + (long long)q * a.g.N + idx, q, wq(q));
+    if (a.rho) { a.rho[idx] = 1.f; a.u[idx] = 0.f; a.v[idx] = 0.f; a.w[idx] = 0.f; }
+}
+
+int make_fused_args(const fc_lbm_step_args* s, FusedArgs& a) {
+    if (!s) return FC_ERR_ARG;
+    if (s->nx < 1 || s->ny < 1 || s->nz < 1) return FC_ERR_ARG;
+    if (s->storage < 0 || s->storage > 2 || s->collision < 0 || s->collision > 3) return FC_ERR_ARG;
+    a.g.nx = s->nx; a.g.ny = s->ny; a.g.nz = s->nz;
+    a.g.px = s->periodic[0] != 0; a.g.py = s->periodic[1] != 0; a.g.pz = s->periodic[2] != 0;
+    a.g.N = (long long)s->nx * s->ny * s->nz;
+    a.g.nynz = s->ny * s->nz;
+    a.pop_in = s->pop_in; a.pop_out = s->pop_out; a.f32 = s->f32;
+    a.rho = s->rho; a.u = s->u; a.v = s->v; a.w = s->w;
+    if (a.rho && (!a.u || !a.v || !a.w)) return FC_ERR_ARG;
+    a.flags = s->cell_flags;
+    a.link_off = s->link_off; a.link_meta = s->link_meta;
+    a.link_w = reinterpret_cast<const float2*>(s->link_w);
+    a.n_links = s->n_links;
+    a.sponge = s->sponge; a.sponge_axis = s->sponge_axis;
+    if (a.sponge && (a.sponge_axis < 0 || a.sponge_axis > 2)) return FC_ERR_ARG;
+    a.has_links = s->has_links;
+    a.cp.omega = s->omega; a.cp.omega_plus = s->omega_plus; a.cp.omega_minus = s->omega_minus;
+    for (int q = 0; q < 19; ++q) a.cp.S[q] = s->S[q];
+    a.cp.Cs_dx2 = s->Cs_dx2; a.cp.omega0 = s->omega0;
+    a.dev_err = s->dev_err;
+    if (!a.flags) return FC_ERR_ARG;
+    if (a.n_links > 0 && (!a.link_off || !a.link_meta || !a.link_w)) return FC_ERR_ARG;
+    return FC_OK;
+}
+
+template <template <int, int> class Launcher>
+int dispatch(int storage, int collision, const FusedArgs& a, cudaStream_t st, int x0, int x1, int x2, int x3) {
+#define FC_CASE(S, M) \
+    if (storage == S && collision == M) return Launcher<S, M>::go(a, st, x0, x1, x2, x3);
+    FC_CASE(ST_F32, CM_BGK) FC_CASE(ST_F32, CM_TRT) FC_CASE(ST_F32, CM_MRT) FC_CASE(ST_F32, CM_MRT_SMAG)
+    FC_CASE(ST_F16S, CM_BGK) FC_CASE(ST_F16S, CM_TRT) FC_CASE(ST_F16S, CM_MRT) FC_CASE(ST_F16S, CM_MRT_SMAG)
+    FC_CASE(ST_BF16S, CM_BGK) FC_CASE(ST_BF16S, CM_TRT) FC_CASE(ST_BF16S, CM_MRT) FC_CASE(ST_BF16S, CM_MRT_SMAG)
+#undef FC_CASE
+    return FC_ERR_ARG;
+}
+
+template <int S, int M>
+struct StepLauncher {
+    static int go(const FusedArgs& a, cudaStream_t st, int, int, int, int) {
+        k_fused_step<S, M><<<grid_for(a.g.N), BLOCK, 0, st>>>(a);
+        return launch_status();
+    }
+};
+template <int S, int M>
+struct CollideF32Launcher {
+    static int go(const FusedArgs& a, cudaStream_t st, int axis, int plane, int n1, int n2) {
+        const long long n = axis < 0 ? a.g.N : (long long)n1 * n2;
+        k_collide_from_f32<S, M><<<grid_for(n), BLOCK, 0, st>>>(a, axis, plane, n1, n2);
+        return launch_status();
+    }
+};
+
+}  // namespace
+
+// ============================================================================
+//  C ABI
+// ============================================================================
+extern "C" {
+
+int fc_abi_version(void) { return FC_ABI_VERSION; }
+
+static int check_collide_ptrs(const float* f, float* fp, float* r, float* u, float* v, float* w,
+                              const uint8_t* s, long long n) {
+    if (!f || !fp || !r || !u || !v || !w || !s || n < 0) return FC_ERR_ARG;
+    return FC_OK;
+}
+
+int fc_lbm_macro_collide_bgk(const float* f, float* f_post, float* rho, float* u, float* v, float* w,
+                             const uint8_t* solid, float omega, long long n_cells, void* stream) {
+    int rc = check_collide_ptrs(f, f_post, rho, u, v, w, solid, n_cells);
+    if (rc) return rc;
+    if (n_cells == 0) return FC_OK;
+    CollideParams p{}; p.omega = omega;
+    const float* S_dev = nullptr;
+    k_macro_collide<CM_BGK><<<grid_for(n_cells), BLOCK, 0, (cudaStream_t)stream>>>(f, f_post, rho, u, v, w, solid, p, S_dev, n_cells);
+    return launch_status();
+}
+
+int fc_lbm_macro_collide_trt(const float* f, float* f_post, float* rho, float* u, float* v, float* w,
+                             const uint8_t* solid, float omega_plus, float omega_minus, long long n_cells,
+                             void* stream) {
+    int rc = check_collide_ptrs(f, f_post, rho, u, v, w, solid, n_cells);
+    if (rc) return rc;
+    if (n_cells == 0) return FC_OK;
+    CollideParams p{}; p.omega_plus = omega_plus; p.omega_minus = omega_minus;
+    const float* S_dev = nullptr;
+    k_macro_collide<CM_TRT><<<grid_for(n_cells), BLOCK, 0, (cudaStream_t)stream>>>(f, f_post, rho, u, v, w, solid, p, S_dev, n_cells);
+    return launch_status();
+}
+
+int fc_lbm_macro_collide_mrt(const float* f, float* f_post, float* rho, float* u, float* v, float* w,
+                             const uint8_t* solid, const float* S_dev, long long n_cells, void* stream) {
+    int rc = check_collide_ptrs(f, f_post, rho, u, v, w, solid, n_cells);
+    if (rc) return rc;
+    if (!S_dev) return FC_ERR_ARG;
+    if (n_cells == 0) return FC_OK;
+    CollideParams p{};
+    k_macro_collide<CM_MRT><<<grid_for(n_cells), BLOCK, 0, (cudaStream_t)stream>>>(f, f_post, rho, u, v, w, solid, p, S_dev, n_cells);
+    return launch_status();
+}
+
+int fc_lbm_macro_collide_mrt_smag(const float* f, float* f_post, float* rho, float* u, float* v, float* w,
+                                  const uint8_t* solid, const float* S_dev, float Cs_dx2, float omega0,
+                                  long long n_cells, void* stream) {
+    int rc = check_collide_ptrs(f, f_post, rho, u, v, w, solid, n_cells);
+    if (rc) return rc;
+    if (!S_dev) return FC_ERR_ARG;
+    if (n_cells == 0) return FC_OK;
+    CollideParams p{};
+    p.Cs_dx2 = Cs_dx2; p.omega0 = omega0;
+    k_macro_collide<CM_MRT_SMAG><<<grid_for(n_cells), BLOCK, 0, (cudaStream_t)stream>>>(f, f_post, rho, u, v, w, solid, p, S_dev, n_cells);
+    return launch_status();
+}
+
+int fc_lbm_stream_pull(const float* f_in, float* f_out, int nx, int ny, int nz, int px, int py, int pz,
+                       void* stream) {
+    if (!f_in || !f_out || nx < 1 || ny < 1 || nz < 1) return FC_ERR_ARG;
+    if (f_in == f_out) return FC_ERR_ARG;
+    const long long N = (long long)nx * ny * nz;
+    k_stream_pull<<<grid_for(N), BLOCK, 0, (cudaStream_t)stream>>>(f_in, f_out, nx, ny, nz, px, py, pz);
+    return launch_status();
+}
+
+int fc_lbm_sponge(float* f, const float* rho, const float* u, const float* v, const float* w,
+                  const float* sigma, long long n_cells, void* stream) {
+    if (!f || !rho || !u || !v || !w || !sigma || n_cells < 0) return FC_ERR_ARG;
+    if (n_cells == 0) return FC_OK;
+    k_sponge<<<grid_for(n_cells), BLOCK, 0, (cudaStream_t)stream>>>(f, rho, u, v, w, sigma, n_cells);
+    return launch_status();
+}
+
+int fc_lbm_ibb(const float* f_post, float* f_stream, const int32_t* fluid_flat, const int32_t* dir_i,
+               const int32_t* dir_opp, const float* w1, const float* w2, const uint8_t* q_ge_half,
+               const int32_t* ff_flat, const uint8_t* ff_valid, long long n_links, long long n_cells,
+               unsigned* dev_err, void* stream) {
+    if (n_links < 0 || n_cells < 0) return FC_ERR_ARG;
+    if (n_links == 0) return FC_OK;
+    if (!f_post || !f_stream || !fluid_flat || !dir_i || !dir_opp || !w1 || !w2 || !q_ge_half ||
+        !ff_flat || !ff_valid)
+        return FC_ERR_ARG;
+    k_ibb_links<<<grid_for(n_links), BLOCK, 0, (cudaStream_t)stream>>>(
+        f_post, f_stream, fluid_flat, dir_i, dir_opp, w1, w2, q_ge_half, ff_flat, ff_valid, n_links,
+        n_cells, dev_err);
+    return launch_status();
+}
+
+int fc_lbm_reset_solid(float* f, const uint8_t* solid, long long n_cells, void* stream) {
+    if (!f || !solid || n_cells < 0) return FC_ERR_ARG;
+    if (n_cells == 0) return FC_OK;
+    k_reset_solid<<<grid_for(n_cells), BLOCK, 0, (cudaStream_t)stream>>>(f, solid, n_cells);
+    return launch_status();
+}
+
+static int plane_dims(int axis, int nx, int ny, int nz, int* n1, int* n2) {
+    if (axis == 0) { *n1 = ny; *n2 = nz; }
+    else if (axis == 1) { *n1 = nx; *n2 = nz; }
+    else if (axis == 2) { *n1 = nx; *n2 = ny; }
+    else return FC_ERR_ARG;
+    return FC_OK;
+}
+
+int fc_lbm_zou_he_bc(float* f, const uint8_t* solid, int nx, int ny, int nz, int axis, int plane_idx,
+                     int interior_idx, int bc_type, float u_in_lat, float rho_out_lat, int sign, void* stream) {
+    int n1, n2;
+    if (!f || !solid || nx < 1 || ny < 1 || nz < 1) return FC_ERR_ARG;
+    if (plane_dims(axis, nx, ny, nz, &n1, &n2)) return FC_ERR_ARG;
+    const int na = axis == 0 ? nx : (axis == 1 ? ny : nz);
+    if (plane_idx < 0 || plane_idx >= na || interior_idx < 0 || interior_idx >= na) return FC_ERR_ARG;
+    if (bc_type != 0 && bc_type != 1) return FC_ERR_ARG;
+    k_zou_he<<<grid_for((long long)n1 * n2), BLOCK, 0, (cudaStream_t)stream>>>(
+        f, solid, nx, ny, nz, axis, plane_idx, interior_idx, bc_type, u_in_lat, rho_out_lat, sign, n1, n2);
+    return launch_status();
+}
+
+long long fc_lbm_convective_workspace_bytes(int n1, int n2) {
+    if (n1 < 1 || n2 < 1) return -1;
+    const long long nb = ((long long)n1 * n2 + BLOCK - 1) / BLOCK;
+    return nb * (long long)(sizeof(double) + sizeof(int)) + 16;
+}
+
+int fc_lbm_convective_bc(float* f, const uint8_t* solid, int nx, int ny, int nz, int axis, int outlet_idx,
+                         int interior_idx, int unknown_cax, float rho_out_lat, int n1, int n2,
+                         void* workspace, long long workspace_bytes, void* stream) {
+    if (!f || !solid || !workspace || nx < 1 || ny < 1 || nz < 1) return FC_ERR_ARG;
+    int e1, e2;
+    if (plane_dims(axis, nx, ny, nz, &e1, &e2)) return FC_ERR_ARG;
+    if (e1 != n1 || e2 != n2) return FC_ERR_ARG;
+    const int na = axis == 0 ? nx : (axis == 1 ? ny : nz);
+    if (outlet_idx < 0 || outlet_idx >= na || interior_idx < 0 || interior_idx >= na) return FC_ERR_ARG;
+    if (unknown_cax != 1 && unknown_cax != -1) return FC_ERR_ARG;
+    if (workspace_bytes < fc_lbm_convective_workspace_bytes(n1, n2)) return FC_ERR_ARG;
+    if (reinterpret_cast<uintptr_t>(workspace) % 8 != 0) return FC_ERR_ARG;
+    const int nb = (int)grid_for((long long)n1 * n2);
+    double* part_rho = reinterpret_cast<double*>(workspace);
+    int* part_cnt = reinterpret_cast<int*>(part_rho + nb);
+    cudaStream_t st = (cudaStream_t)stream;
+    k_convective_pass1<<<nb, BLOCK, 0, st>>>(f, solid, nx, ny, nz, axis, outlet_idx, interior_idx, unknown_cax,
+                                             n1, n2, part_rho, part_cnt);
+    int rc = launch_status();
+    if (rc) return rc;
+    k_convective_pass2<<<nb, BLOCK, 0, st>>>(f, solid, nx, ny, nz, axis, outlet_idx, rho_out_lat, n1, n2,
+                                             part_rho, part_cnt, nb);
+    return launch_status();
+}
+
+int fc_lbm_fused_step(const fc_lbm_step_args* args, void* stream) {
+    FusedArgs a;
+    int rc = make_fused_args(args, a);
+    if (rc) return rc;
+    if (!a.pop_in || !a.pop_out || a.pop_in == a.pop_out) return FC_ERR_ARG;
+    return dispatch<StepLauncher>(args->storage, args->collision, a, (cudaStream_t)stream, 0, 0, 0, 0);
+}
+
+int fc_lbm_collide_from_f32(const fc_lbm_step_args* args, int axis, int plane_idx, void* stream) {
+    FusedArgs a;
+    int rc = make_fused_args(args, a);
+    if (rc) return rc;
+    if (!a.f32 || !a.pop_out) return FC_ERR_ARG;
+    int n1 = 0, n2 = 0;
+    if (axis >= 0) {
+        if (plane_dims(axis, a.g.nx, a.g.ny, a.g.nz, &n1, &n2)) return FC_ERR_ARG;
+        const int na = axis == 0 ? a.g.nx : (axis == 1 ? a.g.ny : a.g.nz);
+        if (plane_idx < 0 || plane_idx >= na) return FC_ERR_ARG;
+    }
+    return dispatch<CollideF32Launcher>(args->storage, args->collision, a, (cudaStream_t)stream, axis,
+                                        plane_idx, n1, n2);
+}
+
+int fc_lbm_materialize(const fc_lbm_step_args* args, void* stream) {
+    FusedArgs a;
+    int rc = make_fused_args(args, a);
+    if (rc) return rc;
+    if (!a.f32 || !a.pop_in) return FC_ERR_ARG;
+    cudaStream_t st = (cudaStream_t)stream;
+    switch (args->storage) {
+        case ST_F32: k_materialize<ST_F32><<<grid_for(a.g.N), BLOCK, 0, st>>>(a); break;
+        case ST_F16S: k_materialize<ST_F16S><<<grid_for(a.g.N), BLOCK, 0, st>>>(a); break;
+        default: k_materialize<ST_BF16S><<<grid_for(a.g.N), BLOCK, 0, st>>>(a); break;
+    }
+    return launch_status();
+}
+
+int fc_lbm_pin_solid(const fc_lbm_step_args* args, void* stream) {
+    FusedArgs a;
+    int rc = make_fused_args(args, a);
+    if (rc) return rc;
+    if (!a.pop_out) return FC_ERR_ARG;
+    cudaStream_t st = (cudaStream_t)stream;
+    switch (args->storage) {
+        case ST_F32: k_pin_solid<ST_F32><<<grid_for(a.g.N), BLOCK, 0, st>>>(a); break;
+        case ST_F16S: k_pin_solid<ST_F16S><<<grid_for(a.g.N), BLOCK, 0, st>>>(a); break;
+        default: k_pin_solid<ST_BF16S><<<grid_for(a.g.N), BLOCK, 0, st>>>(a); break;
+    }
+    return launch_status();
+}
+
+}  // extern "C"

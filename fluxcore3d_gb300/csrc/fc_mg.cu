@@ -1,0 +1,418 @@
+// fc_mg.cu -- geometric-multigrid kernels for the thermal advection-diffusion
+// operator (sm_103a), behind a C ABI.
+//
+// Operator (reference solver/nlevel_mg_cuda.py:417-507 and mg_kernels.cu:55-106):
+//   L(T)_c = diagL_c T_c - sum_n a_n,c T_n          (7-point, per-cell a_E..a_D)
+//   M(T)   = T + dt L(T)                             ("mop")
+// Ghost cells: the high face of every axis mirrors the cell below it; the low
+// face mirrors the cell above it except on the flow axis when the inlet sits at
+// index 0, where the cell itself is the ghost (mg_kernels.cu:37-44).
+//
+// Kernels: the reference pair (mop, jacobi) plus fused forms used by the
+// V-cycle: one Jacobi sweep in a single pass (x_out = x + invD (b - M x)),
+// the first sweep from a zero guess (x = invD b), residual + 2x mean
+// restriction, trilinear prolongation + damped correction + mask, and the
+// operator / hierarchy builders.  Reductions are FP64 with a fixed tree order.
+#include "fc_common.cuh"
+#include "../../include/fluxcore3d_gb300.h"
+
+using namespace fc;
+
+namespace {
+
+constexpr int BLOCK = 256;
+inline unsigned grid_for(long long n) { return (unsigned)((n + BLOCK - 1) / BLOCK); }
+
+struct Lvl {
+    int nx, ny, nz;
+    int ax, out_idx;
+};
+
+__device__ __forceinline__ int low_ghost(const Lvl& g, int axis) {
+    return (g.ax == axis && g.out_idx != 0) ? 0 : 1;
+}
+
+// neighbour indices with the operator's ghosting
+struct Nb7 {
+    long long c, e, w, n, s, u, d;
+};
+__device__ __forceinline__ Nb7 nb7(const Lvl& g, int i, int j, int k) {
+    const int iE = i < g.nx - 1 ? i + 1 : i - 1;
+    const int iW = i > 0 ? i - 1 : low_ghost(g, 0);
+    const int jN = j < g.ny - 1 ? j + 1 : j - 1;
+    const int jS = j > 0 ? j - 1 : low_ghost(g, 1);
+    const int kU = k < g.nz - 1 ? k + 1 : k - 1;
+    const int kD = k > 0 ? k - 1 : low_ghost(g, 2);
+    const long long nynz = (long long)g.ny * g.nz;
+    Nb7 n;
+    n.c = i * nynz + (long long)j * g.nz + k;
+    n.e = iE * nynz + (long long)j * g.nz + k;
+    n.w = iW * nynz + (long long)j * g.nz + k;
+    n.n = i * nynz + (long long)jN * g.nz + k;
+    n.s = i * nynz + (long long)jS * g.nz + k;
+    n.u = i * nynz + (long long)j * g.nz + kU;
+    n.d = i * nynz + (long long)j * g.nz + kD;
+    return n;
+}
+
+struct Coef {
+    const float *aE, *aW, *aN, *aS, *aU, *aD, *diagL;
+};
+
+template <typename T>
+__device__ __forceinline__ T apply_L(const Coef& a, const T* __restrict__ x, const Nb7& n, T xc) {
+    return (T)__ldg(a.diagL + n.c) * xc - (T)__ldg(a.aE + n.c) * x[n.e] - (T)__ldg(a.aW + n.c) * x[n.w] -
+           (T)__ldg(a.aN + n.c) * x[n.n] - (T)__ldg(a.aS + n.c) * x[n.s] - (T)__ldg(a.aU + n.c) * x[n.u] -
+           (T)__ldg(a.aD + n.c) * x[n.d];
+}
+
+__device__ __forceinline__ void coords(const Lvl& g, long long idx, int& i, int& j, int& k) {
+    const int nynz = g.ny * g.nz;
+    i = (int)(idx / nynz);
+    const int r = (int)(idx - (long long)i * nynz);
+    j = r / g.nz;
+    k = r - j * g.nz;
+}
+
+// ---- reference pair -------------------------------------------------------
+__global__ void __launch_bounds__(BLOCK) k_mop(const float* __restrict__ T, Coef a, float* __restrict__ Lo,
+                                               float dt, Lvl g) {
+    const long long idx = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (idx >= (long long)g.nx * g.ny * g.nz) return;
+    int i, j, k;
+    coords(g, idx, i, j, k);
+    const Nb7 n = nb7(g, i, j, k);
+    const float tc = T[idx];
+    Lo[idx] = tc + dt * apply_L<float>(a, T, n, tc);
+}
+
+__global__ void __launch_bounds__(BLOCK) k_jacobi(float* __restrict__ x, const float* __restrict__ b,
+                                                  const float* __restrict__ Lo, const float* __restrict__ inv,
+                                                  long long n) {
+    const long long idx = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (idx >= n) return;
+    x[idx] += inv[idx] * (b[idx] - Lo[idx]);
+}
+
+// L(T) = (M(T) - T) / dt, evaluated the way the reference's L_apply_fine does
+__global__ void __launch_bounds__(BLOCK) k_apply_L(const float* __restrict__ T, Coef a, float* __restrict__ out,
+                                                   float dt, Lvl g) {
+    const long long idx = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (idx >= (long long)g.nx * g.ny * g.nz) return;
+    int i, j, k;
+    coords(g, idx, i, j, k);
+    const Nb7 n = nb7(g, i, j, k);
+    const float tc = T[idx];
+    const float lo = tc + dt * apply_L<float>(a, T, n, tc);
+    out[idx] = (lo - tc) / dt;
+}
+
+// ---- fused V-cycle pieces ------------------------------------------------
+__global__ void __launch_bounds__(BLOCK) k_smooth(const float* __restrict__ x, float* __restrict__ xo,
+                                                  const float* __restrict__ b, const float* __restrict__ inv,
+                                                  Coef a, float dt, Lvl g) {
+    const long long idx = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (idx >= (long long)g.nx * g.ny * g.nz) return;
+    int i, j, k;
+    coords(g, idx, i, j, k);
+    const Nb7 n = nb7(g, i, j, k);
+    const float tc = x[idx];
+    const float lo = tc + dt * apply_L<float>(a, x, n, tc);
+    xo[idx] = tc + __ldg(inv + idx) * (__ldg(b + idx) - lo);
+}
+
+__global__ void __launch_bounds__(BLOCK) k_smooth_zero(float* __restrict__ xo, const float* __restrict__ b,
+                                                       const float* __restrict__ inv, long long n) {
+    const long long idx = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (idx >= n) return;
+    xo[idx] = 0.f + inv[idx] * (b[idx] - 0.f);
+}
+
+// coarse b = mean over each 2x2x2 block of r = mask * (b - M x); fine cells
+// beyond the even-cropped extent do not contribute (view(...).mean semantics)
+__global__ void __launch_bounds__(BLOCK) k_residual_restrict(const float* __restrict__ x, const float* __restrict__ b,
+                                                             const float* __restrict__ mask, Coef a, float dt, Lvl g,
+                                                             float* __restrict__ bc, int cx, int cy, int cz) {
+    const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= (long long)cx * cy * cz) return;
+    const int ic = (int)(t / ((long long)cy * cz));
+    const int rr = (int)(t - (long long)ic * cy * cz);
+    const int jc = rr / cz, kc = rr - (rr / cz) * cz;
+    float s = 0.f;
+#pragma unroll
+    for (int di = 0; di < 2; ++di)
+#pragma unroll
+        for (int dj = 0; dj < 2; ++dj)
+#pragma unroll
+            for (int dk = 0; dk < 2; ++dk) {
+                const int i = 2 * ic + di, j = 2 * jc + dj, k = 2 * kc + dk;
+                const Nb7 n = nb7(g, i, j, k);
+                const float tc = x[n.c];
+                const float lo = tc + dt * apply_L<float>(a, x, n, tc);
+                s += (__ldg(b + n.c) - lo) * __ldg(mask + n.c);
+            }
+    bc[t] = s * 0.125f;
+}
+
+// trilinear (align_corners = False) source coordinate of fine index i
+__device__ __forceinline__ void src_coord(int i, int nf, int nc, int& i0, int& i1, float& l1) {
+    const float scale = (float)nc / (float)nf;
+    float s = scale * ((float)i + 0.5f) - 0.5f;
+    if (s < 0.f) s = 0.f;
+    i0 = (int)s;
+    if (i0 > nc - 1) i0 = nc - 1;
+    i1 = i0 + (i0 < nc - 1 ? 1 : 0);
+    l1 = s - (float)i0;
+}
+
+__global__ void __launch_bounds__(BLOCK) k_prolong_correct(float* __restrict__ x, const float* __restrict__ xc,
+                                                           const float* __restrict__ mask, int nx, int ny, int nz,
+                                                           int cx, int cy, int cz, float alpha) {
+    const long long idx = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (idx >= (long long)nx * ny * nz) return;
+    const int i = (int)(idx / ((long long)ny * nz));
+    const int r = (int)(idx - (long long)i * ny * nz);
+    const int j = r / nz, k = r - (r / nz) * nz;
+    int i0, i1, j0, j1, k0, k1;
+    float li, lj, lk;
+    src_coord(i, nx, cx, i0, i1, li);
+    src_coord(j, ny, cy, j0, j1, lj);
+    src_coord(k, nz, cz, k0, k1, lk);
+    const float hi = 1.f - li, hj = 1.f - lj, hk = 1.f - lk;
+    auto X = [&](int a, int b, int c) { return __ldg(xc + ((long long)a * cy + b) * cz + c); };
+    const float e = hi * (hj * (hk * X(i0, j0, k0) + lk * X(i0, j0, k1)) + lj * (hk * X(i0, j1, k0) + lk * X(i0, j1, k1))) +
+                    li * (hj * (hk * X(i1, j0, k0) + lk * X(i1, j0, k1)) + lj * (hk * X(i1, j1, k0) + lk * X(i1, j1, k1)));
+    x[idx] = (x[idx] + alpha * e) * __ldg(mask + idx);
+}
+
+// per-block partial sums of (w * (b - M x))^2 in FP64, w = mask or 1
+__global__ void __launch_bounds__(BLOCK) k_residual_sq(const float* __restrict__ x, const float* __restrict__ b,
+                                                       const float* __restrict__ mask, Coef a, float dt, Lvl g,
+                                                       float* __restrict__ r_out, double* __restrict__ part) {
+    __shared__ double sh[BLOCK];
+    const long long idx = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    double v = 0.0;
+    if (idx < (long long)g.nx * g.ny * g.nz) {
+        int i, j, k;
+        coords(g, idx, i, j, k);
+        const Nb7 n = nb7(g, i, j, k);
+        const float tc = x[idx];
+        const float lo = tc + dt * apply_L<float>(a, x, n, tc);
+        float r = __ldg(b + idx) - lo;
+        if (mask) r *= __ldg(mask + idx);
+        if (r_out) r_out[idx] = r;
+        v = (double)r * (double)r;
+    }
+    sh[threadIdx.x] = v;
+    __syncthreads();
+    for (int s = BLOCK / 2; s > 0; s >>= 1) {
+        if ((int)threadIdx.x < s) sh[threadIdx.x] += sh[threadIdx.x + s];
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) part[blockIdx.x] = sh[0];
+}
+
+// sum of partials in fixed order by one block
+__global__ void __launch_bounds__(BLOCK) k_sum_partials(const double* __restrict__ part, int n, double* __restrict__ out) {
+    __shared__ double sh[BLOCK];
+    double v = 0.0;
+    for (int p = threadIdx.x; p < n; p += BLOCK) v += part[p];
+    sh[threadIdx.x] = v;
+    __syncthreads();
+    for (int s = BLOCK / 2; s > 0; s >>= 1) {
+        if ((int)threadIdx.x < s) sh[threadIdx.x] += sh[threadIdx.x + s];
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) *out = sh[0];
+}
+
+// ---- operator / hierarchy builders ---------------------------------------
+// Harmonic-mean face conductivity, diffusion s k_f /(rho cp dx^2), first-order
+// upwind convection s max(+-u, 0)/dx (nlevel_mg_cuda.py:417-507), evaluated as
+// separately rounded FP32 operations in the reference's order.
+__global__ void __launch_bounds__(BLOCK) k_build_coeffs(const float* __restrict__ kk, const float* __restrict__ rcp,
+                                                        const float* __restrict__ u, const float* __restrict__ v,
+                                                        const float* __restrict__ w, Lvl g, float cd, float ca,
+                                                        float* aE, float* aW, float* aN, float* aS, float* aU,
+                                                        float* aD, float* diagL) {
+    const long long idx = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (idx >= (long long)g.nx * g.ny * g.nz) return;
+    int i, j, k;
+    coords(g, idx, i, j, k);
+    const Nb7 n = nb7(g, i, j, k);
+    const float kc = kk[idx];
+    const float inv_rcp = __fdiv_rn(1.0f, __fadd_rn(rcp[idx], 1e-30f));
+    auto hm = [&](long long o) {
+        const float kn = kk[o];
+        return __fdiv_rn(__fmul_rn(__fmul_rn(2.0f, kc), kn), __fadd_rn(__fadd_rn(kc, kn), 1e-30f));
+    };
+    auto dif = [&](long long o) { return __fmul_rn(__fmul_rn(cd, hm(o)), inv_rcp); };
+    const float uc = u[idx], vc = v[idx], wc = w[idx];
+    const float upx = fmaxf(uc, 0.f), umx = fmaxf(-uc, 0.f);
+    const float upy = fmaxf(vc, 0.f), umy = fmaxf(-vc, 0.f);
+    const float upz = fmaxf(wc, 0.f), umz = fmaxf(-wc, 0.f);
+    const float e = __fadd_rn(dif(n.e), __fmul_rn(ca, umx));
+    const float ww = __fadd_rn(dif(n.w), __fmul_rn(ca, upx));
+    const float no = __fadd_rn(dif(n.n), __fmul_rn(ca, umy));
+    const float so = __fadd_rn(dif(n.s), __fmul_rn(ca, upy));
+    const float up = __fadd_rn(dif(n.u), __fmul_rn(ca, umz));
+    const float dn = __fadd_rn(dif(n.d), __fmul_rn(ca, upz));
+    aE[idx] = e; aW[idx] = ww; aN[idx] = no; aS[idx] = so; aU[idx] = up; aD[idx] = dn;
+    diagL[idx] = __fadd_rn(__fadd_rn(__fadd_rn(__fadd_rn(__fadd_rn(e, ww), no), so), up), dn);
+}
+
+// 2x mean restriction of a field (even-cropped); mask variant thresholds at 0.999
+__global__ void __launch_bounds__(BLOCK) k_restrict_mean(const float* __restrict__ src, int nx, int ny, int nz,
+                                                         float* __restrict__ dst, int cx, int cy, int cz, int as_mask) {
+    const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= (long long)cx * cy * cz) return;
+    const int ic = (int)(t / ((long long)cy * cz));
+    const int rr = (int)(t - (long long)ic * cy * cz);
+    const int jc = rr / cz, kc = rr - (rr / cz) * cz;
+    float s = 0.f;
+    for (int di = 0; di < 2; ++di)
+        for (int dj = 0; dj < 2; ++dj)
+            for (int dk = 0; dk < 2; ++dk)
+                s += src[((long long)(2 * ic + di) * ny + (2 * jc + dj)) * nz + (2 * kc + dk)];
+    const float m = s * 0.125f;
+    dst[t] = as_mask ? (m >= 0.999f ? 1.f : 0.f) : m;
+}
+
+__global__ void __launch_bounds__(BLOCK) k_inv_diag(const float* __restrict__ diagL, const float* __restrict__ mask,
+                                                    float* __restrict__ inv, float dt, float omega, long long n) {
+    const long long idx = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (idx >= n) return;
+    float d = 1.0f + dt * diagL[idx];
+    d = fmaxf(d, 1e-12f);
+    inv[idx] = (omega / d) * mask[idx];
+}
+
+int level_ok(const Lvl& g) {
+    if (g.nx < 2 || g.ny < 2 || g.nz < 2) return FC_ERR_ARG;
+    if (g.ax < 0 || g.ax > 2) return FC_ERR_ARG;
+    return FC_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+int fc_mg_mop(const float* T, const float* aE, const float* aW, const float* aN, const float* aS, const float* aU,
+              const float* aD, const float* diagL, float* Lo, float dt, int nx, int ny, int nz, int ax, int out_idx,
+              void* stream) {
+    Lvl g{nx, ny, nz, ax, out_idx};
+    if (level_ok(g) || !T || !Lo || !aE || !aW || !aN || !aS || !aU || !aD || !diagL) return FC_ERR_ARG;
+    Coef a{aE, aW, aN, aS, aU, aD, diagL};
+    k_mop<<<grid_for((long long)nx * ny * nz), BLOCK, 0, (cudaStream_t)stream>>>(T, a, Lo, dt, g);
+    return launch_status();
+}
+
+int fc_mg_jacobi(float* x, const float* b, const float* Lo, const float* inv_diagM, long long n, void* stream) {
+    if (!x || !b || !Lo || !inv_diagM || n < 0) return FC_ERR_ARG;
+    if (n == 0) return FC_OK;
+    k_jacobi<<<grid_for(n), BLOCK, 0, (cudaStream_t)stream>>>(x, b, Lo, inv_diagM, n);
+    return launch_status();
+}
+
+int fc_mg_apply_L(const float* T, const float* aE, const float* aW, const float* aN, const float* aS,
+                  const float* aU, const float* aD, const float* diagL, float* out, float dt, int nx, int ny, int nz,
+                  int ax, int out_idx, void* stream) {
+    Lvl g{nx, ny, nz, ax, out_idx};
+    if (level_ok(g) || !T || !out || dt == 0.f) return FC_ERR_ARG;
+    Coef a{aE, aW, aN, aS, aU, aD, diagL};
+    k_apply_L<<<grid_for((long long)nx * ny * nz), BLOCK, 0, (cudaStream_t)stream>>>(T, a, out, dt, g);
+    return launch_status();
+}
+
+int fc_mg_smooth(const float* x_in, float* x_out, const float* b, const float* inv_diagM, const float* aE,
+                 const float* aW, const float* aN, const float* aS, const float* aU, const float* aD,
+                 const float* diagL, float dt, int nx, int ny, int nz, int ax, int out_idx, void* stream) {
+    Lvl g{nx, ny, nz, ax, out_idx};
+    if (level_ok(g) || !x_in || !x_out || x_in == x_out || !b || !inv_diagM) return FC_ERR_ARG;
+    Coef a{aE, aW, aN, aS, aU, aD, diagL};
+    k_smooth<<<grid_for((long long)nx * ny * nz), BLOCK, 0, (cudaStream_t)stream>>>(x_in, x_out, b, inv_diagM, a, dt, g);
+    return launch_status();
+}
+
+int fc_mg_smooth_from_zero(float* x_out, const float* b, const float* inv_diagM, long long n, void* stream) {
+    if (!x_out || !b || !inv_diagM || n < 0) return FC_ERR_ARG;
+    if (n == 0) return FC_OK;
+    k_smooth_zero<<<grid_for(n), BLOCK, 0, (cudaStream_t)stream>>>(x_out, b, inv_diagM, n);
+    return launch_status();
+}
+
+int fc_mg_residual_restrict(const float* x, const float* b, const float* mask, const float* aE, const float* aW,
+                            const float* aN, const float* aS, const float* aU, const float* aD, const float* diagL,
+                            float dt, int nx, int ny, int nz, int ax, int out_idx, float* b_coarse, int cx, int cy,
+                            int cz, void* stream) {
+    Lvl g{nx, ny, nz, ax, out_idx};
+    if (level_ok(g) || !x || !b || !mask || !b_coarse) return FC_ERR_ARG;
+    if (cx != nx / 2 || cy != ny / 2 || cz != nz / 2 || cx < 1 || cy < 1 || cz < 1) return FC_ERR_ARG;
+    Coef a{aE, aW, aN, aS, aU, aD, diagL};
+    k_residual_restrict<<<grid_for((long long)cx * cy * cz), BLOCK, 0, (cudaStream_t)stream>>>(
+        x, b, mask, a, dt, g, b_coarse, cx, cy, cz);
+    return launch_status();
+}
+
+int fc_mg_prolong_correct(float* x, const float* x_coarse, const float* mask, int nx, int ny, int nz, int cx,
+                          int cy, int cz, float alpha, void* stream) {
+    if (!x || !x_coarse || !mask || nx < 1 || ny < 1 || nz < 1 || cx < 1 || cy < 1 || cz < 1) return FC_ERR_ARG;
+    k_prolong_correct<<<grid_for((long long)nx * ny * nz), BLOCK, 0, (cudaStream_t)stream>>>(
+        x, x_coarse, mask, nx, ny, nz, cx, cy, cz, alpha);
+    return launch_status();
+}
+
+long long fc_mg_reduce_workspace_bytes(long long n) {
+    if (n < 0) return -1;
+    return (long long)(grid_for(n) + 1) * (long long)sizeof(double);
+}
+
+int fc_mg_residual_norm2(const float* x, const float* b, const float* mask, const float* aE, const float* aW,
+                         const float* aN, const float* aS, const float* aU, const float* aD, const float* diagL,
+                         float dt, int nx, int ny, int nz, int ax, int out_idx, float* r_out, void* workspace,
+                         long long workspace_bytes, double* result, void* stream) {
+    Lvl g{nx, ny, nz, ax, out_idx};
+    const long long n = (long long)nx * ny * nz;
+    if (level_ok(g) || !x || !b || !workspace || !result) return FC_ERR_ARG;
+    if (workspace_bytes < fc_mg_reduce_workspace_bytes(n)) return FC_ERR_ARG;
+    Coef a{aE, aW, aN, aS, aU, aD, diagL};
+    double* part = reinterpret_cast<double*>(workspace);
+    const unsigned nb = grid_for(n);
+    cudaStream_t st = (cudaStream_t)stream;
+    k_residual_sq<<<nb, BLOCK, 0, st>>>(x, b, mask, a, dt, g, r_out, part);
+    int rc = launch_status();
+    if (rc) return rc;
+    k_sum_partials<<<1, BLOCK, 0, st>>>(part, (int)nb, result);
+    return launch_status();
+}
+
+int fc_mg_build_coeffs(const float* k, const float* rho_cp, const float* u, const float* v, const float* w, int nx,
+                       int ny, int nz, int ax, int out_idx, float dx, float s, float* aE, float* aW, float* aN,
+                       float* aS, float* aU, float* aD, float* diagL, void* stream) {
+    Lvl g{nx, ny, nz, ax, out_idx};
+    if (level_ok(g) || !k || !rho_cp || !u || !v || !w || !aE || !aW || !aN || !aS || !aU || !aD || !diagL)
+        return FC_ERR_ARG;
+    const float cd = (float)((double)s / ((double)dx * (double)dx));
+    const float ca = (float)((double)s / (double)dx);
+    k_build_coeffs<<<grid_for((long long)nx * ny * nz), BLOCK, 0, (cudaStream_t)stream>>>(
+        k, rho_cp, u, v, w, g, cd, ca, aE, aW, aN, aS, aU, aD, diagL);
+    return launch_status();
+}
+
+int fc_mg_restrict_mean(const float* src, int nx, int ny, int nz, float* dst, int as_mask, void* stream) {
+    const int cx = nx / 2, cy = ny / 2, cz = nz / 2;
+    if (!src || !dst || cx < 1 || cy < 1 || cz < 1) return FC_ERR_ARG;
+    k_restrict_mean<<<grid_for((long long)cx * cy * cz), BLOCK, 0, (cudaStream_t)stream>>>(src, nx, ny, nz, dst, cx, cy,
+                                                                                            cz, as_mask);
+    return launch_status();
+}
+
+int fc_mg_inv_diag(const float* diagL, const float* mask, float* inv_diagM, float dt, float omega, long long n,
+                   void* stream) {
+    if (!diagL || !mask || !inv_diagM || n < 0) return FC_ERR_ARG;
+    if (n == 0) return FC_OK;
+    k_inv_diag<<<grid_for(n), BLOCK, 0, (cudaStream_t)stream>>>(diagL, mask, inv_diagM, dt, omega, n);
+    return launch_status();
+}
+
+}  // extern "C"

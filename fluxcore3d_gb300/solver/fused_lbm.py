@@ -1,0 +1,282 @@
+"""Fused step engine behind LBMCUDAUpgrade.patch(sim).step.
+
+State kept between steps
+------------------------
+The reference stores post-stream populations S_k in `sim.f` and recollides
+them at the start of every step.  This engine stores the post-collision
+populations P_{k+1} = C(S_k) instead (two ping-pong buffers, FP32 or FP16/BF16
+shifted by w_q) so that one pass per step can pull, bounce back, collide and
+store: step k reads P_k and writes P_{k+1}.  S_k is not stored; `sync_f()`
+rebuilds it into `sim.f` from P_k on demand.
+
+Observable behaviour compared with the reference step (solver/lbm_cuda_ext.py:445-517)
+  - sim.rho/u/v/wv after step k hold the macros of S_{k-1}, exactly as in the
+    reference (its collide writes the pre-collision macros).  They are written
+    every step unless `cfg.macro_stride = s > 1`, in which case only the
+    macros needed after steps k with (k-1) % s == 0 are written (the cadence of
+    a monitor that reads every s steps starting after the first).  The macro
+    tensors are double-buffered, so the attributes are rebound each step.
+  - sim.f is only current after `sim.sync_f()` (and on inlet/outlet planes,
+    which the plane BCs update in place every step).
+  - The collision of step k+1 happens inside step k, so parameters changed on
+    the solver object between steps take effect one step later; call
+    `sim._fc.invalidate()` after editing sim.f or the collision parameters.
+"""
+from __future__ import annotations
+
+import torch
+
+from .. import _lib
+from .._lib import StepArgs
+from .._torch import ptr, stream_ptr
+from .face_roles import periodic_flags, resolve_face_roles, _face_ax_idx_fsign
+
+CF_SOLID, CF_LINK, CF_DEFER, CF_WRITE_S = 1, 2, 4, 8
+STORAGE = {"fp32": 0, "float32": 0, "f32": 0, "fp16": 1, "float16": 1, "f16": 1, "bf16": 2, "bfloat16": 2}
+STORAGE_DTYPE = {0: torch.float32, 1: torch.float16, 2: torch.bfloat16}
+COLLISION = {"bgk": 0, "trt": 1, "mrt": 2, "mrt_smag": 3}
+_CX = (0, 1, -1, 0, 0, 0, 0, 1, 1, -1, -1, 1, 1, -1, -1, 0, 0, 0, 0)
+_CY = (0, 0, 0, 1, -1, 0, 0, 1, -1, 1, -1, 0, 0, 0, 0, 1, 1, -1, -1)
+_CZ = (0, 0, 0, 0, 0, 1, -1, 0, 0, 0, 0, 1, -1, 1, -1, 1, -1, 1, -1)
+_OPP = (0, 2, 1, 4, 3, 6, 5, 10, 9, 8, 7, 14, 13, 12, 11, 18, 17, 16, 15)
+
+
+def build_link_table(ibb, solid_flow_u8: torch.Tensor, nx: int, ny: int, nz: int):
+    """Per-cell interpolated-bounce-back table from the reference's link-major IBBData.
+
+    Returns (link_off[N] int32, link_meta[L] uint8, link_w[L,2] float32, link cells mask).
+    Links are grouped by fluid cell (sorted by cell, then direction); meta packs
+    dir | mode << 5 | last << 7 with mode 0 (q >= 1/2), 1 (q < 1/2 with a second
+    fluid node x_f - c_dir), 2 (q < 1/2 without one: plain bounce-back).
+    Links whose fluid cell is a flow solid are dropped: the reference resets
+    those cells right after the bounce-back pass.
+    """
+    dev = solid_flow_u8.device
+    N = nx * ny * nz
+    nynz = ny * nz
+    ff = ibb.fluid_flat.to(device=dev, dtype=torch.int64).reshape(-1)
+    d = ibb.dir_i.to(device=dev, dtype=torch.int64).reshape(-1)
+    do = ibb.dir_opp.to(device=dev, dtype=torch.int64).reshape(-1)
+    ge = ibb.q_ge_half.to(device=dev).reshape(-1).bool()
+    fv = ibb.ff_valid.to(device=dev).reshape(-1).bool()
+    fff = ibb.ff_flat.to(device=dev, dtype=torch.int64).reshape(-1)
+    w1 = ibb.w_i.to(device=dev, dtype=torch.float32).reshape(-1)
+    w2 = ibb.w_second.to(device=dev, dtype=torch.float32).reshape(-1)
+    if ff.numel() and (int(ff.min()) < 0 or int(ff.max()) >= N):
+        raise ValueError("IBB fluid_flat index out of range")
+    if d.numel() and (int(d.min()) < 1 or int(d.max()) > 18):
+        raise ValueError("IBB dir_i must lie in 1..18")
+    opp = torch.tensor(_OPP, device=dev)
+    if not torch.equal(opp[d], do):
+        raise ValueError("IBB dir_opp is not the opposite of dir_i")
+    cxyz = torch.tensor([[_CX[q] * nynz + _CY[q] * nz + _CZ[q]] for q in range(19)], device=dev).reshape(-1)
+    need_ff = (~ge) & fv
+    if need_ff.any() and not torch.equal(fff[need_ff], ff[need_ff] - cxyz[d[need_ff]]):
+        raise ValueError("IBB ff_flat must be the cell x_f - c_dir for valid second nodes")
+    keep = solid_flow_u8.reshape(-1)[ff] == 0
+    ff, d, ge, fv, w1, w2 = ff[keep], d[keep], ge[keep], fv[keep], w1[keep], w2[keep]
+    key = ff * 32 + d
+    if key.numel() != torch.unique(key).numel():
+        raise ValueError("IBB links repeat a (cell, direction) pair")
+    order = torch.argsort(key)
+    ff, d, ge, fv, w1, w2 = ff[order], d[order], ge[order], fv[order], w1[order], w2[order]
+    mode = torch.where(ge, 0, torch.where(fv, 1, 2))
+    L = ff.numel()
+    last = torch.ones(L, dtype=torch.bool, device=dev)
+    if L > 1:
+        last[:-1] = ff[1:] != ff[:-1]
+    first = torch.ones(L, dtype=torch.bool, device=dev)
+    if L > 1:
+        first[1:] = ff[1:] != ff[:-1]
+    link_off = torch.full((N,), -1, dtype=torch.int32, device=dev)
+    pos = torch.arange(L, device=dev, dtype=torch.int32)
+    link_off[ff[first]] = pos[first]
+    meta = (d | (mode << 5) | (last.to(torch.int64) << 7)).to(torch.uint8)
+    link_w = torch.stack([w1, w2], dim=1).contiguous()
+    has = torch.zeros(N, dtype=torch.bool, device=dev)
+    has[ff] = True
+    return link_off, meta.contiguous(), link_w, has
+
+
+class FusedLBM:
+    def __init__(self, sim):
+        self.sim = sim
+        cfg = sim.cfg
+        dev = sim.device
+        nx, ny, nz = sim.nx, sim.ny, sim.nz
+        self.N = N = nx * ny * nz
+        self.storage = STORAGE[str(getattr(cfg, "lbm_storage", "fp32")).lower()]
+        self.storage_name = {0: "fp32", 1: "fp16-shifted", 2: "bf16-shifted"}[self.storage]
+        mode = getattr(cfg, "collision", "bgk").lower()
+        self.collision = COLLISION.get(mode, 0)
+        self.macro_stride = max(1, int(getattr(cfg, "macro_stride", 1)))
+
+        solid = sim._solid_u8.reshape(N)
+        flags = solid.clone()
+        # links
+        self.has_links = bool(getattr(sim, "ibb_data", None) is not None and int(sim.ibb_data.n_links) > 0)
+        if self.has_links:
+            self.link_off, self.link_meta, self.link_w, has = build_link_table(sim.ibb_data, solid, nx, ny, nz)
+            flags |= has.to(torch.uint8) * CF_LINK
+            self.n_links = int(self.link_meta.numel())
+        else:
+            self.link_off = self.link_meta = self.link_w = None
+            self.n_links = 0
+        # inlet/outlet planes are finished by the plane BC kernels after the fused pass
+        f3 = flags.view(nx, ny, nz)
+        self.planes = []
+        for face, role in resolve_face_roles(cfg).items():
+            if role not in ("inlet", "outlet"):
+                continue
+            ax, pidx, _ = _face_ax_idx_fsign(sim, face)
+            iidx = pidx - 1 if pidx > 0 else 1
+            sl = [slice(None)] * 3
+            sl[ax] = pidx
+            f3[tuple(sl)] |= CF_DEFER
+            sl[ax] = iidx
+            f3[tuple(sl)] |= CF_WRITE_S
+            self.planes.append((ax, pidx))
+        self.flags = flags.contiguous()
+        # sponge: sigma must be a profile along one axis
+        self.sponge = None
+        self.sponge_axis = 0
+        sig = getattr(sim, "_sponge_sigma", None)
+        if int(getattr(cfg, "sponge_length", 0)) > 0 and sig is not None:
+            ax = int(getattr(sim, "_sponge_axis", 0))
+            prof = sig.to(torch.float32).movedim(ax, 0).reshape(sig.shape[ax], -1)
+            if not torch.equal(prof, prof[:, :1].expand_as(prof)):
+                raise NotImplementedError("sponge sigma must be constant on planes normal to the sponge axis")
+            self.sponge = prof[:, 0].contiguous().to(dev)
+            self.sponge_axis = ax
+        # buffers
+        sdt = STORAGE_DTYPE[self.storage]
+        self.P = [torch.empty((19, N), dtype=sdt, device=dev) for _ in range(2)]
+        self.M = [[torch.empty(N, dtype=torch.float32, device=dev) for _ in range(4)] for _ in range(2)]
+        self.dev_err = torch.zeros(1, dtype=torch.int32, device=dev)
+        self.periodic = periodic_flags(cfg)
+        self.k = 0          # steps taken since priming
+        self.cur = 0        # P[cur] holds the latest post-collision populations
+        self.primed = False
+        self.args = StepArgs()
+        self._fill_static_args()
+
+    # -- argument block ------------------------------------------------------
+    def _fill_static_args(self):
+        sim, a = self.sim, self.args
+        a.storage = self.storage
+        a.collision = self.collision
+        a.nx, a.ny, a.nz = sim.nx, sim.ny, sim.nz
+        for d in range(3):
+            a.periodic[d] = int(self.periodic[d])
+        a.f32 = ptr(sim.f)
+        a.cell_flags = ptr(self.flags)
+        a.link_off = ptr(self.link_off)
+        a.link_meta = ptr(self.link_meta)
+        a.link_w = ptr(self.link_w)
+        a.n_links = self.n_links
+        a.sponge = ptr(self.sponge)
+        a.sponge_axis = self.sponge_axis
+        a.has_links = int(self.has_links)
+        a.dev_err = ptr(self.dev_err)
+        self.refresh_params()
+
+    def refresh_params(self):
+        """Re-read the collision parameters from the solver object."""
+        sim, a = self.sim, self.args
+        a.omega = float(getattr(sim, "omega", 1.0))
+        a.omega_plus = float(getattr(sim, "omega_plus", a.omega))
+        a.omega_minus = float(getattr(sim, "omega_minus", a.omega)) if hasattr(sim, "omega_minus") else 1.0
+        S = getattr(sim, "_mrt_S", None)
+        vals = [float(x) for x in S.tolist()] if S is not None else [0.0] * 19
+        for q in range(19):
+            a.S[q] = vals[q]
+        a.Cs_dx2 = float(getattr(sim, "_cuda_Cs_dx2", None) or 0.0)
+        a.omega0 = float(getattr(sim, "_cuda_omega0", None) or a.omega_plus)
+
+    def _set_macros(self, m):
+        a = self.args
+        if m is None:
+            a.rho = a.u = a.v = a.w = None
+        else:
+            a.rho, a.u, a.v, a.w = (ptr(t) for t in m)
+
+    def _expose(self, m):
+        sim = self.sim
+        shp = (sim.nx, sim.ny, sim.nz)
+        sim.rho, sim.u, sim.v, sim.wv = (t.view(shp) for t in m)
+
+    def invalidate(self):
+        """Forget the stored post-collision state; the next step re-primes from sim.f."""
+        self.primed = False
+
+    # -- stepping --------------------------------------------------------------
+    def _prime(self):
+        """P_1 = C(S_0) from sim.f; macros of S_0; solid cells pinned in both buffers."""
+        sim, a = self.sim, self.args
+        self.refresh_params()
+        if sim.f.dtype != torch.float32 or not sim.f.is_contiguous():
+            raise RuntimeError("sim.f must be a contiguous float32 tensor")
+        a.f32 = ptr(sim.f)
+        st = stream_ptr()
+        for m in self.M:
+            for t in m:
+                t.zero_()
+        for b in range(2):
+            a.pop_out = ptr(self.P[b])
+            self._set_macros(self.M[b])
+            _lib.call("fc_lbm_pin_solid", a, st)
+        self.cur = 0
+        a.pop_out = ptr(self.P[0])
+        self._set_macros(self.M[0])
+        _lib.call("fc_lbm_collide_from_f32", a, -1, 0, st)
+        self.k = 0
+        self.primed = True
+
+    def step(self, phase_event=None):
+        sim, a = self.sim, self.args
+        if not self.primed:
+            self._prime()
+        st = stream_ptr()
+        k = self.k + 1          # reference step number being completed
+        nxt = 1 - self.cur
+        write_m = (k % self.macro_stride) == 0
+        m_out = self.M[k % 2] if write_m else None
+        a.pop_in = ptr(self.P[self.cur])
+        a.pop_out = ptr(self.P[nxt])
+        a.f32 = ptr(sim.f)
+        self._set_macros(m_out)
+        _lib.call("fc_lbm_fused_step", a, st)
+        if phase_event is not None:
+            phase_event.record()
+        if self.planes:
+            from .lbm_cuda_ext import _apply_flow_bcs_cuda
+            _apply_flow_bcs_cuda(sim)
+            for ax, pidx in self.planes:
+                _lib.call("fc_lbm_collide_from_f32", a, ax, pidx, st)
+        self.cur = nxt
+        self.k = k
+        # the reference exposes the pre-collision macros of this step's input state
+        self._expose(self.M[(k - 1) % 2])
+
+    def sync_f(self):
+        """Write the current post-stream populations S_k into sim.f."""
+        if not self.primed or self.k == 0:
+            return
+        a = self.args
+        a.pop_in = ptr(self.P[1 - self.cur])
+        a.f32 = ptr(self.sim.f)
+        _lib.call("fc_lbm_materialize", a, stream_ptr())
+
+    def post_collision(self) -> torch.Tensor:
+        """Latest post-collision populations as FP32 [19, N] (unshifted)."""
+        P = self.P[self.cur]
+        if self.storage == 0:
+            return P.clone()
+        from .fused_lbm import _W
+        return P.float() + _W.to(P.device)[:, None]
+
+    def check_device_error(self) -> int:
+        return int(self.dev_err.item())
+
+
+_W = torch.tensor([0.33333333] + [0.05555556] * 6 + [0.02777778] * 12, dtype=torch.float32)

@@ -1,0 +1,184 @@
+/*
+ * fluxcore3d_gb300.h -- C ABI of libfluxcore3d_gb300.so (sm_103a kernels for the
+ * conjugate-heat-transfer hot path: D3Q19 lattice Boltzmann, interpolated
+ * bounce-back, multigrid / Krylov thermal solve).
+ *
+ * Conventions
+ *   - Every pointer argument is a device pointer unless its name ends in _host.
+ *   - Every function returns an int status: 0 ok, 1 bad argument, 2 launch
+ *     failure, 3 unsupported combination.  Nothing in this library allocates
+ *     device memory behind the caller's back: scratch space is passed in as a
+ *     workspace pointer whose size the matching *_workspace_bytes() reports.
+ *   - `stream` is a cudaStream_t passed as void*; NULL is the legacy stream.
+ *   - Populations are [19][N] row-major with N = nx*ny*nz and cell index
+ *     flat = i*ny*nz + j*nz + k, direction order of the reference solver.
+ *
+ * Each declaration names the reference interface it replaces (file:line in
+ * the fluxcore3D tree).
+ */
+#ifndef FLUXCORE3D_GB300_H
+#define FLUXCORE3D_GB300_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define FC_ABI_VERSION 1
+
+int fc_abi_version(void);
+
+/* ---------------------------------------------------------------------------
+ * Per-operation lattice kernels (the LBM_CUDA module surface)
+ * ------------------------------------------------------------------------- */
+
+/* replaces LBM_CUDA.macro_collide_bgk  (solver/lbm_kernels.cu:628-646) */
+int fc_lbm_macro_collide_bgk(const float* f, float* f_post, float* rho, float* u, float* v, float* w,
+                             const uint8_t* solid, float omega, long long n_cells, void* stream);
+/* replaces LBM_CUDA.macro_collide_trt  (solver/lbm_kernels.cu:649-668) */
+int fc_lbm_macro_collide_trt(const float* f, float* f_post, float* rho, float* u, float* v, float* w,
+                             const uint8_t* solid, float omega_plus, float omega_minus, long long n_cells,
+                             void* stream);
+/* replaces LBM_CUDA.macro_collide_mrt  (solver/lbm_kernels.cu:671-692); S_dev: 19 floats on the device */
+int fc_lbm_macro_collide_mrt(const float* f, float* f_post, float* rho, float* u, float* v, float* w,
+                             const uint8_t* solid, const float* S_dev, long long n_cells, void* stream);
+/* replaces LBM_CUDA.macro_collide_mrt_smag  (solver/lbm_kernels.cu:1120-1145) */
+int fc_lbm_macro_collide_mrt_smag(const float* f, float* f_post, float* rho, float* u, float* v, float* w,
+                                  const uint8_t* solid, const float* S_dev, float Cs_dx2, float omega0,
+                                  long long n_cells, void* stream);
+/* replaces LBM_CUDA.stream_pull  (solver/lbm_kernels.cu:695-708) */
+int fc_lbm_stream_pull(const float* f_in, float* f_out, int nx, int ny, int nz, int px, int py, int pz,
+                       void* stream);
+/* replaces LBM_CUDA.sponge  (solver/lbm_kernels.cu:711-727) */
+int fc_lbm_sponge(float* f, const float* rho, const float* u, const float* v, const float* w,
+                  const float* sigma, long long n_cells, void* stream);
+/* replaces LBM_CUDA.ibb  (solver/lbm_kernels.cu:730-754); dev_err may be NULL */
+int fc_lbm_ibb(const float* f_post, float* f_stream, const int32_t* fluid_flat, const int32_t* dir_i,
+               const int32_t* dir_opp, const float* w1, const float* w2, const uint8_t* q_ge_half,
+               const int32_t* ff_flat, const uint8_t* ff_valid, long long n_links, long long n_cells,
+               unsigned* dev_err, void* stream);
+/* replaces LBM_CUDA.reset_solid  (solver/lbm_kernels.cu:757-764) */
+int fc_lbm_reset_solid(float* f, const uint8_t* solid, long long n_cells, void* stream);
+/* replaces LBM_CUDA.zou_he_bc  (solver/lbm_kernels.cu:975-996) */
+int fc_lbm_zou_he_bc(float* f, const uint8_t* solid, int nx, int ny, int nz, int axis, int plane_idx,
+                     int interior_idx, int bc_type, float u_in_lat, float rho_out_lat, int sign, void* stream);
+/* replaces LBM_CUDA.convective_bc  (solver/lbm_kernels.cu:1299-1344).  The reference keeps two
+ * process-global device scalars; here the caller passes a workspace of
+ * fc_lbm_convective_workspace_bytes(n1, n2) bytes (8-byte aligned) and the
+ * plane reduction is deterministic (fixed-order FP64 tree). */
+long long fc_lbm_convective_workspace_bytes(int n1, int n2);
+int fc_lbm_convective_bc(float* f, const uint8_t* solid, int nx, int ny, int nz, int axis, int outlet_idx,
+                         int interior_idx, int unknown_cax, float rho_out_lat, int n1, int n2,
+                         void* workspace, long long workspace_bytes, void* stream);
+
+/* ---------------------------------------------------------------------------
+ * Fused step (replaces the collide -> sponge -> stream -> ibb -> reset_solid
+ * launch sequence of LBMCUDAUpgrade._step_cuda, solver/lbm_cuda_ext.py:445-517)
+ * ------------------------------------------------------------------------- */
+typedef struct fc_lbm_step_args {
+    int32_t storage;         /* 0 FP32, 1 FP16 shifted (f - w_q), 2 BF16 shifted */
+    int32_t collision;       /* 0 BGK, 1 TRT, 2 MRT, 3 MRT + Smagorinsky */
+    int32_t nx, ny, nz;
+    int32_t periodic[3];     /* per-axis periodic streaming flags */
+    const void* pop_in;      /* [19][N] post-collision populations of the previous step */
+    void* pop_out;           /* [19][N] post-collision populations of this step */
+    float* f32;              /* [19][N] FP32 post-stream export (cells flagged DEFER / WRITE_S) */
+    float* rho;              /* [N] macro outputs, or NULL to skip the macro write */
+    float* u;
+    float* v;
+    float* w;
+    const uint8_t* cell_flags;   /* [N] bit0 solid, bit1 has links, bit2 deferred plane, bit3 export */
+    const int32_t* link_off;     /* [N] first link of the cell (read only where bit1 is set) */
+    const uint8_t* link_meta;    /* [n_links] dir | mode<<5 | last<<7 ; mode 0 q>=1/2, 1 q<1/2, 2 fallback */
+    const float* link_w;         /* [n_links][2] (w1, w2) */
+    long long n_links;
+    const float* sponge;         /* sigma per plane along sponge_axis, or NULL */
+    int32_t sponge_axis;
+    int32_t has_links;           /* 0: solid cells export the in-cell swap (no-link bounce-back) */
+    float omega, omega_plus, omega_minus;
+    float S[19];
+    float Cs_dx2, omega0;
+    unsigned* dev_err;           /* device error word (bit0 index out of range), may be NULL */
+} fc_lbm_step_args;
+
+/* One full time step for every non-deferred cell. */
+int fc_lbm_fused_step(const fc_lbm_step_args* args, void* stream);
+/* Collide cells straight from args->f32: axis < 0 => every fluid cell (start-up),
+ * else the plane plane_idx along axis (after that plane's boundary condition). */
+int fc_lbm_collide_from_f32(const fc_lbm_step_args* args, int axis, int plane_idx, void* stream);
+/* Rebuild post-stream FP32 populations (the reference's sim.f) from args->pop_in
+ * for every cell that is not on a deferred plane. */
+int fc_lbm_materialize(const fc_lbm_step_args* args, void* stream);
+/* Write rest populations w_q into args->pop_out (and macros 1,0,0,0) at solid cells. */
+int fc_lbm_pin_solid(const fc_lbm_step_args* args, void* stream);
+
+/* ---------------------------------------------------------------------------
+ * Multigrid thermal operator (the MG_CUDA module surface plus fused V-cycle
+ * kernels).  Fields are [nx][ny][nz] FP32; ax is the flow axis and out_idx the
+ * outlet plane index on it (ghosting rule of solver/mg_kernels.cu:17-44).
+ * ------------------------------------------------------------------------- */
+/* replaces MG_CUDA.mop_fused  (solver/mg_kernels.cu:133-175): Lo = T + dt L(T) */
+int fc_mg_mop(const float* T, const float* aE, const float* aW, const float* aN, const float* aS, const float* aU,
+              const float* aD, const float* diagL, float* Lo, float dt, int nx, int ny, int nz, int ax, int out_idx,
+              void* stream);
+/* replaces MG_CUDA.jacobi_smooth  (solver/mg_kernels.cu:177-197): x += inv_diagM (b - Lo) */
+int fc_mg_jacobi(float* x, const float* b, const float* Lo, const float* inv_diagM, long long n, void* stream);
+/* replaces NLevelGeometricMGSolver.L_apply_fine  (solver/nlevel_mg_cuda.py:164-175): (M(T) - T) / dt */
+int fc_mg_apply_L(const float* T, const float* aE, const float* aW, const float* aN, const float* aS,
+                  const float* aU, const float* aD, const float* diagL, float* out, float dt, int nx, int ny, int nz,
+                  int ax, int out_idx, void* stream);
+/* replaces one mop_fused + jacobi_smooth pair of _vcycle (solver/nlevel_mg_cuda.py:285-287): x_out = x_in + invD (b - M x_in) */
+int fc_mg_smooth(const float* x_in, float* x_out, const float* b, const float* inv_diagM, const float* aE,
+                 const float* aW, const float* aN, const float* aS, const float* aU, const float* aD,
+                 const float* diagL, float dt, int nx, int ny, int nz, int ax, int out_idx, void* stream);
+/* the first sweep from a zero guess (nlevel_mg_cuda.py:297 zero + first smooth): x_out = invD b */
+int fc_mg_smooth_from_zero(float* x_out, const float* b, const float* inv_diagM, long long n, void* stream);
+/* replaces the residual + _restrict_into pair (nlevel_mg_cuda.py:289-295, :521-528); c* = n* / 2 */
+int fc_mg_residual_restrict(const float* x, const float* b, const float* mask, const float* aE, const float* aW,
+                            const float* aN, const float* aS, const float* aU, const float* aD, const float* diagL,
+                            float dt, int nx, int ny, int nz, int ax, int out_idx, float* b_coarse, int cx, int cy,
+                            int cz, void* stream);
+/* replaces _prolong_2x + x.add_(e, alpha) + x.mul_(mask) (nlevel_mg_cuda.py:300-303, :531-537) */
+int fc_mg_prolong_correct(float* x, const float* x_coarse, const float* mask, int nx, int ny, int nz, int cx,
+                          int cy, int cz, float alpha, void* stream);
+/* ||w (b - M x)||^2 in FP64 (w = mask, or 1 when mask is NULL), replaces the residual
+ * norm of NLevelGeometricMGSolver.solve (nlevel_mg_cuda.py:132-135).  r_out (optional)
+ * receives the FP32 residual.  result: one device double. */
+long long fc_mg_reduce_workspace_bytes(long long n);
+int fc_mg_residual_norm2(const float* x, const float* b, const float* mask, const float* aE, const float* aW,
+                         const float* aN, const float* aS, const float* aU, const float* aD, const float* diagL,
+                         float dt, int nx, int ny, int nz, int ax, int out_idx, float* r_out, void* workspace,
+                         long long workspace_bytes, double* result, void* stream);
+/* replaces NLevelGeometricMGSolver._build_coeffs_full  (solver/nlevel_mg_cuda.py:417-507) */
+int fc_mg_build_coeffs(const float* k, const float* rho_cp, const float* u, const float* v, const float* w, int nx,
+                       int ny, int nz, int ax, int out_idx, float dx, float s, float* aE, float* aW, float* aN,
+                       float* aS, float* aU, float* aD, float* diagL, void* stream);
+/* replaces _restrict_2x (solver/nlevel_mg_cuda.py:511-519); as_mask thresholds the mean at 0.999 (:255) */
+int fc_mg_restrict_mean(const float* src, int nx, int ny, int nz, float* dst, int as_mask, void* stream);
+/* replaces _update_inv_diag  (solver/nlevel_mg_cuda.py:262-267) */
+int fc_mg_inv_diag(const float* diagL, const float* mask, float* inv_diagM, float dt, float omega, long long n,
+                   void* stream);
+
+/* ---------------------------------------------------------------------------
+ * Krylov vector kernels (replace the torch.dot / Tensor.norm / axpy calls of
+ * solver/mg_pcg.py:25-187 with FP64-accumulated, deterministic versions)
+ * ------------------------------------------------------------------------- */
+long long fc_vec_workspace_bytes(long long n);
+/* kind 0 (f64,f64), 1 (f32,f32), 2 (f64,f32); weight optional; result: device double */
+int fc_vec_dot(int kind, const void* x, const void* y, long long n, const float* weight, void* workspace,
+               long long workspace_bytes, double* result, void* stream);
+/* y = alpha x + beta y, alpha = alpha_host * (*alpha_num / *alpha_den) when alpha_num is set; then * mask */
+int fc_vec_axpby(int is_f64, void* y, const void* x, long long n, double alpha_host, const double* alpha_num,
+                 const double* alpha_den, double beta, const float* mask, void* stream);
+/* dst = scale * src (* mask); kind 0 f32->f64, 1 f64->f32, 2 f32->f32, 3 f64->f64 */
+int fc_vec_convert(int kind, void* dst, const void* src, long long n, const float* mask, double scale, void* stream);
+/* y = M(x) or y = b - M(x) in FP64 with the FP32 fine-level coefficients; optional mask */
+int fc_mg_mop_f64(const double* x, const float* aE, const float* aW, const float* aN, const float* aS,
+                  const float* aU, const float* aD, const float* diagL, double dt, int nx, int ny, int nz, int ax,
+                  int out_idx, const double* b, const float* mask, double* y, void* stream);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* FLUXCORE3D_GB300_H */

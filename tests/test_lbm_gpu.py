@@ -1,0 +1,147 @@
+"""GPU parity of the lattice kernels against the C oracle (reference CUDA-path semantics).
+
+Tolerances: FP32 paths must agree with the FP32 oracle within 1e-5 relative L2
+on populations after the stated number of steps (the oracle differs only in
+FMA contraction and division rounding); FP16/BF16 shifted storage is compared
+with the FP64 oracle and must stay within 1e-3 relative error on velocity.
+"""
+import numpy as np
+import pytest
+import torch
+
+from fluxcore3d_gb300 import case as cases
+from fluxcore3d_gb300.solver.lbm_cuda_ext import LBM_CUDA, LBMCUDAUpgrade
+from oracle.lbm import OracleLBM
+
+pytestmark = pytest.mark.gpu
+
+
+def rel_l2(a, b):
+    a = np.asarray(a, np.float64)
+    b = np.asarray(b, np.float64)
+    return float(np.linalg.norm(a - b) / max(np.linalg.norm(b), 1e-300))
+
+
+def oracle_for(sim, real="f32"):
+    cfg = sim.cfg
+    links = None
+    if sim.ibb_data is not None and sim.ibb_data.n_links > 0:
+        d = sim.ibb_data
+        links = {k: getattr(d, k).cpu().numpy() for k in
+                 ("fluid_flat", "dir_i", "dir_opp", "w_i", "w_second", "q_ge_half", "ff_flat", "ff_valid")}
+    sigma = sim._sponge_sigma.cpu().numpy() if getattr(cfg, "sponge_length", 0) > 0 else None
+    om_minus = float(sim.omega_minus) if hasattr(sim, "omega_minus") else None
+    S = sim._mrt_S.cpu().numpy() if hasattr(sim, "_mrt_S") else None
+    return OracleLBM(sim.nx, sim.ny, sim.nz, sim.f.cpu().numpy(), sim.solid_flow.cpu().numpy(),
+                     collision=cfg.collision, omega=float(sim.omega_plus), omega_minus=om_minus, S=S,
+                     Cs_dx2=cfg.smag_Cs ** 2, sigma=sigma, links=links, flow_dir=cfg.flow_dir,
+                     domain_walls=cfg.domain_walls, domain_outlets=cfg.domain_outlets,
+                     transverse_walls=cfg.transverse_walls, u_in_lat=sim.u_in_lat,
+                     rho_out_lat=cfg.rho_out_lat, u_lat_max=cfg.u_lat_max,
+                     outlet_bc_mode=cfg.outlet_bc_mode, real=real)
+
+
+def run_pair(sim, steps, real="f32"):
+    orc = oracle_for(sim, real)
+    LBMCUDAUpgrade.patch(sim)
+    for _ in range(steps):
+        sim.step(do_thermal=False)
+    sim.sync_f()
+    torch.cuda.synchronize()
+    orc.step(steps)
+    assert sim._fc.check_device_error() == 0
+    return orc
+
+
+@pytest.mark.parametrize("collision", ["bgk", "trt", "mrt", "mrt_smag"])
+def test_fused_step_fp32_matches_oracle_small(cuda, collision):
+    sim = cases.channel_cube(device=cuda, collision=collision, nx=32, ny=16, nz=16, cube=6, cube_x=10,
+                             sponge_length=8, outlet="pressure")
+    orc = run_pair(sim, 200)
+    N = sim.nx * sim.ny * sim.nz
+    e = rel_l2(sim.f.reshape(19, N).cpu().numpy(), orc.f)
+    assert e < 1e-5, e
+    assert rel_l2(sim.u.reshape(-1).cpu().numpy(), orc.u) < 1e-4
+    assert rel_l2(sim.rho.reshape(-1).cpu().numpy(), orc.rho) < 1e-6
+
+
+def test_fused_step_c1_channel_1000_steps(cuda):
+    """Plain method, small channel (64x32x32, BGK FP32, convective outlet, cube IBB): 1000 steps."""
+    sim = cases.channel_cube(device=cuda, collision="bgk")
+    orc = run_pair(sim, 1000)
+    N = sim.nx * sim.ny * sim.nz
+    e = rel_l2(sim.f.reshape(19, N).cpu().numpy(), orc.f)
+    assert e < 1e-5, e
+
+
+def test_fused_step_no_links_periodic(cuda):
+    """No IBB links: flow-solid cells act through the in-cell swap; two periodic axes."""
+    sim = cases.channel_cube(device=cuda, collision="mrt", nx=24, ny=12, nz=10, cube=4, cube_x=8,
+                             with_links=False, outlet="pressure")
+    sim.cfg.domain_walls = []
+    orc = run_pair(sim, 100)
+    N = sim.nx * sim.ny * sim.nz
+    assert rel_l2(sim.f.reshape(19, N).cpu().numpy(), orc.f) < 1e-5
+
+
+def test_fused_step_convective_and_macro_lag(cuda):
+    sim = cases.channel_cube(device=cuda, collision="trt", nx=32, ny=12, nz=12, cube=4, cube_x=10)
+    orc = run_pair(sim, 50)
+    # macros after step k are those of the step's input state (reference semantics)
+    assert rel_l2(sim.v.reshape(-1).cpu().numpy(), orc.v) < 1e-4
+    assert rel_l2(sim.rho.reshape(-1).cpu().numpy(), orc.rho) < 1e-6
+
+
+@pytest.mark.parametrize("storage", ["fp16", "bf16"])
+def test_shifted_storage_vs_fp64(cuda, storage):
+    sim = cases.channel_cube(device=cuda, collision="mrt", storage=storage, nx=48, ny=16, nz=16, cube=6,
+                             cube_x=14, outlet="pressure", sponge_length=8)
+    orc = run_pair(sim, 300, real="f64")
+    u_ref = orc.u
+    err = np.abs(sim.u.reshape(-1).cpu().numpy() - u_ref).max() / np.abs(u_ref).max()
+    tol = 1e-3 if storage == "fp16" else 2e-2
+    assert err < tol, err
+
+
+def test_per_op_kernels_match_oracle(cuda):
+    """The LBM_CUDA per-operation surface reproduces one oracle step op by op."""
+    sim = cases.channel_cube(device=cuda, collision="mrt", nx=20, ny=10, nz=10, cube=4, cube_x=6,
+                             sponge_length=6, outlet="pressure")
+    orc = oracle_for(sim)
+    LBMCUDAUpgrade.patch(sim)
+    for _ in range(5):
+        LBMCUDAUpgrade._step_unfused(sim)
+    torch.cuda.synchronize()
+    orc.step(5)
+    N = sim.nx * sim.ny * sim.nz
+    assert rel_l2(sim.f.reshape(19, N).cpu().numpy(), orc.f) < 1e-6
+    # and the fused engine picks up from the unfused state
+    for _ in range(5):
+        sim.step(do_thermal=False)
+    sim.sync_f()
+    orc.step(5)
+    assert rel_l2(sim.f.reshape(19, N).cpu().numpy(), orc.f) < 1e-6
+
+
+def test_stream_pull_exact(cuda):
+    nx, ny, nz = 7, 5, 6
+    g = torch.Generator().manual_seed(3)
+    f = torch.rand((19, nx * ny * nz), generator=g).to(cuda)
+    out = torch.empty_like(f)
+    LBM_CUDA.stream_pull(f, out, nx, ny, nz, 0, 1, 0)
+    orc = OracleLBM(nx, ny, nz, np.zeros((19, nx * ny * nz)), np.zeros(nx * ny * nz), real="f32")
+    fo = np.empty((19, nx * ny * nz), np.float32)
+    from oracle.lbm import _p
+    src = np.ascontiguousarray(f.cpu().numpy())
+    orc.L.or_stream_pull(_p(src), _p(fo), nx, ny, nz, 0, 1, 0)
+    assert np.array_equal(out.cpu().numpy(), fo)
+
+
+def test_argument_errors_raise(cuda):
+    f = torch.zeros((19, 8), device=cuda)
+    with pytest.raises(RuntimeError):
+        LBM_CUDA.stream_pull(f, f.t().contiguous().t(), 2, 2, 2, 0, 0, 0)
+    with pytest.raises(RuntimeError):
+        LBM_CUDA.macro_collide_mrt(f, f.clone(), torch.zeros(8, device=cuda), torch.zeros(8, device=cuda),
+                                   torch.zeros(8, device=cuda), torch.zeros(8, device=cuda),
+                                   torch.zeros(8, dtype=torch.uint8, device=cuda), torch.zeros(5, device=cuda))
