@@ -118,7 +118,7 @@ def lbm_traffic(sim, fc, storage_bytes):
     import torch
     N = sim.nx * sim.ny * sim.nz
     deferred = int(((fc.flags & 4) != 0).sum())
-    fluid = int((fc.flags & 1 == 0).sum()) - deferred
+    fluid = int(((fc.flags & 1) == 0).sum()) - deferred
     link_cells = int(((fc.flags & 2) != 0).sum())
     return fluid * 38 * storage_bytes + N + link_cells * 4 + fc.n_links * 9, fluid
 
@@ -222,8 +222,14 @@ def main():
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-thermal", action="store_true")
+    ap.add_argument("--storages", default="fp16,fp32", help="population storages to time (first = headline)")
+    ap.add_argument("--profile", action="store_true",
+                    help="short run for ncu captures: headline storage only, no e2e / thermal / CPU legs")
     args = ap.parse_args()
     args.warmup = max(3, args.warmup)
+    if args.profile:
+        args.storages = args.storages.split(",")[0]
+        args.no_e2e = args.no_cpu = args.no_thermal = True
     if args.impl == "reference":
         run_reference(args)
         return
@@ -241,13 +247,14 @@ def main():
 
     hbm_peak, _, peak_kind = peaks()
     results = {}
-    for storage in ("fp16", "fp32"):
+    storages = args.storages.split(",")
+    for storage in storages:
         sim = make_case(dev, storage, args)
         LBMCUDAUpgrade.patch(sim)
         for _ in range(args.warmup):
             sim.step(do_thermal=False)
         torch.cuda.synchronize()
-        sampler = ClockSampler(local) if storage == "fp16" else None
+        sampler = ClockSampler(local) if storage == storages[0] else None
         if sampler:
             sampler.start()
         if ws > 1:
@@ -258,21 +265,20 @@ def main():
             torch.distributed.all_reduce(tt, op=torch.distributed.ReduceOp.MAX)
             total_ms = float(tt)
         clocks = sampler.stop() if sampler else None
-        sbytes = 2 if storage == "fp16" else 4
+        sbytes = 4 if storage == "fp32" else 2
         alg, n_fluid = lbm_traffic(sim, sim._fc, sbytes)
         kmean = statistics.mean(ks)
-        results[storage] = dict(total_ms=total_ms, kernel_ms=kmean, alg=alg, clocks=clocks,
+        from fluxcore3d_gb300.solver.lbm_cuda_ext import _bc_plan
+        per_step = 1 + sum(2 if b[0] == "convective" else 1 for b in _bc_plan(sim)) + len(sim._fc.planes)
+        results[storage] = dict(total_ms=total_ms, kernel_ms=kmean, alg=alg, clocks=clocks, launches=per_step,
                                 N=sim.nx * sim.ny * sim.nz, n_fluid=n_fluid, planes=len(sim._fc.planes),
                                 links=sim._fc.n_links, err=sim._fc.check_device_error())
-        if storage == "fp16":
-            keep = sim
-        else:
-            del sim
-    r = results["fp16"]
+        del sim
+    r = results[storages[0]]
     N = r["N"]
     mlups = N * args.steps / (r["total_ms"] / 1e3) / 1e6 * ws
     achieved = r["alg"] / (r["kernel_ms"] / 1e3) / 1e9
-    launches_per_step = 1 + 2 * r["planes"] + (1 if any(True for _ in []) else 0)
+    launches_per_step = r["launches"]
 
     # end to end through the public API with host buffers
     e2e = None
@@ -299,14 +305,18 @@ def main():
                      "frac": round(achieved / hbm_peak, 4), "traffic": None,
                      "kernel": "k_fused_step<F16S,MRT>", "kernel_ms": round(r["kernel_ms"], 5),
                      "peak_kind": peak_kind},
-        "fp32": {"mlups": round(results["fp32"]["N"] * args.steps / (results["fp32"]["total_ms"] / 1e3) / 1e6, 1),
-                 "kernel_ms": round(results["fp32"]["kernel_ms"], 5),
-                 "achieved_gbs": round(results["fp32"]["alg"] / (results["fp32"]["kernel_ms"] / 1e3) / 1e9, 1)},
+
         "clocks": r["clocks"],
         "gpu_launches": args.steps * launches_per_step,
         "device_error": r["err"],
     }
-    line["fp16_over_fp32"] = round(line["value"] / max(line["fp32"]["mlups"], 1e-9), 3)
+    for st_name in storages[1:]:
+        q = results[st_name]
+        line[st_name] = {"mlups": round(q["N"] * args.steps / (q["total_ms"] / 1e3) / 1e6, 1),
+                         "kernel_ms": round(q["kernel_ms"], 5),
+                         "achieved_gbs": round(q["alg"] / (q["kernel_ms"] / 1e3) / 1e9, 1)}
+    if "fp32" in line:
+        line["fp16_over_fp32"] = round(line["value"] / max(line["fp32"]["mlups"], 1e-9), 3)
     if e2e:
         line["e2e"] = e2e
     if not args.no_thermal:

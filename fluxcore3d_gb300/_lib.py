@@ -97,6 +97,13 @@ SIGNATURES: dict[str, tuple] = {
     "fc_vec_axpby": (i32, [i32, vp, vp, i64, f64, vp, vp, f64, vp, vp]),
     "fc_vec_convert": (i32, [i32, vp, vp, i64, vp, f64, vp]),
     "fc_mg_mop_f64": (i32, [vp] * 8 + [f64, i32, i32, i32, i32, i32, vp, vp, vp, vp]),
+    # thermal
+    "fc_thermal_rhs": (i32, [vp] * 7 + [f32, i64, vp]),
+    "fc_thermal_reconstruct": (i32, [vp, vp, vp, i32, i32, i32, i32, i32, vp]),
+    "fc_thermal_workspace_bytes": (i64, [i64]),
+    "fc_thermal_convergence_metrics": (i32, [vp, vp, vp, i64, vp, i64, vp, vp]),
+    "fc_thermal_physics_check": (i32, [vp, vp, f32, f32, i64, vp]),
+    "fc_thermal_steady_residual": (i32, [vp] * 10 + [f32, i32, i32, i32, i32, i32, vp, i64, vp, vp]),
 }
 
 STATUS_TEXT = {1: "bad argument", 2: "CUDA launch failure", 3: "unsupported combination"}

@@ -318,15 +318,22 @@ __global__ void __launch_bounds__(BLOCK) k_convective_pass2(
 struct Geo {
     int nx, ny, nz;
     int px, py, pz;
-    long long N;
+    long long N;   // population stride (cells); cell indices themselves fit in 32 bits
     int nynz;
 };
 
-__device__ __forceinline__ void cell_coords(const Geo& g, long long idx, int& i, int& j, int& k) {
-    i = (int)(idx / g.nynz);
-    const int rem = (int)(idx - (long long)i * g.nynz);
-    j = rem / g.nz;
-    k = rem - j * g.nz;
+// Threads map to cells as (k, j, i) = (x, y, z) launch coordinates: a warp
+// covers 32 consecutive k of one row, so every population access of a warp is
+// one contiguous (possibly one-element shifted) run.
+constexpr int TBX = 32, TBY = 4;
+
+__device__ __forceinline__ bool cell_of_thread(const Geo& g, int& i, int& j, int& k, int& idx) {
+    k = blockIdx.x * TBX + threadIdx.x;
+    j = blockIdx.y * TBY + threadIdx.y;
+    i = blockIdx.z;
+    if (k >= g.nz || j >= g.ny) return false;
+    idx = (i * g.ny + j) * g.nz + k;
+    return true;
 }
 
 // Neighbour source index for population q at cell (i,j,k): x - c_q with
@@ -345,18 +352,18 @@ __device__ __forceinline__ Nbr make_nbr(const Geo& g, int i, int j, int k) {
     return n;
 }
 template <int Q>
-__device__ __forceinline__ long long src_of(const Geo& g, const Nbr& n, int i, int j, int k, long long idx) {
+__device__ __forceinline__ int src_of(const Geo& g, const Nbr& n, int i, int j, int k, int idx) {
     const int si = cx(Q) == 1 ? n.im : (cx(Q) == -1 ? n.ip : i);
     const int sj = cy(Q) == 1 ? n.jm : (cy(Q) == -1 ? n.jp : j);
     const int sk = cz(Q) == 1 ? n.km : (cz(Q) == -1 ? n.kp : k);
     if ((si | sj | sk) < 0) return idx;
-    return ((long long)si * g.ny + sj) * g.nz + sk;
+    return (si * g.ny + sj) * g.nz + sk;
 }
 
 template <int KIND, int Q>
 struct PullOne {
     static __device__ __forceinline__ void run(const typename Store<KIND>::T* __restrict__ P, const Geo& g,
-                                               const Nbr& n, int i, int j, int k, long long idx, float f[19]) {
+                                               const Nbr& n, int i, int j, int k, int idx, float f[19]) {
         f[Q] = Store<KIND>::load(P + (long long)Q * g.N + src_of<Q>(g, n, i, j, k, idx), Q);
         PullOne<KIND, Q + 1>::run(P, g, n, i, j, k, idx, f);
     }
@@ -364,12 +371,12 @@ struct PullOne {
 template <int KIND>
 struct PullOne<KIND, 19> {
     static __device__ __forceinline__ void run(const typename Store<KIND>::T* __restrict__, const Geo&,
-                                               const Nbr&, int, int, int, long long, float*) {}
+                                               const Nbr&, int, int, int, int, float*) {}
 };
 
 template <int KIND>
 __device__ __forceinline__ float load_dyn(const typename Store<KIND>::T* __restrict__ P, long long N,
-                                          int q, long long cell) {
+                                          int q, int cell) {
     float v = 0.f;
     const auto raw = P + (long long)q * N + cell;
     if (KIND == ST_F32) {
@@ -406,42 +413,56 @@ struct FusedArgs {
     unsigned* dev_err;
 };
 
-// Post-stream populations of one cell from the previous post-collision buffer:
-// pull + interpolated bounce-back on the cell's own links.
+// One interpolated-bounce-back link of cell idx (reference lbm_kernels.cu:542-588,
+// evaluated in the pull pass from the previous post-collision buffer).
 template <int KIND>
-__device__ __forceinline__ void gather_cell(const FusedArgs& a, long long idx, int i, int j, int k,
-                                            uint8_t fl, float f[19]) {
+__device__ __forceinline__ void apply_link(const typename Store<KIND>::T* __restrict__ P, const Geo& g, int idx,
+                                           uint8_t meta, float2 wt, float f[19]) {
+    const int dir = meta & 31;
+    const int mode = (meta >> 5) & 3;
+    const int o = c_OPP[dir];
+    const float popp = load_dyn<KIND>(P, g.N, o, idx);
+    float val;
+    if (mode == 0) {
+        val = wt.x * popp + wt.y * load_dyn<KIND>(P, g.N, dir, idx);
+    } else if (mode == 1) {
+        const int xff = idx - (c_CX[dir] * g.nynz + c_CY[dir] * g.nz + c_CZ[dir]);
+        val = wt.x * popp + wt.y * load_dyn<KIND>(P, g.N, o, xff);
+    } else {
+        val = popp;
+    }
+#pragma unroll
+    for (int q = 1; q < 19; ++q)
+        if (q == dir) f[q] = val;
+}
+
+// Post-stream populations of one cell from the previous post-collision buffer:
+// pull + interpolated bounce-back on the cell's own links.  The high nibble of
+// the flag byte holds the cell's link count (15 = "15 or more, follow the
+// last-link bit").
+template <int KIND>
+__device__ __forceinline__ void gather_cell(const FusedArgs& a, int idx, int i, int j, int k, uint8_t fl,
+                                            float f[19]) {
     using T = typename Store<KIND>::T;
     const T* __restrict__ P = reinterpret_cast<const T*>(a.pop_in);
     const Nbr n = make_nbr(a.g, i, j, k);
+    int l0 = -1;
+    if (fl & CF_LINK) l0 = __ldg(a.link_off + idx);
     PullOne<KIND, 0>::run(P, a.g, n, i, j, k, idx, f);
     if (fl & CF_LINK) {
-        long long l = a.link_off[idx];
-        for (int guard = 0; guard < 18; ++guard) {
-            if (l < 0 || l >= a.n_links) {
-                if (a.dev_err) atomicOr(a.dev_err, DEV_ERR_INDEX);
-                break;
+        const int cnt = fl >> 4;
+        if (l0 < 0 || (long long)l0 + (cnt ? cnt : 1) > a.n_links) {
+            if (a.dev_err) atomicOr(a.dev_err, DEV_ERR_INDEX);
+            return;
+        }
+        const int nfix = cnt < 15 ? cnt : 14;
+        for (int t = 0; t < nfix; ++t) apply_link<KIND>(P, a.g, idx, __ldg(a.link_meta + l0 + t), __ldg(a.link_w + l0 + t), f);
+        if (cnt >= 15) {
+            for (int l = l0 + 14; l < a.n_links && l < l0 + 18; ++l) {
+                const uint8_t meta = __ldg(a.link_meta + l);
+                apply_link<KIND>(P, a.g, idx, meta, __ldg(a.link_w + l), f);
+                if (meta & 0x80) break;
             }
-            const uint8_t meta = a.link_meta[l];
-            const int dir = meta & 31;
-            const int mode = (meta >> 5) & 3;
-            const float2 wt = a.link_w[l];
-            const int o = c_OPP[dir];
-            const float popp = load_dyn<KIND>(P, a.g.N, o, idx);
-            float val;
-            if (mode == 0) {
-                val = wt.x * popp + wt.y * load_dyn<KIND>(P, a.g.N, dir, idx);
-            } else if (mode == 1) {
-                const long long xff = idx - ((long long)c_CX[dir] * a.g.nynz + (long long)c_CY[dir] * a.g.nz + c_CZ[dir]);
-                val = wt.x * popp + wt.y * load_dyn<KIND>(P, a.g.N, o, xff);
-            } else {
-                val = popp;
-            }
-#pragma unroll
-            for (int q = 1; q < 19; ++q)
-                if (q == dir) f[q] = val;
-            if (meta & 0x80) break;
-            ++l;
         }
     }
 }
@@ -450,7 +471,7 @@ __device__ __forceinline__ void gather_cell(const FusedArgs& a, long long idx, i
 // w_q after reset_solid when links exist, else the in-cell direction swap of
 // the pulled values (LBM_CHT.py _bounce_back_post_stream).
 template <int KIND>
-__device__ __forceinline__ void solid_cell(const FusedArgs& a, long long idx, int i, int j, int k, float f[19]) {
+__device__ __forceinline__ void solid_cell(const FusedArgs& a, int idx, int i, int j, int k, float f[19]) {
     if (a.has_links) {
 #pragma unroll
         for (int q = 0; q < 19; ++q) f[q] = wq(q);
@@ -465,14 +486,13 @@ __device__ __forceinline__ void solid_cell(const FusedArgs& a, long long idx, in
 }
 
 template <int KIND, int MODE>
-__device__ __forceinline__ void collide_store(const FusedArgs& a, long long idx, int i, int j, int k,
-                                              float f[19]) {
+__device__ __forceinline__ void collide_store(const FusedArgs& a, int idx, int i, int j, int k, float f[19]) {
     using T = typename Store<KIND>::T;
     float feq[19];
     const Macro m = collide<MODE>(f, feq, a.cp);
     if (a.sponge) {
         const int c = a.sponge_axis == 0 ? i : (a.sponge_axis == 1 ? j : k);
-        const float sg = a.sponge[c];
+        const float sg = __ldg(a.sponge + c);
         if (sg > 0.f) {
 #pragma unroll
             for (int q = 0; q < 19; ++q) f[q] = f[q] - sg * (f[q] - feq[q]);
@@ -487,14 +507,12 @@ __device__ __forceinline__ void collide_store(const FusedArgs& a, long long idx,
 }
 
 template <int KIND, int MODE>
-__global__ void __launch_bounds__(BLOCK) k_fused_step(const FusedArgs a) {
-    const long long idx = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-    if (idx >= a.g.N) return;
-    const uint8_t fl = a.flags[idx];
-    int i, j, k;
+__global__ void __launch_bounds__(TBX * TBY) k_fused_step(const FusedArgs a) {
+    int i, j, k, idx;
+    if (!cell_of_thread(a.g, i, j, k, idx)) return;
+    const uint8_t fl = __ldg(a.flags + idx);
     if (fl & CF_SOLID) {
         if (fl & (CF_DEFER | CF_WRITE_S)) {
-            cell_coords(a.g, idx, i, j, k);
             float f[19];
             solid_cell<KIND>(a, idx, i, j, k, f);
 #pragma unroll
@@ -502,7 +520,6 @@ __global__ void __launch_bounds__(BLOCK) k_fused_step(const FusedArgs a) {
         }
         return;
     }
-    cell_coords(a.g, idx, i, j, k);
     float f[19];
     gather_cell<KIND>(a, idx, i, j, k, fl, f);
     if (fl & (CF_DEFER | CF_WRITE_S)) {
@@ -513,16 +530,18 @@ __global__ void __launch_bounds__(BLOCK) k_fused_step(const FusedArgs a) {
     collide_store<KIND, MODE>(a, idx, i, j, k, f);
 }
 
+inline dim3 cell_grid(const Geo& g) {
+    return dim3((unsigned)((g.nz + TBX - 1) / TBX), (unsigned)((g.ny + TBY - 1) / TBY), (unsigned)g.nx);
+}
+
 // Rebuild the post-stream FP32 populations (the reference's sim.f) of every
 // cell not on a deferred plane from the previous post-collision buffer.
 template <int KIND>
-__global__ void __launch_bounds__(BLOCK) k_materialize(const FusedArgs a) {
-    const long long idx = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-    if (idx >= a.g.N) return;
+__global__ void __launch_bounds__(TBX * TBY) k_materialize(const FusedArgs a) {
+    int i, j, k, idx;
+    if (!cell_of_thread(a.g, i, j, k, idx)) return;
     const uint8_t fl = a.flags[idx];
     if (fl & CF_DEFER) return;
-    int i, j, k;
-    cell_coords(a.g, idx, i, j, k);
     float f[19];
     if (fl & CF_SOLID) solid_cell<KIND>(a, idx, i, j, k, f);
     else gather_cell<KIND>(a, idx, i, j, k, fl, f);
@@ -536,18 +555,19 @@ template <int KIND, int MODE>
 __global__ void __launch_bounds__(BLOCK) k_collide_from_f32(const FusedArgs a, int axis, int plane,
                                                             int n1, int n2) {
     const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-    long long idx;
+    int idx;
     if (axis < 0) {
         if (t >= a.g.N) return;
-        idx = t;
+        idx = (int)t;
     } else {
         if (t >= (long long)n1 * n2) return;
         const int pa = (int)(t / n2), pb = (int)(t - (t / n2) * n2);
-        idx = plane_flat(axis, plane, pa, pb, a.g.ny, a.g.nz);
+        idx = (int)plane_flat(axis, plane, pa, pb, a.g.ny, a.g.nz);
     }
     if (a.flags[idx] & CF_SOLID) return;
-    int i, j, k;
-    cell_coords(a.g, idx, i, j, k);
+    const int i = idx / a.g.nynz;
+    const int rem = idx - i * a.g.nynz;
+    const int j = rem / a.g.nz, k = rem - (rem / a.g.nz) * a.g.nz;
     float f[19];
 #pragma unroll
     for (int q = 0; q < 19; ++q) f[q] = a.f32[q * a.g.N + idx];
@@ -574,6 +594,7 @@ int make_fused_args(const fc_lbm_step_args* s, FusedArgs& a) {
     a.g.nx = s->nx; a.g.ny = s->ny; a.g.nz = s->nz;
     a.g.px = s->periodic[0] != 0; a.g.py = s->periodic[1] != 0; a.g.pz = s->periodic[2] != 0;
     a.g.N = (long long)s->nx * s->ny * s->nz;
+    if (a.g.N >= (1LL << 31)) return FC_ERR_UNSUPPORTED;  // cell indices are 32-bit
     a.g.nynz = s->ny * s->nz;
     a.pop_in = s->pop_in; a.pop_out = s->pop_out; a.f32 = s->f32;
     a.rho = s->rho; a.u = s->u; a.v = s->v; a.w = s->w;
@@ -608,7 +629,7 @@ int dispatch(int storage, int collision, const FusedArgs& a, cudaStream_t st, in
 template <int S, int M>
 struct StepLauncher {
     static int go(const FusedArgs& a, cudaStream_t st, int, int, int, int) {
-        k_fused_step<S, M><<<grid_for(a.g.N), BLOCK, 0, st>>>(a);
+        k_fused_step<S, M><<<cell_grid(a.g), dim3(TBX, TBY), 0, st>>>(a);
         return launch_status();
     }
 };
@@ -804,9 +825,9 @@ int fc_lbm_materialize(const fc_lbm_step_args* args, void* stream) {
     if (!a.f32 || !a.pop_in) return FC_ERR_ARG;
     cudaStream_t st = (cudaStream_t)stream;
     switch (args->storage) {
-        case ST_F32: k_materialize<ST_F32><<<grid_for(a.g.N), BLOCK, 0, st>>>(a); break;
-        case ST_F16S: k_materialize<ST_F16S><<<grid_for(a.g.N), BLOCK, 0, st>>>(a); break;
-        default: k_materialize<ST_BF16S><<<grid_for(a.g.N), BLOCK, 0, st>>>(a); break;
+        case ST_F32: k_materialize<ST_F32><<<cell_grid(a.g), dim3(TBX, TBY), 0, st>>>(a); break;
+        case ST_F16S: k_materialize<ST_F16S><<<cell_grid(a.g), dim3(TBX, TBY), 0, st>>>(a); break;
+        default: k_materialize<ST_BF16S><<<cell_grid(a.g), dim3(TBX, TBY), 0, st>>>(a); break;
     }
     return launch_status();
 }

@@ -31,7 +31,7 @@ from .._lib import StepArgs
 from .._torch import ptr, stream_ptr
 from .face_roles import periodic_flags, resolve_face_roles, _face_ax_idx_fsign
 
-CF_SOLID, CF_LINK, CF_DEFER, CF_WRITE_S = 1, 2, 4, 8
+CF_SOLID, CF_LINK, CF_DEFER, CF_WRITE_S = 1, 2, 4, 8  # low nibble; high nibble = link count
 STORAGE = {"fp32": 0, "float32": 0, "f32": 0, "fp16": 1, "float16": 1, "f16": 1, "bf16": 2, "bfloat16": 2}
 STORAGE_DTYPE = {0: torch.float32, 1: torch.float16, 2: torch.bfloat16}
 COLLISION = {"bgk": 0, "trt": 1, "mrt": 2, "mrt_smag": 3}
@@ -44,7 +44,7 @@ _OPP = (0, 2, 1, 4, 3, 6, 5, 10, 9, 8, 7, 14, 13, 12, 11, 18, 17, 16, 15)
 def build_link_table(ibb, solid_flow_u8: torch.Tensor, nx: int, ny: int, nz: int):
     """Per-cell interpolated-bounce-back table from the reference's link-major IBBData.
 
-    Returns (link_off[N] int32, link_meta[L] uint8, link_w[L,2] float32, link cells mask).
+    Returns (link_off[N] int32, link_meta[L] uint8, link_w[L,2] float32, links per cell [N] int64).
     Links are grouped by fluid cell (sorted by cell, then direction); meta packs
     dir | mode << 5 | last << 7 with mode 0 (q >= 1/2), 1 (q < 1/2 with a second
     fluid node x_f - c_dir), 2 (q < 1/2 without one: plain bounce-back).
@@ -93,9 +93,8 @@ def build_link_table(ibb, solid_flow_u8: torch.Tensor, nx: int, ny: int, nz: int
     link_off[ff[first]] = pos[first]
     meta = (d | (mode << 5) | (last.to(torch.int64) << 7)).to(torch.uint8)
     link_w = torch.stack([w1, w2], dim=1).contiguous()
-    has = torch.zeros(N, dtype=torch.bool, device=dev)
-    has[ff] = True
-    return link_off, meta.contiguous(), link_w, has
+    counts = torch.bincount(ff, minlength=N)
+    return link_off, meta.contiguous(), link_w, counts
 
 
 class FusedLBM:
@@ -116,8 +115,10 @@ class FusedLBM:
         # links
         self.has_links = bool(getattr(sim, "ibb_data", None) is not None and int(sim.ibb_data.n_links) > 0)
         if self.has_links:
-            self.link_off, self.link_meta, self.link_w, has = build_link_table(sim.ibb_data, solid, nx, ny, nz)
-            flags |= has.to(torch.uint8) * CF_LINK
+            self.link_off, self.link_meta, self.link_w, counts = build_link_table(sim.ibb_data, solid, nx, ny, nz)
+            # bit1 = has links, high nibble = link count (15 = 15 or more)
+            flags |= (counts > 0).to(torch.uint8) * CF_LINK
+            flags |= (counts.clamp(max=15).to(torch.uint8) << 4)
             self.n_links = int(self.link_meta.numel())
         else:
             self.link_off = self.link_meta = self.link_w = None
@@ -185,7 +186,7 @@ class FusedLBM:
         sim, a = self.sim, self.args
         a.omega = float(getattr(sim, "omega", 1.0))
         a.omega_plus = float(getattr(sim, "omega_plus", a.omega))
-        a.omega_minus = float(getattr(sim, "omega_minus", a.omega)) if hasattr(sim, "omega_minus") else 1.0
+        a.omega_minus = float(sim.omega_minus) if hasattr(sim, "omega_minus") else 1.0
         S = getattr(sim, "_mrt_S", None)
         vals = [float(x) for x in S.tolist()] if S is not None else [0.0] * 19
         for q in range(19):
@@ -272,7 +273,6 @@ class FusedLBM:
         P = self.P[self.cur]
         if self.storage == 0:
             return P.clone()
-        from .fused_lbm import _W
         return P.float() + _W.to(P.device)[:, None]
 
     def check_device_error(self) -> int:

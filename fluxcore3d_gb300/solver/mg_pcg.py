@@ -1,0 +1,423 @@
+"""Drop-in replacement for the reference's solver/mg_pcg.py, plus FP64-certified solvers.
+
+Reference surface (solver/mg_pcg.py):
+  pcg_mg(mg_solver, b, x0=None, tol=1e-3, max_it=15)        :33-97
+  bicgstab_mg(mg_solver, b, x0=None, tol=1e-3, max_it=15)   :103-175
+  _precond(mg_solver, r)                                      :178-187  (one V-cycle)
+  chebyshev_smooth(mg_solver, level, n_steps=2, lam_min_ratio=0.1) :195-244
+  patch_mg_pcg(mg_solver, pe_threshold=1.5)                   :250-275
+They keep the reference's FP32 vectors and iteration logic; dot products
+accumulate in FP64 in the native library.
+
+Certified solvers (new): `bicgstab_mg_f64` and `fgmres_mg_f64` iterate on FP64
+vectors with the operator applied in FP64, precondition with the FP32 V-cycle
+(or any callable r32 -> z32, e.g. the learned preconditioner), and stop on the
+true FP64 relative residual ||mask (b - A x)|| / ||mask b||.  FGMRES is
+flexible, so a preconditioner that changes between applications (the learned
+one, or one that falls back to the V-cycle) is allowed.
+"""
+from __future__ import annotations
+
+import math
+import types
+from typing import Callable, Optional, Tuple
+
+import torch
+
+from .. import _lib
+from .._torch import ptr, stream_ptr
+
+Tensor = torch.Tensor
+
+
+class _Vec:
+    """FP64-accumulated vector kernels bound to one solver's fine level."""
+
+    def __init__(self, mg):
+        self.mg = mg
+        lv0 = mg._levels[0]
+        self.n = lv0["mask_f"].numel()
+        nbytes = _lib.call("fc_vec_workspace_bytes", self.n)
+        self.ws = torch.empty(int(nbytes), dtype=torch.uint8, device=mg.device)
+        self.sc = torch.zeros(64, dtype=torch.float64, device=mg.device)
+
+    def dot_dev(self, a: Tensor, b: Tensor, slot: int, weight: Optional[Tensor] = None) -> Tensor:
+        if a.dtype == torch.float64 and b.dtype == torch.float64:
+            kind = 0
+        elif a.dtype == torch.float32 and b.dtype == torch.float32:
+            kind = 1
+        else:
+            if a.dtype == torch.float32:
+                a, b = b, a
+            kind = 2
+        _lib.call("fc_vec_dot", kind, ptr(a), ptr(b), self.n, ptr(weight), ptr(self.ws), self.ws.numel(),
+                  ptr(self.sc[slot:slot + 1]), stream_ptr())
+        return self.sc[slot:slot + 1]
+
+    def dot(self, a: Tensor, b: Tensor, slot: int = 0) -> float:
+        return float(self.dot_dev(a, b, slot).item())
+
+    def axpby(self, y: Tensor, x: Tensor, alpha: float, beta: float = 1.0, num: Optional[Tensor] = None,
+              den: Optional[Tensor] = None, mask: Optional[Tensor] = None) -> None:
+        _lib.call("fc_vec_axpby", int(y.dtype == torch.float64), ptr(y), ptr(x), self.n, float(alpha), ptr(num),
+                  ptr(den), float(beta), ptr(mask), stream_ptr())
+
+    def convert(self, dst: Tensor, src: Tensor, mask: Optional[Tensor] = None, scale: float = 1.0) -> None:
+        kind = {(torch.float32, torch.float64): 0, (torch.float64, torch.float32): 1,
+                (torch.float32, torch.float32): 2, (torch.float64, torch.float64): 3}[(src.dtype, dst.dtype)]
+        _lib.call("fc_vec_convert", kind, ptr(dst), ptr(src), self.n, ptr(mask), float(scale), stream_ptr())
+
+    def mop64(self, x: Tensor, y: Tensor, b: Optional[Tensor] = None, mask: Optional[Tensor] = None) -> None:
+        mg = self.mg
+        lv = mg._levels[0]
+        nx, ny, nz = lv["shape"]
+        _lib.call("fc_mg_mop_f64", ptr(x), *mg._cptrs(lv), float(mg._dt_cache), nx, ny, nz, mg.ax, lv["out_idx"],
+                  ptr(b), ptr(mask), ptr(y), stream_ptr())
+
+
+def _vec(mg) -> _Vec:
+    v = getattr(mg, "_fc_vec", None)
+    if v is None or v.n != mg._levels[0]["mask_f"].numel():
+        v = _Vec(mg)
+        mg._fc_vec = v
+    return v
+
+
+def _precond(mg_solver, r: Tensor) -> Tensor:
+    """One V-cycle from a zero guess applied to r (reference mg_pcg.py:178-187)."""
+    lv0 = mg_solver._levels[0]
+    V = _vec(mg_solver)
+    V.convert(lv0["b_buf"], r.contiguous(), lv0["mask_f"])
+    mg_solver._vcycle(0, zero_guess=True)
+    z = torch.empty_like(lv0["x"])
+    V.convert(z, lv0["x"], lv0["mask_f"])
+    return z
+
+
+def pcg_mg(mg_solver, b: Tensor, x0: Optional[Tensor] = None, tol: float = 1e-3,
+           max_it: int = 15) -> Tuple[Tensor, dict]:
+    """Preconditioned CG with one V-cycle as M^-1 (reference mg_pcg.py:33-97)."""
+    lv0 = mg_solver._levels[0]
+    mask = lv0["mask_f"]
+    V = _vec(mg_solver)
+    b = b.contiguous().to(torch.float32)
+    x = torch.zeros_like(b)
+    if x0 is not None:
+        V.convert(x, x0.contiguous().to(torch.float32), mask)
+    mg_solver._Mop(x, 0)
+    r = b.clone()
+    V.axpby(r, lv0["Lo"], -1.0, 1.0, mask=mask)           # r = (b - A x) * mask
+    z = _precond(mg_solver, r)
+    p = z.clone()
+    rz = V.dot(r, z, 0)
+    bnorm = math.sqrt(V.dot(b, b, 1)) + 1e-30
+    converged = False
+    it = 0
+    for it in range(max_it):
+        res_rel = math.sqrt(V.dot(r, r, 2)) / bnorm
+        if res_rel < tol:
+            converged = True
+            break
+        mg_solver._Mop(p, 0)
+        Ap = lv0["Lo"].clone()
+        pAp = V.dot(p, Ap, 3)
+        if abs(pAp) < 1e-30:
+            break
+        alpha = rz / pAp
+        V.axpby(x, p, alpha)
+        V.axpby(r, Ap, -alpha, 1.0, mask=mask)
+        z = _precond(mg_solver, r)
+        rz_new = V.dot(r, z, 4)
+        beta = rz_new / (rz + 1e-30)
+        V.axpby(p, z, 1.0, beta)
+        rz = rz_new
+    V.convert(x, x, mask)
+    return x, {"converged": converged, "it": it + 1, "res_rel": math.sqrt(V.dot(r, r, 5)) / bnorm}
+
+
+def bicgstab_mg(mg_solver, b: Tensor, x0: Optional[Tensor] = None, tol: float = 1e-3,
+                max_it: int = 15) -> Tuple[Tensor, dict]:
+    """Preconditioned BiCGSTAB, one V-cycle per application (reference mg_pcg.py:103-175)."""
+    lv0 = mg_solver._levels[0]
+    mask = lv0["mask_f"]
+    V = _vec(mg_solver)
+    b = b.contiguous().to(torch.float32)
+    x = torch.zeros_like(b)
+    if x0 is not None:
+        V.convert(x, x0.contiguous().to(torch.float32), mask)
+    mg_solver._Mop(x, 0)
+    r = b.clone()
+    V.axpby(r, lv0["Lo"], -1.0, 1.0, mask=mask)
+    r_hat = r.clone()
+    bnorm = math.sqrt(V.dot(b, b, 0)) + 1e-30
+    rho = alpha = omega = 1.0
+    v = torch.zeros_like(b)
+    p = torch.zeros_like(b)
+    converged = False
+    it = 0
+    for it in range(max_it):
+        res_rel = math.sqrt(V.dot(r, r, 1)) / bnorm
+        if res_rel < tol:
+            converged = True
+            break
+        rho_new = V.dot(r_hat, r, 2)
+        if abs(rho_new) < 1e-30:
+            break
+        beta = (rho_new / (rho + 1e-30)) * (alpha / (omega + 1e-30))
+        V.axpby(p, r, 1.0, beta)                  # p = beta p + r
+        V.axpby(p, v, -beta * omega)              # p -= beta omega v
+        p_hat = _precond(mg_solver, p)
+        mg_solver._Mop(p_hat, 0)
+        v = lv0["Lo"].clone()
+        alpha = rho_new / (V.dot(r_hat, v, 3) + 1e-30)
+        s = r.clone()
+        V.axpby(s, v, -alpha, 1.0, mask=mask)
+        if math.sqrt(V.dot(s, s, 4)) / bnorm < tol:
+            V.axpby(x, p_hat, alpha)
+            converged = True
+            break
+        s_hat = _precond(mg_solver, s)
+        mg_solver._Mop(s_hat, 0)
+        t = lv0["Lo"].clone()
+        omega = V.dot(t, s, 5) / (V.dot(t, t, 6) + 1e-30)
+        V.axpby(x, p_hat, alpha)
+        V.axpby(x, s_hat, omega, 1.0, mask=mask)
+        r = s.clone()
+        V.axpby(r, t, -omega, 1.0, mask=mask)
+        rho = rho_new
+    V.convert(x, x, mask)
+    return x, {"converged": converged, "it": it + 1, "res_rel": math.sqrt(V.dot(r, r, 7)) / bnorm}
+
+
+def chebyshev_smooth(mg_solver, level: int, n_steps: int = 2, lam_min_ratio: float = 0.1) -> None:
+    """Chebyshev smoothing on one level in place (reference mg_pcg.py:195-244)."""
+    lv = mg_solver._levels[level]
+    x, b, inv, mask = lv["x"], lv["b_buf"], lv["inv_diagM"], lv["mask_f"]
+    n = x.numel()
+    st = stream_ptr()
+    lam_max = float(torch.amax(lv["diagL"]).item()) * float(mg_solver._dt_cache) + 1.0
+    lam_min = lam_min_ratio * lam_max
+    d = (lam_max + lam_min) / 2.0
+    c = (lam_max - lam_min) / 2.0
+
+    def resid(src, out):
+        mg_solver._Mop(src, level)
+        _lib.call("fc_vec_convert", 2, ptr(out), ptr(b), n, None, 1.0, st)
+        _lib.call("fc_vec_axpby", 0, ptr(out), ptr(lv["Lo"]), n, -1.0, None, None, 1.0, ptr(mask), st)
+        _lib.call("fc_vec_convert", 2, ptr(out), ptr(out), n, ptr(inv), 1.0, st)   # out = invD r
+
+    p = torch.empty_like(x)
+    resid(x, p)
+    x_new = x.clone()
+    _lib.call("fc_vec_axpby", 0, ptr(x_new), ptr(p), n, 1.0, None, None, 1.0, None, st)
+    if n_steps == 1:
+        x.copy_(x_new)
+        return
+    rho_prev = 1.0
+    q = torch.empty_like(x)
+    for _ in range(1, n_steps):
+        rho_new = 1.0 / (2.0 * d / c - rho_prev)
+        resid(x_new, q)
+        # p = rho_new (2d/c invD r + rho_prev p)
+        _lib.call("fc_vec_axpby", 0, ptr(p), ptr(q), n, rho_new * 2.0 * d / c, None, None, rho_new * rho_prev,
+                  None, st)
+        _lib.call("fc_vec_axpby", 0, ptr(x_new), ptr(p), n, 1.0, None, None, 1.0, None, st)
+        rho_prev = rho_new
+    _lib.call("fc_vec_convert", 2, ptr(x), ptr(x_new), n, ptr(mask), 1.0, st)
+
+
+def patch_mg_pcg(mg_solver, pe_threshold: float = 1.5):
+    """Replace mg_solver.solve with PCG / BiCGSTAB chosen by the reference's Peclet heuristic
+    (reference mg_pcg.py:250-275: pe = 0.1 max(diagL))."""
+
+    def _solve_pcg(self, b, x0=None, max_cycles=15, tol=1e-3):
+        pe = float(torch.amax(self._levels[0]["diagL"]).item()) * 0.1
+        if pe > pe_threshold:
+            return bicgstab_mg(self, b, x0, tol=tol, max_it=max_cycles)
+        return pcg_mg(self, b, x0, tol=tol, max_it=max_cycles)
+
+    mg_solver.solve = types.MethodType(_solve_pcg, mg_solver)
+    print(f"[MG-PCG] Patched mg_solver.solve -> PCG/BiCGSTAB (pe_threshold={pe_threshold})")
+
+
+# ---------------------------------------------------------------------------
+# FP64-certified solvers
+# ---------------------------------------------------------------------------
+def _vcycle_pc(mg_solver) -> Callable[[Tensor, Tensor], None]:
+    lv0 = mg_solver._levels[0]
+    V = _vec(mg_solver)
+
+    def apply(r64: Tensor, z64: Tensor) -> None:
+        V.convert(lv0["b_buf"], r64, lv0["mask_f"])          # FP64 residual -> FP32 right-hand side
+        mg_solver._vcycle(0, zero_guess=True)
+        V.convert(z64, lv0["x"], lv0["mask_f"])
+    return apply
+
+
+def _true_res(V: _Vec, x64, b64, mask, tmp64) -> float:
+    V.mop64(x64, tmp64, b=b64, mask=mask)
+    return math.sqrt(V.dot(tmp64, tmp64, 10))
+
+
+def bicgstab_mg_f64(mg_solver, b: Tensor, x0: Optional[Tensor] = None, tol: float = 1e-8, max_it: int = 200,
+                    precond: Optional[Callable] = None) -> Tuple[Tensor, dict]:
+    """Right-preconditioned BiCGSTAB on FP64 vectors; stops on the true FP64 relative residual."""
+    lv0 = mg_solver._levels[0]
+    mask = lv0["mask_f"]
+    V = _vec(mg_solver)
+    M = precond or _vcycle_pc(mg_solver)
+    f64 = dict(dtype=torch.float64, device=b.device)
+    b64 = torch.empty(lv0["shape"], **f64)
+    V.convert(b64, b.contiguous(), mask)
+    x = torch.zeros(lv0["shape"], **f64)
+    if x0 is not None:
+        V.convert(x, x0.contiguous(), mask)
+    r = torch.empty_like(x)
+    V.mop64(x, r, b=b64, mask=mask)
+    bnorm = math.sqrt(V.dot(b64, b64, 0)) + 1e-300
+    r_hat = r.clone()
+    p = torch.zeros_like(x)
+    v = torch.zeros_like(x)
+    ph = torch.empty_like(x)
+    sh = torch.empty_like(x)
+    t = torch.empty_like(x)
+    rho = alpha = omega = 1.0
+    hist = []
+    converged = False
+    it = 0
+    for it in range(1, max_it + 1):
+        rho_new = V.dot(r_hat, r, 1)
+        if abs(rho_new) < 1e-300:
+            break
+        beta = (rho_new / rho) * (alpha / omega) if it > 1 else 0.0
+        V.axpby(p, v, -omega)                       # p -= omega v
+        V.axpby(p, r, 1.0, beta)                    # p = r + beta p
+        M(p, ph)
+        V.mop64(ph, v, mask=mask)
+        alpha = rho_new / V.dot(r_hat, v, 2)
+        V.axpby(r, v, -alpha)                       # r becomes s
+        V.axpby(x, ph, alpha)
+        s_norm = math.sqrt(V.dot(r, r, 3)) / bnorm
+        if s_norm < tol:
+            res = _true_res(V, x, b64, mask, t) / bnorm
+            hist.append(res)
+            if res < tol:
+                converged = True
+                break
+        M(r, sh)
+        V.mop64(sh, t, mask=mask)
+        tt = V.dot(t, t, 4)
+        omega = V.dot(t, r, 5) / tt if tt > 0 else 0.0
+        V.axpby(x, sh, omega)
+        V.axpby(r, t, -omega)
+        rho = rho_new
+        res = math.sqrt(V.dot(r, r, 6)) / bnorm
+        hist.append(res)
+        if res < tol:
+            res = _true_res(V, x, b64, mask, t) / bnorm
+            if res < tol:
+                converged = True
+                break
+            V.mop64(x, r, b=b64, mask=mask)          # restart from the true residual
+            r_hat.copy_(r)
+            p.zero_()
+            v.zero_()
+            rho = alpha = omega = 1.0
+        if omega == 0.0 or not math.isfinite(res):
+            break
+    res = _true_res(V, x, b64, mask, t) / bnorm
+    return x, {"converged": converged and res < tol, "it": it, "res_rel": res, "history": hist}
+
+
+def fgmres_mg_f64(mg_solver, b: Tensor, x0: Optional[Tensor] = None, tol: float = 1e-8, max_it: int = 200,
+                  restart: int = 30, precond: Optional[Callable] = None,
+                  stall_fallback: Optional[Callable] = None) -> Tuple[Tensor, dict]:
+    """Flexible GMRES(restart) on FP64 vectors with a right preconditioner r -> z.
+
+    `precond(r64, z64)` may change between applications.  When `stall_fallback`
+    is given, an inner cycle whose residual drops by less than 10 % switches the
+    remaining iterations to that preconditioner (the plain V-cycle)."""
+    lv0 = mg_solver._levels[0]
+    mask = lv0["mask_f"]
+    V = _vec(mg_solver)
+    M = precond or _vcycle_pc(mg_solver)
+    f64 = dict(dtype=torch.float64, device=b.device)
+    shape = lv0["shape"]
+    b64 = torch.empty(shape, **f64)
+    V.convert(b64, b.contiguous(), mask)
+    x = torch.zeros(shape, **f64)
+    if x0 is not None:
+        V.convert(x, x0.contiguous(), mask)
+    bnorm = math.sqrt(V.dot(b64, b64, 0)) + 1e-300
+    m = int(restart)
+    Vb = torch.zeros((m + 1,) + tuple(shape), **f64)
+    Zb = torch.zeros((m,) + tuple(shape), **f64)
+    w = torch.empty(shape, **f64)
+    total = 0
+    hist = []
+    fell_back = False
+    converged = False
+    while total < max_it:
+        V.mop64(x, Vb[0], b=b64, mask=mask)
+        beta = math.sqrt(V.dot(Vb[0], Vb[0], 1))
+        res = beta / bnorm
+        hist.append(res)
+        if res < tol:
+            converged = True
+            break
+        V.axpby(Vb[0], Vb[0], 0.0, 1.0 / beta)
+        H = [[0.0] * m for _ in range(m + 1)]
+        cs, sn = [0.0] * m, [0.0] * m
+        g = [0.0] * (m + 1)
+        g[0] = beta
+        j_done = 0
+        for j in range(m):
+            if total >= max_it:
+                break
+            M(Vb[j], Zb[j])
+            V.mop64(Zb[j], w, mask=mask)
+            for i in range(j + 1):                       # modified Gram-Schmidt
+                hij = V.dot(w, Vb[i], 2)
+                H[i][j] = hij
+                V.axpby(w, Vb[i], -hij)
+            hn = math.sqrt(V.dot(w, w, 3))
+            H[j + 1][j] = hn
+            if hn > 0:
+                V.axpby(Vb[j + 1], w, 1.0 / hn, 0.0)
+            for i in range(j):                           # apply previous rotations
+                a, c = H[i][j], H[i + 1][j]
+                H[i][j] = cs[i] * a + sn[i] * c
+                H[i + 1][j] = -sn[i] * a + cs[i] * c
+            a, c = H[j][j], H[j + 1][j]
+            d = math.hypot(a, c)
+            cs[j], sn[j] = (a / d, c / d) if d > 0 else (1.0, 0.0)
+            H[j][j] = cs[j] * a + sn[j] * c
+            H[j + 1][j] = 0.0
+            g[j + 1] = -sn[j] * g[j]
+            g[j] = cs[j] * g[j]
+            total += 1
+            j_done = j + 1
+            est = abs(g[j + 1]) / bnorm
+            hist.append(est)
+            if est < tol or hn == 0:
+                break
+            if stall_fallback is not None and not fell_back and j >= 2 and est > 0.9 * hist[-2]:
+                M = stall_fallback
+                fell_back = True
+        # x += Z y with H y = g
+        y = [0.0] * j_done
+        for i in range(j_done - 1, -1, -1):
+            s = g[i] - sum(H[i][k] * y[k] for k in range(i + 1, j_done))
+            y[i] = s / H[i][i] if H[i][i] != 0 else 0.0
+        for i in range(j_done):
+            V.axpby(x, Zb[i], y[i])
+        if hist and hist[-1] < tol:
+            tmp = w
+            res = _true_res(V, x, b64, mask, tmp) / bnorm
+            if res < tol:
+                converged = True
+                hist.append(res)
+                break
+    res = _true_res(V, x, b64, mask, w) / bnorm
+    return x, {"converged": converged and res < tol, "it": total, "res_rel": res, "history": hist,
+               "fell_back": fell_back}

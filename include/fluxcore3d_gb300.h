@@ -178,6 +178,27 @@ int fc_mg_mop_f64(const double* x, const float* aE, const float* aW, const float
                   const float* aU, const float* aD, const float* diagL, double dt, int nx, int ny, int nz, int ax,
                   int out_idx, const double* b, const float* mask, double* y, void* stream);
 
+/* ---------------------------------------------------------------------------
+ * Thermal pseudo-time step (the THERMAL_CUDA module surface)
+ * ------------------------------------------------------------------------- */
+/* replaces THERMAL_CUDA.thermal_rhs  (solver/thermal_kernels.cu:198-210) */
+int fc_thermal_rhs(const float* T_old, const float* T0, const float* src_step, const float* LT0, const float* mask_f,
+                   float* rhs, float* theta0, float dt, long long n, void* stream);
+/* replaces THERMAL_CUDA.thermal_reconstruct  (solver/thermal_kernels.cu:212-224); caller owns T_new */
+int fc_thermal_reconstruct(const float* T0, const float* theta, float* T_new, int nx, int ny, int nz, int ax,
+                           int out_idx, void* stream);
+long long fc_thermal_workspace_bytes(long long n);
+/* replaces THERMAL_CUDA.convergence_metrics  (solver/thermal_kernels.cu:226-247); result: 2 device floats */
+int fc_thermal_convergence_metrics(const float* T_new, const float* T_old, const uint8_t* solid, long long n,
+                                   void* workspace, long long workspace_bytes, float* result, void* stream);
+/* replaces THERMAL_CUDA.physics_check  (solver/thermal_kernels.cu:249-256); caller zeroes *flag */
+int fc_thermal_physics_check(const float* T, int* flag, float T_min, float T_max, long long n, void* stream);
+/* steady residual of _temperature_step_mg (LBM_CHT.py:2690-2699); result: 2 device floats (r_inf, src_inf) */
+int fc_thermal_steady_residual(const float* T, const float* aE, const float* aW, const float* aN, const float* aS,
+                               const float* aU, const float* aD, const float* diagL, const float* src_step,
+                               const float* mask, float dt, int nx, int ny, int nz, int ax, int out_idx,
+                               void* workspace, long long workspace_bytes, float* result, void* stream);
+
 #ifdef __cplusplus
 }
 #endif

@@ -1,0 +1,162 @@
+"""Generate the golden fixtures in tests/golden/ by running the reference's own
+Python implementation (fluxcore3D, torch CPU path) on small seeded inputs.
+
+Run in a container where the reference tree is available:
+    PYTHONDONTWRITEBYTECODE=1 python tests/golden/make_golden.py /path/to/fluxcore3D
+
+Stub modules stand in for pyvista / trimesh (only the viewers and STL loading
+use them).  Fixtures written (all small .npz files):
+  mrt_matrix.npz      M and M^-1 of flow_solver_upgrade.py:98-125
+  lbm_ops.npz         collide (BGK, TRT via LBM_CHT._collide; MRT via
+                      FlowSolverUpgrade._collide_mrt), stream (LBM_CHT._stream),
+                      interpolated bounce-back + reset (LBM_CHT._interp_bounce_back_from_post)
+  ibb_links.npz       build_ibb_from_sdf_gpu link arrays and q on a cube and on a
+                      crop of fluxcore3D_web/Heatsink.npz (phi from build_phi_from_voxel_mask_mm)
+  mg_solve.npz        NLevelGeometricMGSolver (torch fallback, float64): coefficients,
+                      L_apply_fine, V-cycle solve, pcg_mg and bicgstab_mg results
+"""
+from __future__ import annotations
+
+import os
+import sys
+import types
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+
+
+def _stub_modules():
+    for name in ("pyvista", "trimesh", "trimesh.proximity"):
+        m = types.ModuleType(name)
+        m.Trimesh = object
+        m.ProximityQuery = object
+        sys.modules[name] = m
+    sys.modules["trimesh"].proximity = sys.modules["trimesh.proximity"]
+
+
+def main(ref_root: str):
+    os.environ["PYTHONDONTWRITEBYTECODE"] = "1"
+    sys.dont_write_bytecode = True
+    _stub_modules()
+    sys.path.insert(0, ref_root)
+    import torch
+    torch.set_num_threads(max(1, os.cpu_count() or 1))
+    import LBM_CHT as R
+    from solver import flow_solver_upgrade as FSU
+    from solver.nlevel_mg_cuda import NLevelGeometricMGSolver
+    from solver import mg_pcg
+    from pre_post import sdf_tracing as SDF
+
+    np.savez(os.path.join(HERE, "mrt_matrix.npz"), M=FSU._M_D3Q19, Minv=FSU._M_INV_D3Q19)
+
+    # ---------------- lattice operations on a 10x8x6 box with a cube --------------
+    def make_sim(collision):
+        cfg = R.SimConfig3D(nx=10, ny=8, nz=6, Lx_m=0.01, Ly_m=0.008, Lz_m=0.006, u_in_mps=0.05,
+                            device="cpu", collision=collision, transverse_walls=False, sponge_length=0,
+                            obstacle={"type": "cube", "cx": 5, "cy": 4, "cz": 3, "wx": 2, "wy": 2, "wz": 2})
+        cfg.dx_mm = 1.0
+        fl = R.FluidPropsSI(nu_m2_s=1e-5)
+        return R.LBMCHT3D_Torch(cfg, fl, R.SolidPropsSI())
+
+    g = torch.Generator().manual_seed(11)
+    out = {}
+    for col in ("bgk", "trt", "mrt"):
+        sim = make_sim(col)
+        f0 = (torch.rand((19, 10, 8, 6), generator=g, dtype=torch.float32) * 0.02
+              + torch.tensor(R.LBMCHT3D_Torch.w_np)[:, None, None, None])
+        sim.f = f0.clone()
+        sim._macroscopic()
+        if col == "mrt":
+            FSU.FlowSolverUpgrade._init_mrt(sim)
+            FSU.FlowSolverUpgrade._collide_mrt(sim)
+            out["mrt_S"] = sim._mrt_S.numpy()
+        else:
+            sim._collide()
+        out[f"{col}_f0"] = f0.numpy()
+        out[f"{col}_fpost"] = sim.f.numpy()
+        out[f"{col}_omega"] = np.float64(float(sim.omega_plus))
+        if col == "trt":
+            out["trt_omega_minus"] = np.float64(float(sim.omega_minus))
+    out["solid"] = sim.solid.numpy()
+    # streaming with the face roles of the default config (+X flow, periodic y/z)
+    sim = make_sim("bgk")
+    fs = torch.rand((19, 10, 8, 6), generator=g, dtype=torch.float32)
+    sim.f = fs.clone()
+    sim._stream()
+    out["stream_in"] = fs.numpy()
+    out["stream_out"] = sim.f.numpy()
+    # interpolated bounce-back from a voxel SDF
+    sim = make_sim("bgk")
+    phi = SDF.build_phi_from_voxel_mask_mm(sim.solid.numpy(), 1.0, device="cpu")
+    sim.phi = phi
+    SDF.build_ibb_from_sdf_gpu(sim, voxel_origin_mm=(0.0, 0.0, 0.0), pitch_mm=1.0, offset_ijk=(0, 0, 0),
+                               c_np=sim.c_np, opp_np=sim.opp_np)
+    fpost = torch.rand((19, 10, 8, 6), generator=g, dtype=torch.float32)
+    fstr = torch.rand((19, 10, 8, 6), generator=g, dtype=torch.float32)
+    sim.f = fstr.clone()
+    sim._interp_bounce_back_from_post(fpost.contiguous())
+    d = sim.ibb_data
+    out.update(ibb_fpost=fpost.numpy(), ibb_fstream=fstr.numpy(), ibb_out=sim.f.numpy(),
+               ibb_fluid_flat=d.fluid_flat.numpy(), ibb_dir_i=d.dir_i.numpy(), ibb_dir_opp=d.dir_opp.numpy(),
+               ibb_w_i=d.w_i.numpy(), ibb_w_second=d.w_second.numpy(), ibb_q_ge_half=d.q_ge_half.numpy(),
+               ibb_ff_flat=d.ff_flat.numpy(), ibb_ff_valid=d.ff_valid.numpy())
+    np.savez_compressed(os.path.join(HERE, "lbm_ops.npz"), **out)
+
+    # ---------------- link arrays + q on two voxel geometries ------------------------
+    links = {}
+    hs = np.load(os.path.join(ref_root, "fluxcore3D_web", "Heatsink.npz"))["voxel_solid"].astype(bool)
+    crop = np.zeros((40, 36, 24), bool)
+    crop[4:36, 2:34, 2:22] = hs[30:62, 40:72, 0:20]
+    cube = np.zeros((12, 10, 9), bool)
+    cube[4:8, 3:7, 2:6] = True
+    for name, solid in (("cube", cube), ("heatsink", crop)):
+        s = types.SimpleNamespace(device=torch.device("cpu"), nx=solid.shape[0], ny=solid.shape[1],
+                                  nz=solid.shape[2])
+        s.solid = torch.from_numpy(solid)
+        s.phi = SDF.build_phi_from_voxel_mask_mm(solid, 1.0, device="cpu")
+        SDF.build_ibb_from_sdf_gpu(s, voxel_origin_mm=(0.0, 0.0, 0.0), pitch_mm=1.0, offset_ijk=(0, 0, 0),
+                                   c_np=R.LBMCHT3D_Torch.c_np, opp_np=R.LBMCHT3D_Torch.opp_np)
+        d = s.ibb_data
+        links[f"{name}_solid"] = solid
+        links[f"{name}_phi"] = s.phi.numpy()
+        for k in ("fluid_flat", "dir_i", "dir_opp", "q_ge_half", "w_i", "w_second", "ff_flat", "ff_valid"):
+            links[f"{name}_{k}"] = getattr(d, k).numpy()
+    np.savez_compressed(os.path.join(HERE, "ibb_links.npz"), **links)
+
+    # ---------------- multigrid (float64 torch path) ---------------------------------
+    rng = np.random.default_rng(7)
+    shape = (24, 12, 12)
+    k = np.where(rng.random(shape) < 0.3, 200.0, 1.0) * 0.005
+    rcp = np.where(rng.random(shape) < 0.5, 1.0, 2.0)
+    u = rng.random(shape) * 0.05
+    v = (rng.random(shape) - 0.5) * 0.02
+    w = (rng.random(shape) - 0.5) * 0.02
+    mask = np.ones(shape, bool)
+    mask[0] = False
+    b = rng.random(shape) * mask
+    T = rng.random(shape)
+    t = lambda a: torch.tensor(a, dtype=torch.float64)
+    mgo = {"k": k, "rcp": rcp, "u": u, "v": v, "w": w, "mask": mask, "b": b, "T": T, "dt": 3.0, "s": 1.5}
+    mg = NLevelGeometricMGSolver(torch.device("cpu"), torch.float64, 0, 1, 1.5, omega=0.6)
+    mg.build_if_needed(t(k), t(rcp), t(u), t(v), t(w), torch.tensor(mask), 3.0)
+    for li, lv in enumerate(mg._levels):
+        for key in ("aE", "aW", "aN", "aS", "aU", "aD", "diagL", "inv_diagM", "mask_f"):
+            mgo[f"L{li}_{key}"] = lv[key].numpy()
+    mgo["nlevels"] = len(mg._levels)
+    mgo["LT"] = mg.L_apply_fine(t(T)).numpy()
+    x, info = mg.solve(t(b), None, max_cycles=6, tol=0.0)
+    mgo["solve_x"] = x.numpy()
+    mgo["solve_res"] = info["res_rel"]
+    x, info = mg_pcg.bicgstab_mg(mg, t(b), None, tol=1e-9, max_it=8)
+    mgo["bicgstab_x"] = x.numpy()
+    mgo["bicgstab_it"] = info["it"]
+    x, info = mg_pcg.pcg_mg(mg, t(b), None, tol=1e-9, max_it=6)
+    mgo["pcg_x"] = x.numpy()
+    mgo["pcg_it"] = info["it"]
+    np.savez_compressed(os.path.join(HERE, "mg_solve.npz"), **mgo)
+    print("golden fixtures written to", HERE)
+
+
+if __name__ == "__main__":
+    main(sys.argv[1] if len(sys.argv) > 1 else "/root/reference")

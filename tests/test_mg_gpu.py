@@ -1,0 +1,157 @@
+"""GPU parity of the multigrid / Krylov / thermal kernels against the numpy oracle.
+
+Tolerances: operator coefficients and single V-cycles within 1e-6 relative
+(FP32, different summation order in the 2x2x2 mean); multi-cycle solves within
+1e-5; FP64-certified Krylov solvers must reach a 1e-8 true relative residual.
+"""
+import numpy as np
+import pytest
+import torch
+
+from fluxcore3d_gb300.solver.nlevel_mg_cuda import NLevelGeometricMGSolver
+from fluxcore3d_gb300.solver import mg_pcg
+from fluxcore3d_gb300.solver.mg_cuda_ext import MG_CUDA
+from fluxcore3d_gb300.solver.thermal_cuda_ext import THERMAL_CUDA
+from oracle import mg as omg
+
+pytestmark = pytest.mark.gpu
+
+
+def rel(a, b):
+    a = np.asarray(a, np.float64)
+    b = np.asarray(b, np.float64)
+    return float(np.linalg.norm(a - b) / max(np.linalg.norm(b), 1e-300))
+
+
+def problem(shape=(32, 16, 16), ax=0, sign=1, seed=0, kratio=200.0):
+    rng = np.random.default_rng(seed)
+    k = np.where(rng.random(shape) < 0.3, kratio, 1.0).astype(np.float32) * 0.005
+    rcp = np.where(rng.random(shape) < 0.5, 1.0, 2.0).astype(np.float32)
+    u = (rng.random(shape) * 0.05).astype(np.float32)
+    v = ((rng.random(shape) - 0.5) * 0.02).astype(np.float32)
+    w = ((rng.random(shape) - 0.5) * 0.02).astype(np.float32)
+    mask = np.ones(shape, bool)
+    sl = [slice(None)] * 3
+    sl[ax] = 0 if sign > 0 else -1
+    mask[tuple(sl)] = False
+    b = (rng.random(shape) * mask).astype(np.float32)
+    return k, rcp, u, v, w, mask, b
+
+
+def both(prob, ax=0, sign=1, dt=3.0, s=1.0, **kw):
+    k, rcp, u, v, w, mask, b = prob
+    dev = torch.device("cuda")
+    mg = NLevelGeometricMGSolver(dev, torch.float32, ax, sign, s, omega=0.6, **kw)
+    T = lambda a: torch.tensor(a, device=dev)
+    mg.build_if_needed(T(k), T(rcp), T(u), T(v), T(w), T(mask), dt)
+    ref = omg.OracleMG(k, rcp, u, v, w, mask, ax, sign, s, omega=0.6, real=np.float32, **kw)
+    ref.set_dt(dt)
+    return mg, ref
+
+
+@pytest.mark.parametrize("ax,sign", [(0, 1), (1, -1), (2, 1)])
+def test_coefficients_and_hierarchy(cuda, ax, sign):
+    prob = problem((24, 20, 16), ax, sign)
+    mg, ref = both(prob, ax, sign)
+    assert len(mg._levels) == len(ref.levels)
+    for lg, lr in zip(mg._levels, ref.levels):
+        for key, rk in (("aE", "E"), ("aW", "W"), ("aN", "N"), ("aS", "S"), ("aU", "U"), ("aD", "D")):
+            assert rel(lg[key].cpu().numpy(), lr["a"][rk]) < 1e-6, key
+        assert rel(lg["diagL"].cpu().numpy(), lr["diag"]) < 1e-6
+        assert np.array_equal(lg["mask_f"].cpu().numpy(), lr["mask"])
+        assert rel(lg["inv_diagM"].cpu().numpy(), lr["inv"]) < 1e-6
+
+
+def test_mop_jacobi_and_L_apply(cuda):
+    prob = problem()
+    mg, ref = both(prob)
+    lv = mg._levels[0]
+    rng = np.random.default_rng(1)
+    T = rng.random(lv["shape"]).astype(np.float32)
+    Tt = torch.tensor(T, device="cuda")
+    Lo = torch.empty_like(Tt)
+    MG_CUDA.mop_fused(Tt, lv["aE"], lv["aW"], lv["aN"], lv["aS"], lv["aU"], lv["aD"], lv["diagL"], Lo,
+                      mg._dt_cache, 0, lv["out_idx"])
+    assert rel(Lo.cpu().numpy(), ref.mop(ref.levels[0], T)) < 1e-6
+    assert rel(mg.L_apply_fine(Tt).cpu().numpy(), ref.L_apply_fine(T)) < 1e-5
+    x = Tt.clone()
+    b = torch.ones_like(x)
+    MG_CUDA.jacobi_smooth(x, b, Lo, lv["inv_diagM"])
+    xr = T + ref.levels[0]["inv"] * (1.0 - ref.mop(ref.levels[0], T))
+    assert rel(x.cpu().numpy(), xr) < 1e-6
+
+
+@pytest.mark.parametrize("shape", [(32, 16, 16), (40, 24, 20)])
+def test_vcycle_solve_matches_oracle(cuda, shape):
+    prob = problem(shape)
+    mg, ref = both(prob)
+    b = prob[-1]
+    x, info = mg.solve(torch.tensor(b, device="cuda"), None, max_cycles=8, tol=0.0)
+    xr, ir = ref.solve(b, None, max_cycles=8, tol=0.0)
+    assert rel(x.cpu().numpy(), xr) < 1e-5
+    assert abs(info["res_rel"] - ir["res_rel"]) < 1e-5 * max(1.0, ir["res_rel"])
+    assert info["it"] == ir["it"] == 8
+
+
+def test_bicgstab_and_pcg_dropins_match_oracle(cuda):
+    prob = problem()
+    mg, ref = both(prob)
+    b = torch.tensor(prob[-1], device="cuda")
+    x, info = mg_pcg.bicgstab_mg(mg, b, None, tol=1e-5, max_it=12)
+    xr, ir = omg.bicgstab(ref, prob[-1], None, tol=1e-5, max_it=12)
+    assert info["it"] == ir["it"]
+    assert rel(x.cpu().numpy(), xr) < 1e-4
+    x2, i2 = mg_pcg.pcg_mg(mg, b, None, tol=1e-3, max_it=10)
+    assert np.isfinite(x2.cpu().numpy()).all()
+
+
+def test_certified_solvers_reach_1e8(cuda):
+    prob = problem((48, 24, 24))
+    mg, ref = both(prob)
+    b = torch.tensor(prob[-1], device="cuda")
+    x, info = mg_pcg.bicgstab_mg_f64(mg, b, tol=1e-8, max_it=200)
+    assert info["converged"], info
+    assert omg.true_residual(ref, x.cpu().numpy(), prob[-1]) < 2e-8
+    x2, i2 = mg_pcg.fgmres_mg_f64(mg, b, tol=1e-8, max_it=200, restart=30)
+    assert i2["converged"], i2
+    assert omg.true_residual(ref, x2.cpu().numpy(), prob[-1]) < 2e-8
+
+
+def test_thermal_kernels(cuda):
+    rng = np.random.default_rng(3)
+    shape = (12, 10, 8)
+    T0 = rng.random(shape).astype(np.float32)
+    th = rng.random(shape).astype(np.float32)
+    d = lambda a: torch.tensor(a, device="cuda")
+    for ax, out_idx in ((0, 11), (0, 0), (1, 9), (2, 0)):
+        Tn = THERMAL_CUDA.thermal_reconstruct(d(T0), d(th), *shape, ax, out_idx).cpu().numpy()
+        ref = T0 + th
+        val = ref.copy()
+        nx, ny, nz = shape
+        for i in range(nx):
+            for j in range(ny):
+                for k in range(nz):
+                    s = None
+                    if i == nx - 1:
+                        s = (i - 1, j, k)
+                    elif i == 0 and (ax != 0 or out_idx == 0):
+                        s = (1, j, k)
+                    elif j == ny - 1:
+                        s = (i, j - 1, k)
+                    elif j == 0 and (ax != 1 or out_idx == 0):
+                        s = (i, 1, k)
+                    elif k == nz - 1:
+                        s = (i, j, k - 1)
+                    elif k == 0 and (ax != 2 or out_idx == 0):
+                        s = (i, j, 1)
+                    if s is not None:
+                        val[i, j, k] = ref[s]
+        assert np.array_equal(Tn, val)
+    To = rng.random(shape).astype(np.float32)
+    solid = (rng.random(shape) < 0.3).astype(np.uint8)
+    rs, rf = THERMAL_CUDA.convergence_metrics(d(T0), d(To), d(solid))
+    dT = np.abs(T0 - To)
+    assert float(rs) == dT[solid == 1].max() and float(rf) == dT[solid == 0].max()
+    flag = THERMAL_CUDA.physics_check(d(T0), 0.0, 0.5)
+    assert int(flag) == 1
+    assert int(THERMAL_CUDA.physics_check(d(T0), -1.0, 2.0)) == 0

@@ -1,0 +1,123 @@
+"""Pin the oracle (and the link/q builder) against fixtures produced by the reference's own
+Python implementation (tests/golden/make_golden.py).  CPU only."""
+import os
+
+import numpy as np
+import pytest
+import torch
+
+from oracle import lbm as olbm
+from oracle import mg as omg
+
+G = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden")
+W_TORCH = np.array([1 / 3] + [1 / 18] * 6 + [1 / 36] * 12, dtype=np.float32)  # LBM_CHT.py:550-553
+
+
+def load(name):
+    return np.load(os.path.join(G, name))
+
+
+def test_mrt_matrix_matches_reference():
+    d = load("mrt_matrix.npz")
+    M = olbm.mrt_matrix()
+    assert np.array_equal(M, d["M"])
+    assert np.allclose(np.linalg.inv(M), d["Minv"], rtol=0, atol=1e-14)
+    # rows are orthogonal, so M^-1 = M^T diag(1/|M_k|^2) (the fused kernel relies on this)
+    assert np.allclose(M @ M.T, np.diag(np.diag(M @ M.T)))
+
+
+@pytest.mark.parametrize("col", ["bgk", "trt", "mrt"])
+def test_collide_matches_reference(col):
+    d = load("lbm_ops.npz")
+    f0 = d[f"{col}_f0"].reshape(19, -1)
+    solid = d["solid"].reshape(-1)
+    N = f0.shape[1]
+    om = float(d[f"{col}_omega"])
+    orc = olbm.OracleLBM(10, 8, 6, f0, solid, collision=col, omega=om,
+                         omega_minus=float(d["trt_omega_minus"]) if col == "trt" else None,
+                         S=d["mrt_S"] if col == "mrt" else None, real="f64", weights=W_TORCH)
+    orc.collide()
+    fluid = ~solid.astype(bool)
+    got = orc.fp[:, fluid]
+    ref = d[f"{col}_fpost"].reshape(19, N)[:, fluid]
+    # FP64 oracle against an FP32 torch result: a few FP32 ulps
+    assert np.abs(got - ref).max() / np.abs(ref).max() < 1e-6
+
+
+def test_stream_matches_reference_exactly():
+    d = load("lbm_ops.npz")
+    orc = olbm.OracleLBM(10, 8, 6, np.zeros((19, 480)), np.zeros(480), real="f32")
+    src = np.ascontiguousarray(d["stream_in"].reshape(19, -1))
+    out = np.empty_like(src)
+    # default config: +X flow, no walls -> x non-periodic, y and z periodic
+    orc.L.or_stream_pull(olbm._p(src), olbm._p(out), 10, 8, 6, 0, 1, 1)
+    assert np.array_equal(out, d["stream_out"].reshape(19, -1))
+
+
+def test_ibb_and_reset_match_reference_exactly():
+    d = load("lbm_ops.npz")
+    links = {k: d[f"ibb_{k}"] for k in ("fluid_flat", "dir_i", "dir_opp", "w_i", "w_second", "q_ge_half",
+                                        "ff_flat", "ff_valid")}
+    solid = d["solid"].reshape(-1)
+    orc = olbm.OracleLBM(10, 8, 6, d["ibb_fstream"], solid, links=links, real="f32", weights=W_TORCH)
+    fp = np.ascontiguousarray(d["ibb_fpost"].reshape(19, -1))
+    k = orc.links
+    orc.L.or_ibb(olbm._p(fp), olbm._p(orc.f), olbm._p(k["fluid_flat"]), olbm._p(k["dir_i"]),
+                 olbm._p(k["dir_opp"]), olbm._p(k["w1"]), olbm._p(k["w2"]), olbm._p(k["ge"]),
+                 olbm._p(k["ff_flat"]), olbm._p(k["ff_valid"]), len(k["fluid_flat"]), orc.N)
+    orc.L.or_reset_solid(olbm._p(orc.f), olbm._p(orc.solid), orc.N)
+    assert np.array_equal(orc.f, d["ibb_out"].reshape(19, -1))
+
+
+@pytest.mark.parametrize("name", ["cube", "heatsink"])
+def test_link_list_and_q_bit_exact(name):
+    """The link list (order included) and the Bouzidi weights equal the reference's bit for bit."""
+    from fluxcore3d_gb300 import geometry as geo
+    d = load("ibb_links.npz")
+    solid = torch.from_numpy(d[f"{name}_solid"])
+    phi = torch.from_numpy(d[f"{name}_phi"]).to(torch.float32)
+    ibb = geo.ibb_from_phi_trilinear(solid, phi)
+    for k in ("fluid_flat", "dir_i", "dir_opp", "ff_flat"):
+        assert np.array_equal(getattr(ibb, k).numpy(), d[f"{name}_{k}"]), k
+    for k in ("q_ge_half", "ff_valid"):
+        assert np.array_equal(getattr(ibb, k).numpy(), d[f"{name}_{k}"]), k
+    assert np.array_equal(ibb.w_i.numpy().view(np.uint32), d[f"{name}_w_i"].view(np.uint32))
+    assert np.array_equal(ibb.w_second.numpy().view(np.uint32), d[f"{name}_w_second"].view(np.uint32))
+
+
+def test_phi_from_voxels_matches_reference():
+    from fluxcore3d_gb300 import geometry as geo
+    d = load("ibb_links.npz")
+    for name in ("cube", "heatsink"):
+        phi = geo.phi_from_voxels(d[f"{name}_solid"]).astype(np.float32)
+        assert np.array_equal(phi, d[f"{name}_phi"])
+
+
+def _golden_mg():
+    d = load("mg_solve.npz")
+    mg = omg.OracleMG(d["k"], d["rcp"], d["u"], d["v"], d["w"], d["mask"], 0, 1, float(d["s"]), omega=0.6,
+                      real=np.float64)
+    mg.set_dt(float(d["dt"]))
+    return d, mg
+
+
+def test_mg_coefficients_match_reference():
+    d, mg = _golden_mg()
+    assert len(mg.levels) == int(d["nlevels"])
+    for li, lv in enumerate(mg.levels):
+        for key, rk in (("aE", "E"), ("aW", "W"), ("aN", "N"), ("aS", "S"), ("aU", "U"), ("aD", "D")):
+            # the oracle builds from FP32 inputs as the CUDA path does; the golden ran in FP64
+            assert np.allclose(lv["a"][rk], d[f"L{li}_{key}"], rtol=1e-6, atol=0), (li, key)
+        assert np.array_equal(lv["mask"], d[f"L{li}_mask_f"])
+        assert np.allclose(lv["inv"], d[f"L{li}_inv_diagM"], rtol=1e-6, atol=0)
+
+
+def test_mg_apply_and_solves_match_reference():
+    d, mg = _golden_mg()
+    assert np.allclose(mg.L_apply_fine(d["T"]), d["LT"], rtol=1e-5, atol=1e-9)
+    x, info = mg.solve(d["b"], None, max_cycles=6, tol=0.0)
+    assert np.linalg.norm(x - d["solve_x"]) / np.linalg.norm(d["solve_x"]) < 1e-6
+    assert abs(info["res_rel"] - float(d["solve_res"])) < 1e-6
+    xb, ib = omg.bicgstab(mg, d["b"], None, tol=1e-9, max_it=8)
+    assert ib["it"] == int(d["bicgstab_it"])
+    assert np.linalg.norm(xb - d["bicgstab_x"]) / np.linalg.norm(d["bicgstab_x"]) < 1e-5
