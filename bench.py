@@ -112,40 +112,42 @@ def make_case(device, storage, args):
 
 
 def lbm_traffic(sim, fc, storage_bytes):
-    """Algorithmic bytes of one fused launch: every fluid cell reads and writes its 19
-    populations once, every cell's flag byte is read, and link cells read their link
-    offset plus 9 bytes per link (w1, w2, meta)."""
-    import torch
+    """Algorithmic bytes of one step's two fused passes.
+
+    main pass : every fluid cell without links and off the inlet/outlet planes
+                reads and writes its 19 populations once; every cell's flag byte is read.
+    link pass : each link cell reads its 19 populations, its flag, list entry and
+                link offset, writes 19 populations; each link reads 9 bytes of
+                table (w1, w2, meta) and 2 extra populations of the cell."""
     N = sim.nx * sim.ny * sim.nz
-    deferred = int(((fc.flags & 4) != 0).sum())
-    fluid = int(((fc.flags & 1) == 0).sum()) - deferred
-    link_cells = int(((fc.flags & 2) != 0).sum())
-    return fluid * 38 * storage_bytes + N + link_cells * 4 + fc.n_links * 9, fluid
+    fl = fc.flags
+    fluid = (fl & 1) == 0
+    deferred = (fl & 4) != 0
+    link = (fl & 2) != 0
+    s = storage_bytes
+    n_main = int((fluid & ~deferred & ~link).sum())
+    n_lc = int((fluid & link).sum())
+    main = n_main * 38 * s + N
+    links = n_lc * (38 * s + 9) + fc.n_links * (9 + 2 * s)
+    if not fc.separate_link_pass:        # link cells run inside the main pass
+        main, links = main + links, 0
+    return {"main": main, "links": links, "n_main": n_main, "n_link_cells": n_lc,
+            "n_fluid": int(fluid.sum())}
 
 
-def time_steps(sim, steps, per_kernel=True):
-    """Returns (total_ms, fused_kernel_ms_list) timed with CUDA events on the current stream."""
+def time_steps(sim, steps):
+    """Total device time (ms) of `steps` solver steps, CUDA events on the current stream."""
     import torch
     st = torch.cuda.current_stream()
-    evs = []
     t0 = torch.cuda.Event(enable_timing=True)
     t1 = torch.cuda.Event(enable_timing=True)
     torch.cuda.synchronize()
     t0.record(st)
     for _ in range(steps):
-        if per_kernel:
-            a = torch.cuda.Event(enable_timing=True)
-            b = torch.cuda.Event(enable_timing=True)
-            a.record(st)
-            sim._fc.step(phase_event=b)
-            evs.append((a, b))
-        else:
-            sim._fc.step()
+        sim.step(do_thermal=False)
     t1.record(st)
     torch.cuda.synchronize()
-    total = t0.elapsed_time(t1)
-    ks = [a.elapsed_time(b) for a, b in evs]
-    return total, ks
+    return t0.elapsed_time(t1)
 
 
 def run_reference(args):
@@ -259,25 +261,30 @@ def main():
             sampler.start()
         if ws > 1:
             torch.distributed.barrier()
-        total_ms, ks = time_steps(sim, args.steps)
+        total_ms = time_steps(sim, args.steps)
         if ws > 1:
             tt = torch.tensor([total_ms], device=dev)
             torch.distributed.all_reduce(tt, op=torch.distributed.ReduceOp.MAX)
             total_ms = float(tt)
         clocks = sampler.stop() if sampler else None
         sbytes = 4 if storage == "fp32" else 2
-        alg, n_fluid = lbm_traffic(sim, sim._fc, sbytes)
-        kmean = statistics.mean(ks)
+        traffic = lbm_traffic(sim, sim._fc, sbytes)
+        err = sim._fc.check_device_error()
+        passes = sim._fc.time_passes(max(20, min(args.steps, 200)))
         from fluxcore3d_gb300.solver.lbm_cuda_ext import _bc_plan
-        per_step = 1 + sum(2 if b[0] == "convective" else 1 for b in _bc_plan(sim)) + len(sim._fc.planes)
-        results[storage] = dict(total_ms=total_ms, kernel_ms=kmean, alg=alg, clocks=clocks, launches=per_step,
-                                N=sim.nx * sim.ny * sim.nz, n_fluid=n_fluid, planes=len(sim._fc.planes),
-                                links=sim._fc.n_links, err=sim._fc.check_device_error())
+        per_step = 1 + (1 if sim._fc.link_cells is not None else 0) + \
+            sum(2 if b[0] == "convective" else 1 for b in _bc_plan(sim)) + len(sim._fc.planes)
+        results[storage] = dict(total_ms=total_ms, passes=passes, traffic=traffic, clocks=clocks, launches=per_step,
+                                N=sim.nx * sim.ny * sim.nz, planes=len(sim._fc.planes),
+                                links=sim._fc.n_links, err=err)
         del sim
     r = results[storages[0]]
     N = r["N"]
     mlups = N * args.steps / (r["total_ms"] / 1e3) / 1e6 * ws
-    achieved = r["alg"] / (r["kernel_ms"] / 1e3) / 1e9
+    tr, ps = r["traffic"], r["passes"]
+    achieved = tr["main"] / (ps["main"] / 1e3) / 1e9
+    link_gbs = tr["links"] / (ps["links"] / 1e3) / 1e9 if ps.get("links") else None
+    step_gbs = (tr["main"] + tr["links"]) / (r["total_ms"] / args.steps / 1e3) / 1e9
     launches_per_step = r["launches"]
 
     # end to end through the public API with host buffers
@@ -298,13 +305,18 @@ def main():
         "vs_baseline": None,
         "dtype": "f16-storage/f32-compute",
         "data": "synthetic",
-        "config": {"workload": WORKLOAD, "cells": N, "fluid_cells": r["n_fluid"], "links": r["links"],
+        "config": {"workload": WORKLOAD, "cells": N, "fluid_cells": tr["n_fluid"], "links": r["links"],
+                   "link_cells": tr["n_link_cells"],
                    "collision": args.collision, "macro_stride": args.macro_stride,
                    "l2_flush": "inputs larger than L2 (2 x 159 MB populations)", "parallelism": "replicas"},
         "roofline": {"bound": "hbm", "achieved": round(achieved, 1), "peak": hbm_peak, "unit": "GB/s",
                      "frac": round(achieved / hbm_peak, 4), "traffic": None,
-                     "kernel": "k_fused_step<F16S,MRT>", "kernel_ms": round(r["kernel_ms"], 5),
-                     "peak_kind": peak_kind},
+                     "kernel": "k_fused_step<FP16 shifted, MRT> (pull + bounce-back + collide + sponge)",
+                     "kernel_ms": round(ps["main"], 5),
+                     "algorithmic_bytes": tr["main"], "peak_kind": peak_kind,
+                     "link_pass": {"ms": round(ps.get("links", 0.0), 5), "algorithmic_bytes": tr["links"],
+                                   "achieved": None if link_gbs is None else round(link_gbs, 1)},
+                     "step_achieved": round(step_gbs, 1)},
 
         "clocks": r["clocks"],
         "gpu_launches": args.steps * launches_per_step,
@@ -313,8 +325,8 @@ def main():
     for st_name in storages[1:]:
         q = results[st_name]
         line[st_name] = {"mlups": round(q["N"] * args.steps / (q["total_ms"] / 1e3) / 1e6, 1),
-                         "kernel_ms": round(q["kernel_ms"], 5),
-                         "achieved_gbs": round(q["alg"] / (q["kernel_ms"] / 1e3) / 1e9, 1)}
+                         "main_ms": round(q["passes"]["main"], 5), "links_ms": round(q["passes"].get("links", 0), 5),
+                         "main_achieved_gbs": round(q["traffic"]["main"] / (q["passes"]["main"] / 1e3) / 1e9, 1)}
     if "fp32" in line:
         line["fp16_over_fp32"] = round(line["value"] / max(line["fp32"]["mlups"], 1e-9), 3)
     if e2e:

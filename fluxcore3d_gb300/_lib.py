@@ -42,7 +42,7 @@ class StepArgs(C.Structure):
         ("w", vp),
         ("cell_flags", vp),
         ("link_off", vp),
-        ("link_meta", vp),
+        ("link_hdr", vp),
         ("link_w", vp),
         ("n_links", i64),
         ("sponge", vp),
@@ -55,6 +55,10 @@ class StepArgs(C.Structure):
         ("Cs_dx2", f32),
         ("omega0", f32),
         ("dev_err", vp),
+        ("link_cells", vp),
+        ("n_link_cells", i64),
+        ("phase_mask", C.c_int32),
+        ("separate_link_pass", C.c_int32),
     ]
 
 
@@ -104,6 +108,23 @@ SIGNATURES: dict[str, tuple] = {
     "fc_thermal_convergence_metrics": (i32, [vp, vp, vp, i64, vp, i64, vp, vp]),
     "fc_thermal_physics_check": (i32, [vp, vp, f32, f32, i64, vp]),
     "fc_thermal_steady_residual": (i32, [vp] * 10 + [f32, i32, i32, i32, i32, i32, vp, i64, vp, vp]),
+    # tcgen05 convolutions
+    "fc_conv3d_fwd": (i32, [vp, vp, vp, i32, i32, i32, i32, i32, i32, i32, i32, vp, vp, vp, vp]),
+    "fc_conv3d_dgrad_workspace_bytes": (i64, [i32, i32]),
+    "fc_conv3d_dgrad": (i32, [vp, vp, i32, i32, i32, i32, i32, i32, i32, vp, i64, vp, vp, vp, vp]),
+    "fc_conv3d_wgrad_workspace_bytes": (i64, [i32, i32, i32, i32, i32, i32, i32]),
+    "fc_conv3d_wgrad": (i32, [vp, vp, i32, i32, i32, i32, i32, i32, i32, i32, vp, i64, vp, vp, vp]),
+    # network glue
+    "fc_nn_pack_input": (i32, [vp, vp, vp, i64, i64, f32, f32, vp, vp]),
+    "fc_nn_avgpool2": (i32, [vp, i32, i32, i32, i32, i32, vp, vp]),
+    "fc_nn_avgpool2_bwd": (i32, [vp, i32, i32, i32, i32, i32, vp, vp]),
+    "fc_nn_upsample_concat": (i32, [vp, i32, vp, i32, i32, i32, i32, i32, vp, vp]),
+    "fc_nn_upsample_concat_bwd": (i32, [vp, i32, i32, i32, i32, i32, i32, vp, vp, vp]),
+    "fc_nn_act_bwd": (i32, [vp, vp, vp, i32, i64, vp, vp, vp]),
+    "fc_nn_take_channel0": (i32, [vp, i32, vp, i64, i64, vp, vp, vp]),
+    "fc_nn_mse_workspace_bytes": (i64, [i64]),
+    "fc_nn_mse_grad": (i32, [vp, i32, vp, vp, i64, vp, vp, i64, vp]),
+    "fc_nn_adam": (i32, [vp, vp, vp, vp, vp, i64, i32, i32, f32, f32, f32, f32, i32, f32, vp]),
 }
 
 STATUS_TEXT = {1: "bad argument", 2: "CUDA launch failure", 3: "unsupported combination"}

@@ -25,7 +25,15 @@ struct CollideParams {
     float S[19];        // MRT rates (channels 0,3,5,7 ignored: conserved)
     float Cs_dx2;       // (Cs*dx)^2 for Smagorinsky
     float omega0;       // base viscous rate for Smagorinsky
+    float SN[19];       // S_k / |M_k|^2 (filled by the host for the shifted-variable collision)
 };
+
+// squared row norms of the D3Q19 moment matrix
+__host__ __device__ constexpr float mrt_row_norm2(int k) {
+    return k == 0 ? 19.f : k == 1 ? 2394.f : k == 2 ? 252.f : (k == 3 || k == 5 || k == 7) ? 10.f
+         : (k == 4 || k == 6 || k == 8) ? 40.f : k == 9 ? 36.f : k == 10 ? 72.f : k == 11 ? 12.f
+         : k == 12 ? 24.f : k <= 15 ? 4.f : 8.f;
+}
 
 struct Macro {
     float rho, ux, uy, uz, inv_rho;
@@ -194,6 +202,169 @@ __device__ __forceinline__ Macro collide(float f[19], float feq[19], const Colli
 #pragma unroll
         for (int q = 0; q < 19; ++q) f[q] = f[q] - df[q];
     }
+    return m;
+}
+
+
+// ---------------------------------------------------------------------------
+// Collision in shifted variables h_q = f_q - w_q (the fused step's working set).
+// With sum_q w_q = 1, sum_q w_q c_q = 0 and sum_q w_q c_q c_q = I/3:
+//   rho = 1 + sum h,  j = sum c h,  M f = M h + (1, -11, 3, 0, ...),
+// and the MRT equilibrium moments are the closed-form polynomials of rho, j
+// for this equilibrium (m_eq = M f_eq evaluated symbolically), so neither f_eq
+// nor M f_eq is formed for MRT.  Returns the macros of the input state.
+// ---------------------------------------------------------------------------
+struct MacroH {
+    float drho, rho, inv_rho, jx, jy, jz, ux, uy, uz;
+};
+
+__device__ __forceinline__ MacroH macros_h(const float h[19]) {
+    MacroH m;
+    float d = 0.f;
+#pragma unroll
+    for (int q = 0; q < 19; ++q) d += h[q];
+    m.drho = d;
+    m.rho = 1.f + d;
+    m.jx = (h[1] - h[2]) + ((h[7] + h[8]) - (h[9] + h[10])) + ((h[11] + h[12]) - (h[13] + h[14]));
+    m.jy = (h[3] - h[4]) + ((h[7] - h[8]) + (h[9] - h[10])) + ((h[15] + h[16]) - (h[17] + h[18]));
+    m.jz = (h[5] - h[6]) + ((h[11] - h[12]) + (h[13] - h[14])) + ((h[15] - h[16]) + (h[17] - h[18]));
+    m.inv_rho = __frcp_rn(m.rho + 1e-12f);
+    m.ux = m.jx * m.inv_rho;
+    m.uy = m.jy * m.inv_rho;
+    m.uz = m.jz * m.inv_rho;
+    return m;
+}
+
+// h_eq,q = f_eq,q - w_q = w_q (drho + rho (cu + cu^2/2 - 3/2 u.u))
+__device__ __forceinline__ void equilibrium_h(const MacroH& m, float heq[19]) {
+    const float usq = 1.5f * (m.ux * m.ux + m.uy * m.uy + m.uz * m.uz);
+    const float tx = 3.f * m.ux, ty = 3.f * m.uy, tz = 3.f * m.uz;
+#pragma unroll
+    for (int q = 0; q < 19; ++q) {
+        float cu = 0.f;
+        if (cx(q) == 1) cu += tx;
+        if (cx(q) == -1) cu -= tx;
+        if (cy(q) == 1) cu += ty;
+        if (cy(q) == -1) cu -= ty;
+        if (cz(q) == 1) cu += tz;
+        if (cz(q) == -1) cu -= tz;
+        heq[q] = wq(q) * (m.drho + m.rho * (cu + 0.5f * cu * cu - usq));
+    }
+}
+
+template <int MODE>
+__device__ __forceinline__ MacroH collide_h(float h[19], const CollideParams& p) {
+    const MacroH m = macros_h(h);
+    if (MODE == CM_BGK || MODE == CM_TRT) {
+        float heq[19];
+        equilibrium_h(m, heq);
+        if (MODE == CM_BGK) {
+#pragma unroll
+            for (int q = 0; q < 19; ++q) h[q] = h[q] + p.omega * (heq[q] - h[q]);
+        } else {
+            float out[19];
+#pragma unroll
+            for (int q = 0; q < 19; ++q) {
+                const int o = opp(q);
+                const float np_ = 0.5f * ((h[q] - heq[q]) + (h[o] - heq[o]));
+                const float nm_ = 0.5f * ((h[q] - heq[q]) - (h[o] - heq[o]));
+                out[q] = h[q] - p.omega_plus * np_ - p.omega_minus * nm_;
+            }
+#pragma unroll
+            for (int q = 0; q < 19; ++q) h[q] = out[q];
+        }
+        return m;
+    }
+    // raw moments of h (same integer rows as mrt_df)
+    const float Fx = h[1] + h[2], Fy = h[3] + h[4], Fz = h[5] + h[6];
+    const float sf = Fx + Fy + Fz;
+    const float Sxy = h[7] + h[8] + h[9] + h[10];
+    const float Sxz = h[11] + h[12] + h[13] + h[14];
+    const float Syz = h[15] + h[16] + h[17] + h[18];
+    const float se = Sxy + Sxz + Syz;
+    const float jxe = (h[7] + h[8] - h[9] - h[10]) + (h[11] + h[12] - h[13] - h[14]);
+    const float jye = (h[7] - h[8] + h[9] - h[10]) + (h[15] + h[16] - h[17] - h[18]);
+    const float jze = (h[11] - h[12] + h[13] - h[14]) + (h[15] - h[16] + h[17] - h[18]);
+    // equilibrium parts (rho u u = j u)
+    const float uxx = m.jx * m.ux, uyy = m.jy * m.uy, uzz = m.jz * m.uz;
+    const float rus = uxx + uyy + uzz;
+    const float pxx = 2.f * uxx - uyy - uzz;
+    const float pww = uyy - uzz;
+    // non-equilibrium moments n_k = (M h)_k - (m_eq,k - (M w)_k)
+    const float n1 = (-30.f * h[0] - 11.f * sf + 8.f * se) + 11.f * m.drho - 19.f * rus;
+    const float n2 = (12.f * h[0] - 4.f * sf + se) - 3.f * m.drho + 5.5f * rus;
+    const float n4 = (-4.f * (h[1] - h[2]) + jxe) + (2.f / 3.f) * m.jx;
+    const float n6 = (-4.f * (h[3] - h[4]) + jye) + (2.f / 3.f) * m.jy;
+    const float n8 = (-4.f * (h[5] - h[6]) + jze) + (2.f / 3.f) * m.jz;
+    const float n9 = (2.f * Fx - Fy - Fz + Sxy + Sxz - 2.f * Syz) - pxx;
+    const float n10 = (-4.f * Fx + 2.f * Fy + 2.f * Fz + Sxy + Sxz - 2.f * Syz) + 0.5f * pxx;
+    const float n11 = (Fy - Fz + Sxy - Sxz) - pww;
+    const float n12 = (-2.f * Fy + 2.f * Fz + Sxy - Sxz) + 0.5f * pww;
+    const float n13 = (h[7] - h[8] - h[9] + h[10]) - m.jx * m.uy;
+    const float n14 = (h[15] - h[16] - h[17] + h[18]) - m.jy * m.uz;
+    const float n15 = (h[11] - h[12] - h[13] + h[14]) - m.jx * m.uz;
+    const float n16 = h[7] + h[8] - h[9] - h[10] - h[11] - h[12] + h[13] + h[14];
+    const float n17 = -h[7] + h[8] - h[9] + h[10] + h[15] + h[16] - h[17] - h[18];
+    const float n18 = h[11] - h[12] + h[13] - h[14] - h[15] + h[16] - h[17] + h[18];
+    float s9 = p.SN[9], s11 = p.SN[11], s13 = p.SN[13], s14 = p.SN[14], s15 = p.SN[15];
+    if (MODE == CM_MRT_SMAG) {
+        // Pi_neq = Pi(h) - rho u u - (drho / 3) I
+        const float third = m.drho * (1.f / 3.f);
+        const float Pxx = (Fx + Sxy + Sxz) - uxx - third;
+        const float Pyy = (Fy + Sxy + Syz) - uyy - third;
+        const float Pzz = (Fz + Sxz + Syz) - uzz - third;
+        const float Pxy = n13, Pyz = n14, Pxz = n15;
+        const float piF = sqrtf(Pxx * Pxx + Pyy * Pyy + Pzz * Pzz + 2.f * (Pxy * Pxy + Pxz * Pxz + Pyz * Pyz));
+        const float nu0 = (1.f / p.omega0 - 0.5f) * (1.f / 3.f);
+        const float disc = nu0 * nu0 + 4.f * p.Cs_dx2 * (piF * m.inv_rho) * 4.5f;
+        const float nu_eff = 0.5f * (nu0 + sqrtf(fmaxf(disc, nu0 * nu0)));
+        const float om = fminf(1.99f, __frcp_rn(3.f * nu_eff + 0.5f));
+        s9 = om * (1.f / 36.f); s11 = om * (1.f / 12.f);
+        s13 = om * 0.25f; s14 = om * 0.25f; s15 = om * 0.25f;
+    }
+    const float g1 = p.SN[1] * n1;
+    const float g2 = p.SN[2] * n2;
+    const float g4 = p.SN[4] * n4;
+    const float g6 = p.SN[6] * n6;
+    const float g8 = p.SN[8] * n8;
+    const float g9 = s9 * n9;
+    const float g10 = p.SN[10] * n10;
+    const float g11 = s11 * n11;
+    const float g12 = p.SN[12] * n12;
+    const float g13 = s13 * n13;
+    const float g14 = s14 * n14;
+    const float g15 = s15 * n15;
+    const float g16 = p.SN[16] * n16;
+    const float g17 = p.SN[17] * n17;
+    const float g18 = p.SN[18] * n18;
+    h[0] -= -30.f * g1 + 12.f * g2;
+    const float face = -11.f * g1 - 4.f * g2;
+    const float fx_ = face + 2.f * g9 - 4.f * g10;
+    h[1] -= fx_ - 4.f * g4;
+    h[2] -= fx_ + 4.f * g4;
+    const float fyz = face - g9 + 2.f * g10;
+    const float fy_ = fyz + g11 - 2.f * g12;
+    const float fz_ = fyz - g11 + 2.f * g12;
+    h[3] -= fy_ - 4.f * g6;
+    h[4] -= fy_ + 4.f * g6;
+    h[5] -= fz_ - 4.f * g8;
+    h[6] -= fz_ + 4.f * g8;
+    const float edge = 8.f * g1 + g2;
+    const float exy = edge + g9 + g10 + g11 + g12;
+    h[7] -= exy + g4 + g6 + g13 + g16 - g17;
+    h[8] -= exy + g4 - g6 - g13 + g16 + g17;
+    h[9] -= exy - g4 + g6 - g13 - g16 - g17;
+    h[10] -= exy - g4 - g6 + g13 - g16 + g17;
+    const float exz = edge + g9 + g10 - g11 - g12;
+    h[11] -= exz + g4 + g8 + g15 - g16 + g18;
+    h[12] -= exz + g4 - g8 - g15 - g16 - g18;
+    h[13] -= exz - g4 + g8 - g15 + g16 + g18;
+    h[14] -= exz - g4 - g8 + g15 + g16 - g18;
+    const float eyz = edge - 2.f * g9 - 2.f * g10;
+    h[15] -= eyz + g6 + g8 + g14 + g17 - g18;
+    h[16] -= eyz + g6 - g8 - g14 + g17 + g18;
+    h[17] -= eyz - g6 + g8 - g14 - g17 - g18;
+    h[18] -= eyz - g6 - g8 + g14 - g17 + g18;
     return m;
 }
 

@@ -324,7 +324,7 @@ struct Geo {
 
 // Threads map to cells as (k, j, i) = (x, y, z) launch coordinates: a warp
 // covers 32 consecutive k of one row, so every population access of a warp is
-// one contiguous (possibly one-element shifted) run.
+// one contiguous (possibly one-element shifted) run, and i, j are warp-uniform.
 constexpr int TBX = 32, TBY = 4;
 
 __device__ __forceinline__ bool cell_of_thread(const Geo& g, int& i, int& j, int& k, int& idx) {
@@ -336,76 +336,55 @@ __device__ __forceinline__ bool cell_of_thread(const Geo& g, int& i, int& j, int
     return true;
 }
 
-// Neighbour source index for population q at cell (i,j,k): x - c_q with
-// periodic wrap, or the cell itself when a non-periodic axis leaves the box.
-struct Nbr {
-    int im, ip, jm, jp, km, kp;  // -1 = leave the box on a non-periodic axis
-};
-__device__ __forceinline__ Nbr make_nbr(const Geo& g, int i, int j, int k) {
-    Nbr n;
-    n.im = i > 0 ? i - 1 : (g.px ? g.nx - 1 : -1);
-    n.ip = i < g.nx - 1 ? i + 1 : (g.px ? 0 : -1);
-    n.jm = j > 0 ? j - 1 : (g.py ? g.ny - 1 : -1);
-    n.jp = j < g.ny - 1 ? j + 1 : (g.py ? 0 : -1);
-    n.km = k > 0 ? k - 1 : (g.pz ? g.nz - 1 : -1);
-    n.kp = k < g.nz - 1 ? k + 1 : (g.pz ? 0 : -1);
-    return n;
-}
-template <int Q>
-__device__ __forceinline__ int src_of(const Geo& g, const Nbr& n, int i, int j, int k, int idx) {
-    const int si = cx(Q) == 1 ? n.im : (cx(Q) == -1 ? n.ip : i);
-    const int sj = cy(Q) == 1 ? n.jm : (cy(Q) == -1 ? n.jp : j);
-    const int sk = cz(Q) == 1 ? n.km : (cz(Q) == -1 ? n.kp : k);
-    if ((si | sj | sk) < 0) return idx;
-    return (si * g.ny + sj) * g.nz + sk;
-}
-
-template <int KIND, int Q>
-struct PullOne {
-    static __device__ __forceinline__ void run(const typename Store<KIND>::T* __restrict__ P, const Geo& g,
-                                               const Nbr& n, int i, int j, int k, int idx, float f[19]) {
-        f[Q] = Store<KIND>::load(P + (long long)Q * g.N + src_of<Q>(g, n, i, j, k, idx), Q);
-        PullOne<KIND, Q + 1>::run(P, g, n, i, j, k, idx, f);
+// Source cell x - c_q of every population: periodic axes wrap, a non-periodic
+// axis that leaves the box makes the cell its own source (stream_pull rule).
+__device__ __forceinline__ void pull_sources(const Geo& g, int i, int j, int k, int idx, int src[19]) {
+    const bool inner = (i > 0) & (i < g.nx - 1) & (j > 0) & (j < g.ny - 1);  // warp-uniform
+    if (inner) {
+        const bool zm_ok = (k > 0) | (g.pz != 0);
+        const bool zp_ok = (k < g.nz - 1) | (g.pz != 0);
+        const int dzm = k > 0 ? -1 : g.nz - 1;          // source k-1 (c_z = +1)
+        const int dzp = k < g.nz - 1 ? 1 : -(g.nz - 1); // source k+1 (c_z = -1)
+#pragma unroll
+        for (int q = 0; q < 19; ++q) {
+            const int base = idx - cx(q) * g.nynz - cy(q) * g.nz;
+            if (cz(q) == 0) src[q] = base;
+            else if (cz(q) == 1) src[q] = zm_ok ? base + dzm : idx;
+            else src[q] = zp_ok ? base + dzp : idx;
+        }
+        return;
     }
-};
-template <int KIND>
-struct PullOne<KIND, 19> {
-    static __device__ __forceinline__ void run(const typename Store<KIND>::T* __restrict__, const Geo&,
-                                               const Nbr&, int, int, int, int, float*) {}
-};
-
-template <int KIND>
-__device__ __forceinline__ float load_dyn(const typename Store<KIND>::T* __restrict__ P, long long N,
-                                          int q, int cell) {
-    float v = 0.f;
-    const auto raw = P + (long long)q * N + cell;
-    if (KIND == ST_F32) {
-        v = __ldg(reinterpret_cast<const float*>(raw));
-    } else if (KIND == ST_F16S) {
-        v = __half2float(__ldg(reinterpret_cast<const __half*>(raw)));
-    } else {
-        v = __bfloat162float(__ldg(reinterpret_cast<const __nv_bfloat16*>(raw)));
+    const int im = i > 0 ? i - 1 : (g.px ? g.nx - 1 : -1);
+    const int ip = i < g.nx - 1 ? i + 1 : (g.px ? 0 : -1);
+    const int jm = j > 0 ? j - 1 : (g.py ? g.ny - 1 : -1);
+    const int jp = j < g.ny - 1 ? j + 1 : (g.py ? 0 : -1);
+    const int km = k > 0 ? k - 1 : (g.pz ? g.nz - 1 : -1);
+    const int kp = k < g.nz - 1 ? k + 1 : (g.pz ? 0 : -1);
+#pragma unroll
+    for (int q = 0; q < 19; ++q) {
+        const int si = cx(q) == 1 ? im : (cx(q) == -1 ? ip : i);
+        const int sj = cy(q) == 1 ? jm : (cy(q) == -1 ? jp : j);
+        const int sk = cz(q) == 1 ? km : (cz(q) == -1 ? kp : k);
+        src[q] = ((si | sj | sk) < 0) ? idx : (si * g.ny + sj) * g.nz + sk;
     }
-    if (KIND != ST_F32) {
-        v += (q == 0) ? 0.33333333f : (q <= 6 ? 0.05555556f : 0.02777778f);
-    }
-    return v;
 }
 
 struct FusedArgs {
     Geo g;
-    const void* pop_in;
-    void* pop_out;
+    const void* pin[19];   // population planes of the previous post-collision buffer
+    void* pout[19];        // population planes of this step's buffer
     float* f32;
     float* rho;
     float* u;
     float* v;
     float* w;
     const uint8_t* flags;
-    const int* link_off;
-    const uint8_t* link_meta;
+    const int* link_off;      // per cell: link-cell ordinal (read where the link flag is set)
+    const uint4* link_hdr;    // per link cell: (dir mask, second-node mask, weight offset, 0)
     const float2* link_w;
     long long n_links;
+    const int* link_cells;    // optional list for the separate link pass
+    long long n_link_cells;
     const float* sponge;
     int sponge_axis;
     int has_links;
@@ -413,121 +392,172 @@ struct FusedArgs {
     unsigned* dev_err;
 };
 
-// One interpolated-bounce-back link of cell idx (reference lbm_kernels.cu:542-588,
-// evaluated in the pull pass from the previous post-collision buffer).
+// shifted value h = f - w_q of population q at `cell` of the input buffer
 template <int KIND>
-__device__ __forceinline__ void apply_link(const typename Store<KIND>::T* __restrict__ P, const Geo& g, int idx,
-                                           uint8_t meta, float2 wt, float f[19]) {
-    const int dir = meta & 31;
-    const int mode = (meta >> 5) & 3;
-    const int o = c_OPP[dir];
-    const float popp = load_dyn<KIND>(P, g.N, o, idx);
-    float val;
-    if (mode == 0) {
-        val = wt.x * popp + wt.y * load_dyn<KIND>(P, g.N, dir, idx);
-    } else if (mode == 1) {
-        const int xff = idx - (c_CX[dir] * g.nynz + c_CY[dir] * g.nz + c_CZ[dir]);
-        val = wt.x * popp + wt.y * load_dyn<KIND>(P, g.N, o, xff);
-    } else {
-        val = popp;
-    }
-#pragma unroll
-    for (int q = 1; q < 19; ++q)
-        if (q == dir) f[q] = val;
+__device__ __forceinline__ float in_h(const FusedArgs& a, int q, int cell) {
+    using T = typename Store<KIND>::T;
+    const T* p = reinterpret_cast<const T*>(a.pin[q]) + cell;
+    if (KIND == ST_F32) return __ldg(reinterpret_cast<const float*>(p)) - wq(q);
+    if (KIND == ST_F16S) return __half2float(__ldg(reinterpret_cast<const __half*>(p)));
+    return __bfloat162float(__ldg(reinterpret_cast<const __nv_bfloat16*>(p)));
 }
+template <int KIND>
+__device__ __forceinline__ void out_h(const FusedArgs& a, int q, int cell, float h) {
+    using T = typename Store<KIND>::T;
+    T* p = reinterpret_cast<T*>(a.pout[q]) + cell;
+    if (KIND == ST_F32) *reinterpret_cast<float*>(p) = h + wq(q);
+    else if (KIND == ST_F16S) *reinterpret_cast<__half*>(p) = __float2half_rn(h);
+    else *reinterpret_cast<__nv_bfloat16*>(p) = __float2bfloat16_rn(h);
+}
+// Interpolated bounce-back of one link cell (reference lbm_kernels.cu:542-588),
+// evaluated in the pull pass from the previous post-collision buffer.  The cell's
+// header (uint4) holds: x = mask of link directions (bit d), y = mask of links
+// whose second term is the opposite population at x_f - c_d (q < 1/2 with a
+// fluid second node) instead of population d at x_f, z = offset of the cell's
+// (w1, w2) pairs, one per set bit of x in ascending d.  q < 1/2 links without a
+// second node are stored as (w1, w2) = (1, 0).  Directions are unrolled so
+// every population index is a compile-time constant.
+template <int KIND, int D>
+struct LinkDir {
+    static __device__ __forceinline__ void run(const FusedArgs& a, int idx, uint4 hd, float h[19]) {
+        if (hd.x & (1u << D)) {
+            using T = typename Store<KIND>::T;
+            constexpr int O = opp(D);
+            const float2 wt = __ldg(a.link_w + hd.z + __popc(hd.x & ((1u << D) - 1u)));
+            const float fo = in_h<KIND>(a, O, idx) + wq(O);
+            const bool second_ff = (hd.y >> D) & 1u;
+            const T* p2 = second_ff
+                ? reinterpret_cast<const T*>(a.pin[O]) + (idx - (cx(D) * a.g.nynz + cy(D) * a.g.nz + cz(D)))
+                : reinterpret_cast<const T*>(a.pin[D]) + idx;
+            float f2;
+            if (KIND == ST_F32) f2 = __ldg(reinterpret_cast<const float*>(p2));
+            else if (KIND == ST_F16S) f2 = __half2float(__ldg(reinterpret_cast<const __half*>(p2))) + (second_ff ? wq(O) : wq(D));
+            else f2 = __bfloat162float(__ldg(reinterpret_cast<const __nv_bfloat16*>(p2))) + (second_ff ? wq(O) : wq(D));
+            h[D] = (wt.x * fo + wt.y * f2) - wq(D);
+        }
+        LinkDir<KIND, D + 1>::run(a, idx, hd, h);
+    }
+};
+template <int KIND>
+struct LinkDir<KIND, 19> {
+    static __device__ __forceinline__ void run(const FusedArgs&, int, uint4, float*) {}
+};
 
-// Post-stream populations of one cell from the previous post-collision buffer:
-// pull + interpolated bounce-back on the cell's own links.  The high nibble of
-// the flag byte holds the cell's link count (15 = "15 or more, follow the
-// last-link bit").
+// Post-stream populations (shifted) of one cell: pull + interpolated bounce-back
+// on the cell's own links.
 template <int KIND>
 __device__ __forceinline__ void gather_cell(const FusedArgs& a, int idx, int i, int j, int k, uint8_t fl,
-                                            float f[19]) {
-    using T = typename Store<KIND>::T;
-    const T* __restrict__ P = reinterpret_cast<const T*>(a.pop_in);
-    const Nbr n = make_nbr(a.g, i, j, k);
-    int l0 = -1;
-    if (fl & CF_LINK) l0 = __ldg(a.link_off + idx);
-    PullOne<KIND, 0>::run(P, a.g, n, i, j, k, idx, f);
+                                            float h[19]) {
+    int lc = -1;
+    if (fl & CF_LINK) lc = __ldg(a.link_off + idx);
+    int src[19];
+    pull_sources(a.g, i, j, k, idx, src);
+#pragma unroll
+    for (int q = 0; q < 19; ++q) h[q] = in_h<KIND>(a, q, src[q]);
     if (fl & CF_LINK) {
-        const int cnt = fl >> 4;
-        if (l0 < 0 || (long long)l0 + (cnt ? cnt : 1) > a.n_links) {
+        if (lc < 0 || (long long)lc >= a.n_link_cells) {
             if (a.dev_err) atomicOr(a.dev_err, DEV_ERR_INDEX);
             return;
         }
-        const int nfix = cnt < 15 ? cnt : 14;
-        for (int t = 0; t < nfix; ++t) apply_link<KIND>(P, a.g, idx, __ldg(a.link_meta + l0 + t), __ldg(a.link_w + l0 + t), f);
-        if (cnt >= 15) {
-            for (int l = l0 + 14; l < a.n_links && l < l0 + 18; ++l) {
-                const uint8_t meta = __ldg(a.link_meta + l);
-                apply_link<KIND>(P, a.g, idx, meta, __ldg(a.link_w + l), f);
-                if (meta & 0x80) break;
-            }
+        const uint4 hd = __ldg(a.link_hdr + lc);
+        if ((long long)hd.z + __popc(hd.x) > a.n_links) {
+            if (a.dev_err) atomicOr(a.dev_err, DEV_ERR_INDEX);
+            return;
         }
+        LinkDir<KIND, 1>::run(a, idx, hd, h);
     }
 }
 
-// Post-stream populations of a flow-solid cell as the reference leaves them:
-// w_q after reset_solid when links exist, else the in-cell direction swap of
-// the pulled values (LBM_CHT.py _bounce_back_post_stream).
+// Post-stream populations (shifted) of a flow-solid cell as the reference leaves
+// them: w_q after reset_solid when links exist, else the in-cell direction swap
+// of the pulled values (LBM_CHT.py _bounce_back_post_stream).
 template <int KIND>
-__device__ __forceinline__ void solid_cell(const FusedArgs& a, int idx, int i, int j, int k, float f[19]) {
+__device__ __forceinline__ void solid_cell(const FusedArgs& a, int idx, int i, int j, int k, float h[19]) {
     if (a.has_links) {
 #pragma unroll
-        for (int q = 0; q < 19; ++q) f[q] = wq(q);
+        for (int q = 0; q < 19; ++q) h[q] = 0.f;
     } else {
-        using T = typename Store<KIND>::T;
-        const Nbr n = make_nbr(a.g, i, j, k);
+        int src[19];
+        pull_sources(a.g, i, j, k, idx, src);
         float t[19];
-        PullOne<KIND, 0>::run(reinterpret_cast<const T*>(a.pop_in), a.g, n, i, j, k, idx, t);
 #pragma unroll
-        for (int q = 0; q < 19; ++q) f[q] = t[opp(q)];
+        for (int q = 0; q < 19; ++q) t[q] = in_h<KIND>(a, q, src[q]);
+#pragma unroll
+        for (int q = 0; q < 19; ++q) h[q] = t[opp(q)];
     }
+}
+
+__device__ __forceinline__ void export_f(const FusedArgs& a, int idx, const float h[19]) {
+#pragma unroll
+    for (int q = 0; q < 19; ++q) a.f32[q * a.g.N + idx] = h[q] + wq(q);
 }
 
 template <int KIND, int MODE>
-__device__ __forceinline__ void collide_store(const FusedArgs& a, int idx, int i, int j, int k, float f[19]) {
-    using T = typename Store<KIND>::T;
-    float feq[19];
-    const Macro m = collide<MODE>(f, feq, a.cp);
+__device__ __forceinline__ void collide_store(const FusedArgs& a, int idx, int i, int j, int k, float h[19]) {
+    const MacroH m = collide_h<MODE>(h, a.cp);
     if (a.sponge) {
         const int c = a.sponge_axis == 0 ? i : (a.sponge_axis == 1 ? j : k);
         const float sg = __ldg(a.sponge + c);
         if (sg > 0.f) {
+            float heq[19];
+            equilibrium_h(m, heq);
 #pragma unroll
-            for (int q = 0; q < 19; ++q) f[q] = f[q] - sg * (f[q] - feq[q]);
+            for (int q = 0; q < 19; ++q) h[q] = h[q] - sg * (h[q] - heq[q]);
         }
     }
-    T* __restrict__ Po = reinterpret_cast<T*>(a.pop_out);
 #pragma unroll
-    for (int q = 0; q < 19; ++q) Store<KIND>::store(Po + (long long)q * a.g.N + idx, q, f[q]);
+    for (int q = 0; q < 19; ++q) out_h<KIND>(a, q, idx, h[q]);
     if (a.rho) {
         a.rho[idx] = m.rho; a.u[idx] = m.ux; a.v[idx] = m.uy; a.w[idx] = m.uz;
     }
 }
 
-template <int KIND, int MODE>
-__global__ void __launch_bounds__(TBX * TBY) k_fused_step(const FusedArgs a) {
+template <int KIND, int MODE, bool SKIP_LINKS>
+__global__ void __launch_bounds__(TBX * TBY, 7) k_fused_step(const FusedArgs a) {
     int i, j, k, idx;
     if (!cell_of_thread(a.g, i, j, k, idx)) return;
     const uint8_t fl = __ldg(a.flags + idx);
+    if (SKIP_LINKS && (fl & CF_LINK)) return;   // finished by k_link_cells
     if (fl & CF_SOLID) {
         if (fl & (CF_DEFER | CF_WRITE_S)) {
-            float f[19];
-            solid_cell<KIND>(a, idx, i, j, k, f);
-#pragma unroll
-            for (int q = 0; q < 19; ++q) a.f32[q * a.g.N + idx] = f[q];
+            float h[19];
+            solid_cell<KIND>(a, idx, i, j, k, h);
+            export_f(a, idx, h);
         }
         return;
     }
-    float f[19];
-    gather_cell<KIND>(a, idx, i, j, k, fl, f);
+    float h[19];
+    gather_cell<KIND>(a, idx, i, j, k, fl, h);
     if (fl & (CF_DEFER | CF_WRITE_S)) {
-#pragma unroll
-        for (int q = 0; q < 19; ++q) a.f32[q * a.g.N + idx] = f[q];
+        export_f(a, idx, h);
         if (fl & CF_DEFER) return;
     }
-    collide_store<KIND, MODE>(a, idx, i, j, k, f);
+    collide_store<KIND, MODE>(a, idx, i, j, k, h);
+}
+
+// Cells that own interpolated-bounce-back links, one thread each, from a
+// compacted ascending cell list: same work as k_fused_step for those cells.
+template <int KIND, int MODE>
+__global__ void __launch_bounds__(128) k_link_cells(const FusedArgs a, const int* __restrict__ cells, int n) {
+    const int t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= n) return;
+    const int idx = __ldg(cells + t);
+    if (idx < 0 || (long long)idx >= a.g.N) {
+        if (a.dev_err) atomicOr(a.dev_err, DEV_ERR_INDEX);
+        return;
+    }
+    const uint8_t fl = __ldg(a.flags + idx);
+    if (fl & CF_SOLID) return;
+    const int i = idx / a.g.nynz;
+    const int rem = idx - i * a.g.nynz;
+    const int j = rem / a.g.nz, k = rem - (rem / a.g.nz) * a.g.nz;
+    float h[19];
+    gather_cell<KIND>(a, idx, i, j, k, fl, h);
+    if (fl & (CF_DEFER | CF_WRITE_S)) {
+        export_f(a, idx, h);
+        if (fl & CF_DEFER) return;
+    }
+    collide_store<KIND, MODE>(a, idx, i, j, k, h);
 }
 
 inline dim3 cell_grid(const Geo& g) {
@@ -542,11 +572,10 @@ __global__ void __launch_bounds__(TBX * TBY) k_materialize(const FusedArgs a) {
     if (!cell_of_thread(a.g, i, j, k, idx)) return;
     const uint8_t fl = a.flags[idx];
     if (fl & CF_DEFER) return;
-    float f[19];
-    if (fl & CF_SOLID) solid_cell<KIND>(a, idx, i, j, k, f);
-    else gather_cell<KIND>(a, idx, i, j, k, fl, f);
-#pragma unroll
-    for (int q = 0; q < 19; ++q) a.f32[q * a.g.N + idx] = f[q];
+    float h[19];
+    if (fl & CF_SOLID) solid_cell<KIND>(a, idx, i, j, k, h);
+    else gather_cell<KIND>(a, idx, i, j, k, fl, h);
+    export_f(a, idx, h);
 }
 
 // Collide cells straight from the FP32 post-stream tensor: the whole grid at
@@ -568,22 +597,21 @@ __global__ void __launch_bounds__(BLOCK) k_collide_from_f32(const FusedArgs a, i
     const int i = idx / a.g.nynz;
     const int rem = idx - i * a.g.nynz;
     const int j = rem / a.g.nz, k = rem - (rem / a.g.nz) * a.g.nz;
-    float f[19];
+    float h[19];
 #pragma unroll
-    for (int q = 0; q < 19; ++q) f[q] = a.f32[q * a.g.N + idx];
-    collide_store<KIND, MODE>(a, idx, i, j, k, f);
+    for (int q = 0; q < 19; ++q) h[q] = a.f32[q * a.g.N + idx] - wq(q);
+    collide_store<KIND, MODE>(a, idx, i, j, k, h);
 }
 
 // Pin solid cells: populations w_q in the given buffer (shifted => 0), macros (1,0,0,0).
 template <int KIND>
 __global__ void __launch_bounds__(BLOCK) k_pin_solid(const FusedArgs a) {
-    const long long idx = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-    if (idx >= a.g.N) return;
+    const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= a.g.N) return;
+    const int idx = (int)t;
     if (!(a.flags[idx] & CF_SOLID)) return;
-    using T = typename Store<KIND>::T;
-    T* Po = reinterpret_cast<T*>(a.pop_out);
 #pragma unroll
-    for (int q = 0; q < 19; ++q) Store<KIND>::store(Po + (long long)q * a.g.N + idx, q, wq(q));
+    for (int q = 0; q < 19; ++q) out_h<KIND>(a, q, idx, 0.f);
     if (a.rho) { a.rho[idx] = 1.f; a.u[idx] = 0.f; a.v[idx] = 0.f; a.w[idx] = 0.f; }
 }
 
@@ -596,22 +624,36 @@ int make_fused_args(const fc_lbm_step_args* s, FusedArgs& a) {
     a.g.N = (long long)s->nx * s->ny * s->nz;
     if (a.g.N >= (1LL << 31)) return FC_ERR_UNSUPPORTED;  // cell indices are 32-bit
     a.g.nynz = s->ny * s->nz;
-    a.pop_in = s->pop_in; a.pop_out = s->pop_out; a.f32 = s->f32;
+    {
+        const size_t eb = s->storage == ST_F32 ? 4 : 2;
+        for (int q = 0; q < 19; ++q) {
+            a.pin[q] = s->pop_in ? (const void*)((const char*)s->pop_in + (size_t)q * (size_t)a.g.N * eb) : nullptr;
+            a.pout[q] = s->pop_out ? (void*)((char*)s->pop_out + (size_t)q * (size_t)a.g.N * eb) : nullptr;
+        }
+    }
+    a.f32 = s->f32;
     a.rho = s->rho; a.u = s->u; a.v = s->v; a.w = s->w;
     if (a.rho && (!a.u || !a.v || !a.w)) return FC_ERR_ARG;
     a.flags = s->cell_flags;
-    a.link_off = s->link_off; a.link_meta = s->link_meta;
+    a.link_off = s->link_off;
+    a.link_hdr = reinterpret_cast<const uint4*>(s->link_hdr);
     a.link_w = reinterpret_cast<const float2*>(s->link_w);
     a.n_links = s->n_links;
+    a.link_cells = s->link_cells;
+    a.n_link_cells = s->n_link_cells;
+    if (a.link_hdr && (reinterpret_cast<uintptr_t>(a.link_hdr) & 15)) return FC_ERR_ARG;
     a.sponge = s->sponge; a.sponge_axis = s->sponge_axis;
     if (a.sponge && (a.sponge_axis < 0 || a.sponge_axis > 2)) return FC_ERR_ARG;
     a.has_links = s->has_links;
     a.cp.omega = s->omega; a.cp.omega_plus = s->omega_plus; a.cp.omega_minus = s->omega_minus;
-    for (int q = 0; q < 19; ++q) a.cp.S[q] = s->S[q];
+    for (int q = 0; q < 19; ++q) {
+        a.cp.S[q] = s->S[q];
+        a.cp.SN[q] = s->S[q] / mrt_row_norm2(q);
+    }
     a.cp.Cs_dx2 = s->Cs_dx2; a.cp.omega0 = s->omega0;
     a.dev_err = s->dev_err;
     if (!a.flags) return FC_ERR_ARG;
-    if (a.n_links > 0 && (!a.link_off || !a.link_meta || !a.link_w)) return FC_ERR_ARG;
+    if (a.n_links > 0 && (!a.link_off || !a.link_hdr || !a.link_w || a.n_link_cells <= 0)) return FC_ERR_ARG;
     return FC_OK;
 }
 
@@ -628,8 +670,18 @@ int dispatch(int storage, int collision, const FusedArgs& a, cudaStream_t st, in
 
 template <int S, int M>
 struct StepLauncher {
+    static int go(const FusedArgs& a, cudaStream_t st, int skip_links, int, int, int) {
+        if (skip_links) k_fused_step<S, M, true><<<cell_grid(a.g), dim3(TBX, TBY), 0, st>>>(a);
+        else k_fused_step<S, M, false><<<cell_grid(a.g), dim3(TBX, TBY), 0, st>>>(a);
+        return launch_status();
+    }
+};
+template <int S, int M>
+struct LinkCellLauncher {
     static int go(const FusedArgs& a, cudaStream_t st, int, int, int, int) {
-        k_fused_step<S, M><<<cell_grid(a.g), dim3(TBX, TBY), 0, st>>>(a);
+        const int n = (int)a.n_link_cells;
+        if (n <= 0) return FC_OK;
+        k_link_cells<S, M><<<(n + 127) / 128, 128, 0, st>>>(a, a.link_cells, n);
         return launch_status();
     }
 };
@@ -799,15 +851,23 @@ int fc_lbm_fused_step(const fc_lbm_step_args* args, void* stream) {
     FusedArgs a;
     int rc = make_fused_args(args, a);
     if (rc) return rc;
-    if (!a.pop_in || !a.pop_out || a.pop_in == a.pop_out) return FC_ERR_ARG;
-    return dispatch<StepLauncher>(args->storage, args->collision, a, (cudaStream_t)stream, 0, 0, 0, 0);
+    if (!args->pop_in || !args->pop_out || args->pop_in == args->pop_out) return FC_ERR_ARG;
+    cudaStream_t st = (cudaStream_t)stream;
+    const int split = args->link_cells != nullptr && args->n_link_cells > 0 && args->separate_link_pass;
+    const int phases = args->phase_mask ? args->phase_mask : 3;
+    if (phases & 1) {
+        rc = dispatch<StepLauncher>(args->storage, args->collision, a, st, split, 0, 0, 0);
+        if (rc) return rc;
+    }
+    if (!split || !(phases & 2)) return FC_OK;
+    return dispatch<LinkCellLauncher>(args->storage, args->collision, a, st, 0, 0, 0, 0);
 }
 
 int fc_lbm_collide_from_f32(const fc_lbm_step_args* args, int axis, int plane_idx, void* stream) {
     FusedArgs a;
     int rc = make_fused_args(args, a);
     if (rc) return rc;
-    if (!a.f32 || !a.pop_out) return FC_ERR_ARG;
+    if (!a.f32 || !args->pop_out) return FC_ERR_ARG;
     int n1 = 0, n2 = 0;
     if (axis >= 0) {
         if (plane_dims(axis, a.g.nx, a.g.ny, a.g.nz, &n1, &n2)) return FC_ERR_ARG;
@@ -822,7 +882,7 @@ int fc_lbm_materialize(const fc_lbm_step_args* args, void* stream) {
     FusedArgs a;
     int rc = make_fused_args(args, a);
     if (rc) return rc;
-    if (!a.f32 || !a.pop_in) return FC_ERR_ARG;
+    if (!a.f32 || !args->pop_in) return FC_ERR_ARG;
     cudaStream_t st = (cudaStream_t)stream;
     switch (args->storage) {
         case ST_F32: k_materialize<ST_F32><<<cell_grid(a.g), dim3(TBX, TBY), 0, st>>>(a); break;
@@ -836,7 +896,7 @@ int fc_lbm_pin_solid(const fc_lbm_step_args* args, void* stream) {
     FusedArgs a;
     int rc = make_fused_args(args, a);
     if (rc) return rc;
-    if (!a.pop_out) return FC_ERR_ARG;
+    if (!args->pop_out) return FC_ERR_ARG;
     cudaStream_t st = (cudaStream_t)stream;
     switch (args->storage) {
         case ST_F32: k_pin_solid<ST_F32><<<grid_for(a.g.N), BLOCK, 0, st>>>(a); break;

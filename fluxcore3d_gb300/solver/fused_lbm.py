@@ -42,14 +42,21 @@ _OPP = (0, 2, 1, 4, 3, 6, 5, 10, 9, 8, 7, 14, 13, 12, 11, 18, 17, 16, 15)
 
 
 def build_link_table(ibb, solid_flow_u8: torch.Tensor, nx: int, ny: int, nz: int):
-    """Per-cell interpolated-bounce-back table from the reference's link-major IBBData.
+    """Per-cell interpolated-bounce-back tables from the reference's link-major IBBData.
 
-    Returns (link_off[N] int32, link_meta[L] uint8, link_w[L,2] float32, links per cell [N] int64).
-    Links are grouped by fluid cell (sorted by cell, then direction); meta packs
-    dir | mode << 5 | last << 7 with mode 0 (q >= 1/2), 1 (q < 1/2 with a second
-    fluid node x_f - c_dir), 2 (q < 1/2 without one: plain bounce-back).
-    Links whose fluid cell is a flow solid are dropped: the reference resets
-    those cells right after the bounce-back pass.
+    Returns a dict with
+      link_off [N] int32   ordinal of the cell among link cells (-1 elsewhere)
+      link_hdr [C, 4] int32 per link cell: mask of link directions (bit d), mask of
+                           links whose second term is the opposite population at
+                           x_f - c_d (q < 1/2 with a fluid second node), offset of the
+                           cell's first (w1, w2) pair, 0
+      link_w   [L, 2] float32 (w1, w2) per link, cells in ordinal order, directions ascending;
+                           q < 1/2 links without a second node become (1, 0): the
+                           plain bounce-back value f_opp(x_f) of the reference
+      link_cells [C] int32 cell index of each link cell (ascending)
+      counts   [N] links per cell
+    Links whose fluid cell is a flow solid are dropped: the reference resets those
+    cells right after the bounce-back pass.
     """
     dev = solid_flow_u8.device
     N = nx * ny * nz
@@ -80,21 +87,24 @@ def build_link_table(ibb, solid_flow_u8: torch.Tensor, nx: int, ny: int, nz: int
         raise ValueError("IBB links repeat a (cell, direction) pair")
     order = torch.argsort(key)
     ff, d, ge, fv, w1, w2 = ff[order], d[order], ge[order], fv[order], w1[order], w2[order]
-    mode = torch.where(ge, 0, torch.where(fv, 1, 2))
+    fallback = (~ge) & (~fv)
+    w1 = torch.where(fallback, torch.ones_like(w1), w1)
+    w2 = torch.where(fallback, torch.zeros_like(w2), w2)
+    second_ff = (~ge) & fv
     L = ff.numel()
-    last = torch.ones(L, dtype=torch.bool, device=dev)
-    if L > 1:
-        last[:-1] = ff[1:] != ff[:-1]
-    first = torch.ones(L, dtype=torch.bool, device=dev)
-    if L > 1:
-        first[1:] = ff[1:] != ff[:-1]
+    cells, inv, counts_c = torch.unique_consecutive(ff, return_inverse=True, return_counts=True)
+    C = cells.numel()
+    bit = torch.ones_like(d) << d
+    dmask = torch.zeros(C, dtype=torch.int64, device=dev).index_add_(0, inv, bit)
+    smask = torch.zeros(C, dtype=torch.int64, device=dev).index_add_(0, inv, bit * second_ff.to(torch.int64))
+    first = torch.cumsum(counts_c, 0) - counts_c
+    hdr = torch.stack([dmask, smask, first, torch.zeros_like(first)], dim=1).to(torch.int32).contiguous()
     link_off = torch.full((N,), -1, dtype=torch.int32, device=dev)
-    pos = torch.arange(L, device=dev, dtype=torch.int32)
-    link_off[ff[first]] = pos[first]
-    meta = (d | (mode << 5) | (last.to(torch.int64) << 7)).to(torch.uint8)
-    link_w = torch.stack([w1, w2], dim=1).contiguous()
-    counts = torch.bincount(ff, minlength=N)
-    return link_off, meta.contiguous(), link_w, counts
+    link_off[cells] = torch.arange(C, device=dev, dtype=torch.int32)
+    counts = torch.zeros(N, dtype=torch.int64, device=dev)
+    counts[cells] = counts_c
+    return {"link_off": link_off, "link_hdr": hdr, "link_w": torch.stack([w1, w2], dim=1).contiguous(),
+            "link_cells": cells.to(torch.int32).contiguous(), "counts": counts, "n_links": L}
 
 
 class FusedLBM:
@@ -115,14 +125,19 @@ class FusedLBM:
         # links
         self.has_links = bool(getattr(sim, "ibb_data", None) is not None and int(sim.ibb_data.n_links) > 0)
         if self.has_links:
-            self.link_off, self.link_meta, self.link_w, counts = build_link_table(sim.ibb_data, solid, nx, ny, nz)
-            # bit1 = has links, high nibble = link count (15 = 15 or more)
-            flags |= (counts > 0).to(torch.uint8) * CF_LINK
-            flags |= (counts.clamp(max=15).to(torch.uint8) << 4)
-            self.n_links = int(self.link_meta.numel())
+            t = build_link_table(sim.ibb_data, solid, nx, ny, nz)
+            self.link_off, self.link_hdr, self.link_w = t["link_off"], t["link_hdr"], t["link_w"]
+            self.link_cells = t["link_cells"]
+            # bit1 = has links, high nibble = link count (15 = 15 or more; informational)
+            flags |= (t["counts"] > 0).to(torch.uint8) * CF_LINK
+            flags |= (t["counts"].clamp(max=15).to(torch.uint8) << 4)
+            self.n_links = int(t["n_links"])
         else:
-            self.link_off = self.link_meta = self.link_w = None
+            self.link_off = self.link_hdr = self.link_w = None
+            self.link_cells = None
             self.n_links = 0
+        # link cells are handled inside the main pass unless cfg.lbm_link_pass == "separate"
+        self.separate_link_pass = str(getattr(cfg, "lbm_link_pass", "inline")).lower() == "separate"
         # inlet/outlet planes are finished by the plane BC kernels after the fused pass
         f3 = flags.view(nx, ny, nz)
         self.planes = []
@@ -158,6 +173,9 @@ class FusedLBM:
         self.k = 0          # steps taken since priming
         self.cur = 0        # P[cur] holds the latest post-collision populations
         self.primed = False
+        self.use_graphs = bool(getattr(cfg, "lbm_cuda_graph", True))
+        self._graphs = {}
+        self._eager_steps = 0
         self.args = StepArgs()
         self._fill_static_args()
 
@@ -172,12 +190,16 @@ class FusedLBM:
         a.f32 = ptr(sim.f)
         a.cell_flags = ptr(self.flags)
         a.link_off = ptr(self.link_off)
-        a.link_meta = ptr(self.link_meta)
+        a.link_hdr = ptr(self.link_hdr)
         a.link_w = ptr(self.link_w)
         a.n_links = self.n_links
         a.sponge = ptr(self.sponge)
         a.sponge_axis = self.sponge_axis
         a.has_links = int(self.has_links)
+        a.phase_mask = 3
+        a.separate_link_pass = int(self.separate_link_pass)
+        a.link_cells = ptr(self.link_cells)
+        a.n_link_cells = 0 if self.link_cells is None else int(self.link_cells.numel())
         a.dev_err = ptr(self.dev_err)
         self.refresh_params()
 
@@ -209,6 +231,8 @@ class FusedLBM:
     def invalidate(self):
         """Forget the stored post-collision state; the next step re-primes from sim.f."""
         self.primed = False
+        self._graphs.clear()
+        self._eager_steps = 0
 
     # -- stepping --------------------------------------------------------------
     def _prime(self):
@@ -218,6 +242,8 @@ class FusedLBM:
         if sim.f.dtype != torch.float32 or not sim.f.is_contiguous():
             raise RuntimeError("sim.f must be a contiguous float32 tensor")
         a.f32 = ptr(sim.f)
+        self._graphs.clear()
+        self._eager_steps = 0
         st = stream_ptr()
         for m in self.M:
             for t in m:
@@ -233,17 +259,12 @@ class FusedLBM:
         self.k = 0
         self.primed = True
 
-    def step(self, phase_event=None):
+    def _enqueue(self, cur, m_out, phase_event=None):
+        """Launch one step's kernels: fused pass P[cur] -> P[1-cur], then the plane BCs."""
         sim, a = self.sim, self.args
-        if not self.primed:
-            self._prime()
         st = stream_ptr()
-        k = self.k + 1          # reference step number being completed
-        nxt = 1 - self.cur
-        write_m = (k % self.macro_stride) == 0
-        m_out = self.M[k % 2] if write_m else None
-        a.pop_in = ptr(self.P[self.cur])
-        a.pop_out = ptr(self.P[nxt])
+        a.pop_in = ptr(self.P[cur])
+        a.pop_out = ptr(self.P[1 - cur])
         a.f32 = ptr(sim.f)
         self._set_macros(m_out)
         _lib.call("fc_lbm_fused_step", a, st)
@@ -254,10 +275,58 @@ class FusedLBM:
             _apply_flow_bcs_cuda(sim)
             for ax, pidx in self.planes:
                 _lib.call("fc_lbm_collide_from_f32", a, ax, pidx, st)
+
+    def _graph(self, cur):
+        """CUDA graph of one step without macro output, captured on first use (per parity)."""
+        key = (cur, self.sim.f.data_ptr())
+        g = self._graphs.get(key)
+        if g is None:
+            g = torch.cuda.CUDAGraph()
+            with torch.cuda.graph(g):
+                self._enqueue(cur, None)
+            self._graphs[key] = g
+        return g
+
+    def step(self, phase_event=None):
+        if not self.primed:
+            self._prime()
+        k = self.k + 1          # reference step number being completed
+        nxt = 1 - self.cur
+        write_m = (k % self.macro_stride) == 0
+        if self.use_graphs and not write_m and phase_event is None and self._eager_steps >= 1:
+            self._graph(self.cur).replay()
+        else:
+            self._enqueue(self.cur, self.M[k % 2] if write_m else None, phase_event)
+            self._eager_steps += 1
         self.cur = nxt
         self.k = k
         # the reference exposes the pre-collision macros of this step's input state
         self._expose(self.M[(k - 1) % 2])
+
+    def time_passes(self, n: int):
+        """Mean device time (ms) of the main fused pass and of the link-cell pass over n launches,
+        measured with CUDA events on the current stream.  Leaves the populations advanced by
+        n steps without plane boundary conditions: call it after the measured run."""
+        a = self.args
+        out = {}
+        for name, mask in (("main", 1), ("links", 2)):
+            if mask == 2 and not (a.n_link_cells and a.separate_link_pass):
+                continue
+            a.phase_mask = mask
+            ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(n)]
+            cur = self.cur
+            for e0, e1 in ev:
+                a.pop_in = ptr(self.P[cur])
+                a.pop_out = ptr(self.P[1 - cur])
+                self._set_macros(None)
+                e0.record()
+                _lib.call("fc_lbm_fused_step", a, stream_ptr())
+                e1.record()
+                cur = 1 - cur
+            torch.cuda.synchronize()
+            out[name] = sum(e0.elapsed_time(e1) for e0, e1 in ev) / n
+        a.phase_mask = 3
+        return out
 
     def sync_f(self):
         """Write the current post-stream populations S_k into sim.f."""

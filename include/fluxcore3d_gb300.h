@@ -89,9 +89,9 @@ typedef struct fc_lbm_step_args {
     float* v;
     float* w;
     const uint8_t* cell_flags;   /* [N] bit0 solid, bit1 has links, bit2 deferred plane, bit3 export */
-    const int32_t* link_off;     /* [N] first link of the cell (read only where bit1 is set) */
-    const uint8_t* link_meta;    /* [n_links] dir | mode<<5 | last<<7 ; mode 0 q>=1/2, 1 q<1/2, 2 fallback */
-    const float* link_w;         /* [n_links][2] (w1, w2) */
+    const int32_t* link_off;     /* [N] link-cell ordinal of the cell (read only where bit1 is set) */
+    const uint32_t* link_hdr;    /* [n_link_cells][4] (dir mask, second-node mask, first weight, 0); 16-B aligned */
+    const float* link_w;         /* [n_links][2] (w1, w2) per link, cells in ordinal order, dirs ascending */
     long long n_links;
     const float* sponge;         /* sigma per plane along sponge_axis, or NULL */
     int32_t sponge_axis;
@@ -100,6 +100,10 @@ typedef struct fc_lbm_step_args {
     float S[19];
     float Cs_dx2, omega0;
     unsigned* dev_err;           /* device error word (bit0 index out of range), may be NULL */
+    const int32_t* link_cells;   /* [n_link_cells] ascending cell list (ordinal order) */
+    long long n_link_cells;
+    int32_t phase_mask;          /* bit0 main pass, bit1 link-cell pass (0 is read as 3) */
+    int32_t separate_link_pass;  /* 1: the main pass skips link cells and a second kernel runs them */
 } fc_lbm_step_args;
 
 /* One full time step for every non-deferred cell. */
@@ -198,6 +202,53 @@ int fc_thermal_steady_residual(const float* T, const float* aE, const float* aW,
                                const float* aU, const float* aD, const float* diagL, const float* src_step,
                                const float* mask, float dt, int nx, int ny, int nz, int ax, int out_idx,
                                void* workspace, long long workspace_bytes, float* result, void* stream);
+
+/* ---------------------------------------------------------------------------
+ * BF16 implicit-GEMM 3-D convolutions on tcgen05 (learned preconditioner;
+ * no counterpart in the reference).  Activations channels-last BF16
+ * [B][D][H][W][C] (16-byte aligned), weights BF16 [C_out][kpad] with
+ * K = 27 C_in tap-major (tap = (dz+1)*9 + (dy+1)*3 + (dx+1)), kpad a multiple
+ * of 64 >= 27 C_in, zero padding outside each volume.  dev_err bit2 = a
+ * bounded mbarrier wait timed out.
+ * ------------------------------------------------------------------------- */
+/* Y = act(conv(X, W) + bias); C_in % 8 == 0, C_out % 16 == 0, 16 <= C_out <= 256 */
+int fc_conv3d_fwd(const void* X, const void* Wt, const float* bias, int B, int D, int H, int W, int cin, int cout,
+                  int kpad, int relu, float* Y_f32, void* Y_bf16, unsigned* dev_err, void* stream);
+long long fc_conv3d_dgrad_workspace_bytes(int cin, int cout);
+/* dX = conv^T(dY, W); C_in % 16 == 0 */
+int fc_conv3d_dgrad(const void* dY, const void* Wt, int B, int D, int H, int W, int cin, int cout, int kpad,
+                    void* workspace, long long workspace_bytes, float* dX_f32, void* dX_bf16, unsigned* dev_err,
+                    void* stream);
+long long fc_conv3d_wgrad_workspace_bytes(int B, int D, int H, int W, int cin, int cout, int splits);
+/* dW[n][k] (FP32, k < 27 C_in written) = sum over voxels of X (x) dY, split-K over `splits` CTAs columns */
+int fc_conv3d_wgrad(const void* X, const void* dY, int B, int D, int H, int W, int cin, int cout, int kpad,
+                    int splits, void* workspace, long long workspace_bytes, float* dW, unsigned* dev_err,
+                    void* stream);
+
+/* ---------------------------------------------------------------------------
+ * Learned-preconditioner network glue (no counterpart in the reference):
+ * channels-last BF16 activations, FP32 gradients.
+ * ------------------------------------------------------------------------- */
+/* 8-channel BF16 input: c0 = r * inv_scale[b], c1 = (log k - k_shift) * k_scale, c2..7 = 0 */
+int fc_nn_pack_input(const float* r, const float* k, const float* inv_scale, long long vox_per_b, long long nvox,
+                     float k_shift, float k_scale, void* out, void* stream);
+int fc_nn_avgpool2(const void* x, int B, int D, int H, int W, int C, void* y, void* stream);
+int fc_nn_avgpool2_bwd(const float* gy, int B, int D, int H, int W, int C, float* gx, void* stream);
+/* y[..., 0:Cx] = nearest-2x-upsampled x, y[..., Cx:Cx+Cs] = skip (D, H, W: fine extents) */
+int fc_nn_upsample_concat(const void* x, int Cx, const void* skip, int Cs, int B, int D, int H, int W, void* y,
+                          void* stream);
+int fc_nn_upsample_concat_bwd(const float* gy, int Cx, int Cs, int B, int D, int H, int W, float* gx, float* gskip,
+                              void* stream);
+/* gout = (g + add) * [y > 0] (ReLU) or g + add, FP32 and/or BF16 */
+int fc_nn_act_bwd(const float* g, const float* add, const void* y, int relu, long long n, float* gout,
+                  void* gout_bf16, void* stream);
+int fc_nn_take_channel0(const float* y, int C, const float* scale, long long vox_per_b, long long nvox,
+                        const float* mask, float* out, void* stream);
+long long fc_nn_mse_workspace_bytes(long long nvox);
+int fc_nn_mse_grad(const float* y, int C, const float* target, const float* mask, long long nvox, float* grad,
+                   void* workspace, long long workspace_bytes, void* stream);
+int fc_nn_adam(float* w, const float* g, float* m, float* v, void* w_bf16, long long n, int kpad, int kvalid,
+               float lr, float beta1, float beta2, float eps, int step, float grad_scale, void* stream);
 
 #ifdef __cplusplus
 }

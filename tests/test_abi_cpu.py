@@ -66,22 +66,39 @@ def test_face_roles_table():
 def test_link_table_groups_links_by_cell():
     from fluxcore3d_gb300 import geometry as geo
     from fluxcore3d_gb300.solver.fused_lbm import build_link_table
-    solid = geo.cube_mask((12, 10, 9), (6, 5, 4), (4, 4, 4))
-    phi = torch.tensor(geo.phi_from_voxels(solid.numpy()), dtype=torch.float32)
+    d = np.load(os.path.join(ROOT, "tests", "golden", "ibb_links.npz"))
+    solid = torch.from_numpy(d["heatsink_solid"])
+    phi = torch.from_numpy(d["heatsink_phi"]).to(torch.float32)
     ibb = geo.ibb_from_phi_trilinear(solid, phi)
-    off, meta, w, counts = build_link_table(ibb, solid.to(torch.uint8).reshape(-1), 12, 10, 9)
-    assert int(counts.sum()) == ibb.n_links
-    # every link reachable from its cell and terminated by the last bit
-    seen = 0
-    for cell in torch.nonzero(counts).reshape(-1).tolist():
-        l0 = int(off[cell])
-        c = int(counts[cell])
-        dirs = [int(meta[l0 + t]) & 31 for t in range(c)]
-        assert all(int(meta[l0 + t]) & 0x80 == 0 for t in range(c - 1)) and int(meta[l0 + c - 1]) & 0x80
-        ref = sorted(int(d) for d, f in zip(ibb.dir_i.tolist(), ibb.fluid_flat.tolist()) if f == cell)
-        assert dirs == ref
-        seen += c
-    assert seen == ibb.n_links
+    nx, ny, nz = solid.shape
+    t = build_link_table(ibb, solid.to(torch.uint8).reshape(-1), nx, ny, nz)
+    assert t["n_links"] == ibb.n_links and int(t["counts"].sum()) == ibb.n_links
+    ref = {}
+    for f, dd, g, fv, w1, w2 in zip(ibb.fluid_flat.tolist(), ibb.dir_i.tolist(), ibb.q_ge_half.tolist(),
+                                    ibb.ff_valid.tolist(), ibb.w_i.tolist(), ibb.w_second.tolist()):
+        ref[(f, dd)] = (g, fv, w1, w2)
+    hdr = t["link_hdr"].numpy().astype(np.int64)
+    lw = t["link_w"].numpy()
+    cells = t["link_cells"].numpy()
+    assert np.all(np.diff(cells) > 0)
+    n_modes = {"ge": 0, "ff": 0, "fallback": 0}
+    for o, cell in enumerate(cells):
+        assert int(t["link_off"][cell]) == o
+        mask, smask, w0 = hdr[o, 0], hdr[o, 1], hdr[o, 2]
+        dirs = [q for q in range(1, 19) if (mask >> q) & 1]
+        for r, q in enumerate(dirs):
+            g, fv, w1, w2 = ref[(int(cell), q)]
+            second = bool((smask >> q) & 1)
+            if g:
+                assert not second and (lw[w0 + r] == np.float32([w1, w2])).all()
+                n_modes["ge"] += 1
+            elif fv:
+                assert second and (lw[w0 + r] == np.float32([w1, w2])).all()
+                n_modes["ff"] += 1
+            else:
+                assert not second and (lw[w0 + r] == np.float32([1.0, 0.0])).all()
+                n_modes["fallback"] += 1
+    assert sum(n_modes.values()) == ibb.n_links and n_modes["ff"] > 0
 
 
 def test_link_table_rejects_inconsistent_data():

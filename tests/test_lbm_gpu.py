@@ -62,7 +62,22 @@ def test_fused_step_fp32_matches_oracle_small(cuda, collision):
     e = rel_l2(sim.f.reshape(19, N).cpu().numpy(), orc.f)
     assert e < 1e-5, e
     assert rel_l2(sim.u.reshape(-1).cpu().numpy(), orc.u) < 1e-4
-    assert rel_l2(sim.rho.reshape(-1).cpu().numpy(), orc.rho) < 1e-6
+    assert rel_l2(sim.rho.reshape(-1).cpu().numpy(), orc.rho) < 1e-5
+
+
+@pytest.mark.parametrize("storage", ["fp32", "fp16"])
+def test_pin_fin_all_link_modes(cuda, storage):
+    """Small pin-fin heat sink with analytic link fractions: q >= 1/2, q < 1/2 with a second
+    fluid node, and q < 1/2 without one all occur; MRT, pressure outlet, sponge."""
+    sim = cases.pin_fin(device=cuda, collision="mrt", storage=storage, nx=48, ny=32, nz=40,
+                        n_pins=(3, 2), radius=3.5, height=24, base=4, sponge_length=8)
+    d = sim.ibb_data
+    ge, fv = d.q_ge_half.bool(), d.ff_valid.bool()
+    assert bool(ge.any()) and bool((~ge & fv).any())
+    orc = run_pair(sim, 200, real="f32" if storage == "fp32" else "f64")
+    N = sim.nx * sim.ny * sim.nz
+    e = rel_l2(sim.f.reshape(19, N).cpu().numpy(), orc.f)
+    assert e < (1e-5 if storage == "fp32" else 2e-4), e
 
 
 def test_fused_step_c1_channel_1000_steps(cuda):
@@ -72,6 +87,16 @@ def test_fused_step_c1_channel_1000_steps(cuda):
     N = sim.nx * sim.ny * sim.nz
     e = rel_l2(sim.f.reshape(19, N).cpu().numpy(), orc.f)
     assert e < 1e-5, e
+
+
+def test_fused_step_separate_link_pass_matches(cuda):
+    """The two-pass variant (link cells in their own kernel) gives the same result."""
+    sim = cases.channel_cube(device=cuda, collision="mrt", nx=32, ny=16, nz=16, cube=6, cube_x=10,
+                             sponge_length=8, outlet="pressure")
+    sim.cfg.lbm_link_pass = "separate"
+    orc = run_pair(sim, 100)
+    N = sim.nx * sim.ny * sim.nz
+    assert rel_l2(sim.f.reshape(19, N).cpu().numpy(), orc.f) < 1e-5
 
 
 def test_fused_step_no_links_periodic(cuda):
@@ -89,7 +114,7 @@ def test_fused_step_convective_and_macro_lag(cuda):
     orc = run_pair(sim, 50)
     # macros after step k are those of the step's input state (reference semantics)
     assert rel_l2(sim.v.reshape(-1).cpu().numpy(), orc.v) < 1e-4
-    assert rel_l2(sim.rho.reshape(-1).cpu().numpy(), orc.rho) < 1e-6
+    assert rel_l2(sim.rho.reshape(-1).cpu().numpy(), orc.rho) < 1e-5
 
 
 @pytest.mark.parametrize("storage", ["fp16", "bf16"])
