@@ -325,7 +325,9 @@ __global__ void k_flip_weights(const __nv_bfloat16* __restrict__ W, __nv_bfloat1
 }
 
 inline size_t smem_bytes(int N) {
-    size_t b = 2 * (size_t)(TM * KC * 2 + N * KC * 2) + 64;
+    // two stages + barriers, plus 32 KB of slack past the last operand byte so that no
+    // descriptor stride read can leave the allocation
+    size_t b = 2 * (size_t)(TM * KC * 2 + N * KC * 2) + 64 + 32768;
     int ncols = 32;
     while (ncols < N) ncols <<= 1;
     // keep (CTAs per SM) x ncols <= 512 TMEM columns: make the smem footprint cap residency
