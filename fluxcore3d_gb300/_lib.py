@@ -77,6 +77,8 @@ SIGNATURES: dict[str, tuple] = {
     "fc_lbm_zou_he_bc": (i32, [vp, vp, i32, i32, i32, i32, i32, i32, i32, f32, f32, i32, vp]),
     "fc_lbm_convective_workspace_bytes": (i64, [i32, i32]),
     "fc_lbm_convective_bc": (i32, [vp, vp, i32, i32, i32, i32, i32, i32, i32, f32, i32, i32, vp, i64, vp]),
+    "fc_lbm_convective_noalloc_max_plane": (i64, []),
+    "fc_lbm_convective_bc_noalloc": (i32, [vp, vp, i32, i32, i32, i32, i32, i32, i32, f32, i32, i32, vp]),
     # lattice, fused
     "fc_lbm_fused_step": (i32, [C.POINTER(StepArgs), vp]),
     "fc_lbm_collide_from_f32": (i32, [C.POINTER(StepArgs), i32, i32, vp]),
@@ -127,7 +129,8 @@ SIGNATURES: dict[str, tuple] = {
     "fc_nn_adam": (i32, [vp, vp, vp, vp, vp, i64, i32, i32, f32, f32, f32, f32, i32, f32, vp]),
 }
 
-STATUS_TEXT = {1: "bad argument", 2: "CUDA launch failure", 3: "unsupported combination"}
+STATUS_TEXT = {1: "bad argument", 2: "CUDA launch failure", 3: "unsupported combination",
+               4: "size exceeds the fixed capacity of this entry point"}
 
 
 def lib_path() -> str:

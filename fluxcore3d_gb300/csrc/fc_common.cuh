@@ -49,7 +49,8 @@ enum Status : int {
     FC_OK = 0,
     FC_ERR_ARG = 1,        // bad argument (null pointer, size, mode)
     FC_ERR_LAUNCH = 2,     // cudaGetLastError after launch was not cudaSuccess
-    FC_ERR_UNSUPPORTED = 3 // valid but not implemented combination
+    FC_ERR_UNSUPPORTED = 3, // valid but not implemented combination
+    FC_ERR_TOO_LARGE = 4    // request exceeds a fixed capacity of the library
 };
 enum DevErr : unsigned {
     DEV_ERR_INDEX = 1u,      // an index read from a table was out of range

@@ -23,6 +23,8 @@
 #include "fc_collide.cuh"
 #include "../../include/fluxcore3d_gb300.h"
 
+#include <mutex>
+
 using namespace fc;
 
 namespace {
@@ -841,6 +843,74 @@ int fc_lbm_convective_bc(float* f, const uint8_t* solid, int nx, int ny, int nz,
     k_convective_pass1<<<nb, BLOCK, 0, st>>>(f, solid, nx, ny, nz, axis, outlet_idx, interior_idx, unknown_cax,
                                              n1, n2, part_rho, part_cnt);
     int rc = launch_status();
+    if (rc) return rc;
+    k_convective_pass2<<<nb, BLOCK, 0, st>>>(f, solid, nx, ny, nz, axis, outlet_idx, rho_out_lat, n1, n2,
+                                             part_rho, part_cnt, nb);
+    return launch_status();
+}
+
+// ---------------------------------------------------------------------------
+// Convective outlet without any device allocation.
+//
+// Some callers cannot allocate device memory once their time loop runs: hosts
+// that hand out all GPU memory from their own pre-reserved arena (a coupled
+// solver driving this library from C or Fortran), or code paths where an
+// allocation would have to synchronise the device.  For them this entry point
+// keeps the plane-reduction partials in a fixed file-scope device array
+// instead of a caller workspace.  Capacity: FC_NOALLOC_CONVECTIVE_MAX_BLOCKS
+// partial slots, i.e. outlet planes of at most 4096 * 256 = 1,048,576 nodes
+// (49,152 bytes, held by every GPU that loads the library until the process
+// exits).  Larger planes are rejected with FC_ERR_TOO_LARGE.
+//
+// The device address of the array is looked up with cudaGetSymbolAddress on
+// the first call made on each device (with that device current) and cached;
+// make that first call before any stream capture.  All calls share the one
+// array, so calls whose kernels overlap on the GPU (different streams without
+// ordering) race on it.  Every slot the second pass reads is written by the
+// first pass of the same call, so nothing has to be cleared between calls.
+// ---------------------------------------------------------------------------
+#define FC_NOALLOC_CONVECTIVE_MAX_BLOCKS 4096
+static __device__ __align__(256) unsigned char g_noalloc_convective_scratch[FC_NOALLOC_CONVECTIVE_MAX_BLOCKS *
+                                                                            (sizeof(double) + sizeof(int))];
+static std::mutex g_noalloc_mutex;
+static void* g_noalloc_ptr[64] = {nullptr};
+
+static int noalloc_scratch(void** out) {
+    int dev = -1;
+    if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= 64) return FC_ERR_LAUNCH;
+    std::lock_guard<std::mutex> lock(g_noalloc_mutex);
+    if (!g_noalloc_ptr[dev]) {
+        void* p = nullptr;
+        if (cudaGetSymbolAddress(&p, g_noalloc_convective_scratch) != cudaSuccess || !p) return FC_ERR_LAUNCH;
+        g_noalloc_ptr[dev] = p;
+    }
+    *out = g_noalloc_ptr[dev];
+    return FC_OK;
+}
+
+long long fc_lbm_convective_noalloc_max_plane(void) { return (long long)FC_NOALLOC_CONVECTIVE_MAX_BLOCKS * BLOCK; }
+
+int fc_lbm_convective_bc_noalloc(float* f, const uint8_t* solid, int nx, int ny, int nz, int axis, int outlet_idx,
+                                 int interior_idx, int unknown_cax, float rho_out_lat, int n1, int n2, void* stream) {
+    if (!f || !solid || nx < 1 || ny < 1 || nz < 1) return FC_ERR_ARG;
+    int e1, e2;
+    if (plane_dims(axis, nx, ny, nz, &e1, &e2)) return FC_ERR_ARG;
+    if (e1 != n1 || e2 != n2) return FC_ERR_ARG;
+    const int na = axis == 0 ? nx : (axis == 1 ? ny : nz);
+    if (outlet_idx < 0 || outlet_idx >= na || interior_idx < 0 || interior_idx >= na) return FC_ERR_ARG;
+    if (unknown_cax != 1 && unknown_cax != -1) return FC_ERR_ARG;
+    const long long nbl = ((long long)n1 * n2 + BLOCK - 1) / BLOCK;
+    if (nbl > FC_NOALLOC_CONVECTIVE_MAX_BLOCKS) return FC_ERR_TOO_LARGE;
+    void* scratch = nullptr;
+    int rc = noalloc_scratch(&scratch);
+    if (rc) return rc;
+    const int nb = (int)nbl;
+    double* part_rho = reinterpret_cast<double*>(scratch);
+    int* part_cnt = reinterpret_cast<int*>(part_rho + FC_NOALLOC_CONVECTIVE_MAX_BLOCKS);
+    cudaStream_t st = (cudaStream_t)stream;
+    k_convective_pass1<<<nb, BLOCK, 0, st>>>(f, solid, nx, ny, nz, axis, outlet_idx, interior_idx, unknown_cax,
+                                             n1, n2, part_rho, part_cnt);
+    rc = launch_status();
     if (rc) return rc;
     k_convective_pass2<<<nb, BLOCK, 0, st>>>(f, solid, nx, ny, nz, axis, outlet_idx, rho_out_lat, n1, n2,
                                              part_rho, part_cnt, nb);

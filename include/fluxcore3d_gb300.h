@@ -6,7 +6,7 @@
  * Conventions
  *   - Every pointer argument is a device pointer unless its name ends in _host.
  *   - Every function returns an int status: 0 ok, 1 bad argument, 2 launch
- *     failure, 3 unsupported combination.  Nothing in this library allocates
+ *     failure, 3 unsupported combination, 4 size beyond a fixed capacity.  Nothing in this library allocates
  *     device memory behind the caller's back: scratch space is passed in as a
  *     workspace pointer whose size the matching *_workspace_bytes() reports.
  *   - `stream` is a cudaStream_t passed as void*; NULL is the legacy stream.
@@ -71,6 +71,18 @@ long long fc_lbm_convective_workspace_bytes(int n1, int n2);
 int fc_lbm_convective_bc(float* f, const uint8_t* solid, int nx, int ny, int nz, int axis, int outlet_idx,
                          int interior_idx, int unknown_cax, float rho_out_lat, int n1, int n2,
                          void* workspace, long long workspace_bytes, void* stream);
+/* Convective outlet that allocates nothing: no counterpart in the reference.  For callers
+ * that may not allocate device memory once their time loop runs (a host that hands out all
+ * GPU memory from its own pre-reserved arena, or a path where an allocation would
+ * synchronise the device).  Same result as fc_lbm_convective_bc, with the plane partials
+ * kept in a fixed file-scope device array (49,152 bytes per GPU that loads the library,
+ * held until exit): planes of at most fc_lbm_convective_noalloc_max_plane() = 1,048,576
+ * nodes, larger ones return 4.  The first call on each device looks the array up and
+ * caches its address; make it before any stream capture.  Calls share the array, so calls
+ * that overlap on the GPU race on it. */
+long long fc_lbm_convective_noalloc_max_plane(void);
+int fc_lbm_convective_bc_noalloc(float* f, const uint8_t* solid, int nx, int ny, int nz, int axis, int outlet_idx,
+                                 int interior_idx, int unknown_cax, float rho_out_lat, int n1, int n2, void* stream);
 
 /* ---------------------------------------------------------------------------
  * Fused step (replaces the collide -> sponge -> stream -> ibb -> reset_solid
