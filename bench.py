@@ -108,6 +108,7 @@ def make_case(device, storage, args):
     sim = cases.pin_fin(device=device, collision=args.collision, storage=storage, nx=args.nx, ny=args.ny,
                         nz=args.nz)
     sim.cfg.macro_stride = args.macro_stride
+    sim.cfg.lbm_cells_per_thread = getattr(args, "cells_per_thread", 1)
     return sim
 
 
@@ -220,6 +221,7 @@ def main():
     ap.add_argument("--ny", type=int, default=128)
     ap.add_argument("--nz", type=int, default=128)
     ap.add_argument("--macro-stride", type=int, default=100)
+    ap.add_argument("--cells-per-thread", type=int, default=1, choices=(1, 2))
     ap.add_argument("--cpu-steps", type=int, default=3)
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")

@@ -59,6 +59,7 @@ class StepArgs(C.Structure):
         ("n_link_cells", i64),
         ("phase_mask", C.c_int32),
         ("separate_link_pass", C.c_int32),
+        ("cells_per_thread", C.c_int32),
     ]
 
 

@@ -134,6 +134,34 @@ class LatticeCase:
         self._sponge_axis = axis
         self._sponge_outlet_idx = out
 
+    # thermal set-up used by the pseudo-time step (LBM_CHT.py:2133-2167, 2361-2386)
+    @property
+    def ax(self):
+        return "XYZ".index(self.cfg.flow_dir.upper().strip()[1])
+
+    @property
+    def sign(self):
+        return +1 if self.cfg.flow_dir.upper().strip()[0] == "+" else -1
+
+    def _build_update_mask_thermal(self):
+        m = torch.ones((self.nx, self.ny, self.nz), dtype=torch.bool, device=self.device)
+        if self.cfg.temp_bc == "periodic":
+            return m
+        n = (self.nx, self.ny, self.nz)[self.ax]
+        sl = [slice(None)] * 3
+        sl[self.ax] = 0 if self.sign > 0 else n - 1
+        m[tuple(sl)] = False
+        return m
+
+    def _build_T_dirichlet_field(self):
+        return torch.full((self.nx, self.ny, self.nz), float(self.fluid.tin_C), device=self.device)
+
+    def _compute_heat_source(self):
+        return getattr(self, "heat_source", None)
+
+    def _compute_surface_flux_sources(self):
+        return torch.zeros((self.nx, self.ny, self.nz), device=self.device)
+
     # methods the patch layer saves or replaces
     def _macroscopic(self):
         N = self.nx * self.ny * self.nz

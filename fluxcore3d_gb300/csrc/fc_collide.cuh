@@ -218,22 +218,43 @@ struct MacroH {
     float drho, rho, inv_rho, jx, jy, jz, ux, uy, uz;
 };
 
-__device__ __forceinline__ MacroH macros_h(const float h[19]) {
+// Shared partial sums of the 19 shifted populations: every conserved and
+// non-conserved moment below is one or two adds away from these.
+struct PairSums {
+    float Fx, Fy, Fz, dx1, dy1, dz1;        // face pairs: h1+h2, ... and h1-h2, ...
+    float Sxy, Sxz, Syz;                    // edge-plane sums
+    float jxe_xy, jxe_xz, jye_xy, jye_yz, jze_xz, jze_yz;
+    float p13, p14, p15;                    // raw xy, yz, xz second moments
+};
+
+__device__ __forceinline__ PairSums pair_sums(const float h[19]) {
+    PairSums p;
+    p.Fx = h[1] + h[2]; p.Fy = h[3] + h[4]; p.Fz = h[5] + h[6];
+    p.dx1 = h[1] - h[2]; p.dy1 = h[3] - h[4]; p.dz1 = h[5] - h[6];
+    const float a78 = h[7] + h[8], a910 = h[9] + h[10], d78 = h[7] - h[8], d910 = h[9] - h[10];
+    const float a1112 = h[11] + h[12], a1314 = h[13] + h[14], d1112 = h[11] - h[12], d1314 = h[13] - h[14];
+    const float a1516 = h[15] + h[16], a1718 = h[17] + h[18], d1516 = h[15] - h[16], d1718 = h[17] - h[18];
+    p.Sxy = a78 + a910; p.jxe_xy = a78 - a910; p.jye_xy = d78 + d910; p.p13 = d78 - d910;
+    p.Sxz = a1112 + a1314; p.jxe_xz = a1112 - a1314; p.jze_xz = d1112 + d1314; p.p15 = d1112 - d1314;
+    p.Syz = a1516 + a1718; p.jye_yz = a1516 - a1718; p.jze_yz = d1516 + d1718; p.p14 = d1516 - d1718;
+    return p;
+}
+
+__device__ __forceinline__ MacroH macros_from(const float h0, const PairSums& p) {
     MacroH m;
-    float d = 0.f;
-#pragma unroll
-    for (int q = 0; q < 19; ++q) d += h[q];
-    m.drho = d;
-    m.rho = 1.f + d;
-    m.jx = (h[1] - h[2]) + ((h[7] + h[8]) - (h[9] + h[10])) + ((h[11] + h[12]) - (h[13] + h[14]));
-    m.jy = (h[3] - h[4]) + ((h[7] - h[8]) + (h[9] - h[10])) + ((h[15] + h[16]) - (h[17] + h[18]));
-    m.jz = (h[5] - h[6]) + ((h[11] - h[12]) + (h[13] - h[14])) + ((h[15] - h[16]) + (h[17] - h[18]));
+    m.drho = h0 + ((p.Fx + p.Fy) + p.Fz) + ((p.Sxy + p.Sxz) + p.Syz);
+    m.rho = 1.f + m.drho;
+    m.jx = p.dx1 + (p.jxe_xy + p.jxe_xz);
+    m.jy = p.dy1 + (p.jye_xy + p.jye_yz);
+    m.jz = p.dz1 + (p.jze_xz + p.jze_yz);
     m.inv_rho = __frcp_rn(m.rho + 1e-12f);
     m.ux = m.jx * m.inv_rho;
     m.uy = m.jy * m.inv_rho;
     m.uz = m.jz * m.inv_rho;
     return m;
 }
+
+__device__ __forceinline__ MacroH macros_h(const float h[19]) { return macros_from(h[0], pair_sums(h)); }
 
 // h_eq,q = f_eq,q - w_q = w_q (drho + rho (cu + cu^2/2 - 3/2 u.u))
 __device__ __forceinline__ void equilibrium_h(const MacroH& m, float heq[19]) {
@@ -252,9 +273,48 @@ __device__ __forceinline__ void equilibrium_h(const MacroH& m, float heq[19]) {
     }
 }
 
+// Subtract d_q = sum_k M[k][q] g_k (g_k = S_k n_k / |M_k|^2) from h, with the
+// +-pattern of each edge quartet factored into two pairs of pairs.
+__device__ __forceinline__ void apply_minv(float h[19], float g1, float g2, float g4, float g6, float g8, float g9,
+                                           float g10, float g11, float g12, float g13, float g14, float g15,
+                                           float g16, float g17, float g18) {
+    h[0] -= -30.f * g1 + 12.f * g2;
+    const float face = -11.f * g1 - 4.f * g2;
+    const float fx_ = face + 2.f * g9 - 4.f * g10;
+    h[1] -= fx_ - 4.f * g4;
+    h[2] -= fx_ + 4.f * g4;
+    const float fyz = face - g9 + 2.f * g10;
+    const float fy_ = fyz + g11 - 2.f * g12;
+    const float fz_ = fyz - g11 + 2.f * g12;
+    h[3] -= fy_ - 4.f * g6;
+    h[4] -= fy_ + 4.f * g6;
+    h[5] -= fz_ - 4.f * g8;
+    h[6] -= fz_ + 4.f * g8;
+    const float edge = 8.f * g1 + g2;
+    {   // xy edges 7..10: exy +- (g4 + g16) +- ((g6 - g17) +- g13)
+        const float exy = edge + g9 + g10 + g11 + g12;
+        const float a = g4 + g16, b = g6 - g17;
+        const float s1 = exy + a, s2 = exy - a, t1 = b + g13, t2 = b - g13;
+        h[7] -= s1 + t1; h[8] -= s1 - t1; h[9] -= s2 + t2; h[10] -= s2 - t2;
+    }
+    {   // xz edges 11..14: exz +- (g4 - g16) +- ((g8 + g18) +- g15)
+        const float exz = edge + g9 + g10 - g11 - g12;
+        const float a = g4 - g16, b = g8 + g18;
+        const float s1 = exz + a, s2 = exz - a, t1 = b + g15, t2 = b - g15;
+        h[11] -= s1 + t1; h[12] -= s1 - t1; h[13] -= s2 + t2; h[14] -= s2 - t2;
+    }
+    {   // yz edges 15..18: eyz +- (g6 + g17) +- ((g8 - g18) +- g14)
+        const float eyz = edge - 2.f * g9 - 2.f * g10;
+        const float a = g6 + g17, b = g8 - g18;
+        const float s1 = eyz + a, s2 = eyz - a, t1 = b + g14, t2 = b - g14;
+        h[15] -= s1 + t1; h[16] -= s1 - t1; h[17] -= s2 + t2; h[18] -= s2 - t2;
+    }
+}
+
 template <int MODE>
 __device__ __forceinline__ MacroH collide_h(float h[19], const CollideParams& p) {
-    const MacroH m = macros_h(h);
+    const PairSums ps = pair_sums(h);
+    const MacroH m = macros_from(h[0], ps);
     if (MODE == CM_BGK || MODE == CM_TRT) {
         float heq[19];
         equilibrium_h(m, heq);
@@ -275,44 +335,41 @@ __device__ __forceinline__ MacroH collide_h(float h[19], const CollideParams& p)
         }
         return m;
     }
-    // raw moments of h (same integer rows as mrt_df)
-    const float Fx = h[1] + h[2], Fy = h[3] + h[4], Fz = h[5] + h[6];
-    const float sf = Fx + Fy + Fz;
-    const float Sxy = h[7] + h[8] + h[9] + h[10];
-    const float Sxz = h[11] + h[12] + h[13] + h[14];
-    const float Syz = h[15] + h[16] + h[17] + h[18];
-    const float se = Sxy + Sxz + Syz;
-    const float jxe = (h[7] + h[8] - h[9] - h[10]) + (h[11] + h[12] - h[13] - h[14]);
-    const float jye = (h[7] - h[8] + h[9] - h[10]) + (h[15] + h[16] - h[17] - h[18]);
-    const float jze = (h[11] - h[12] + h[13] - h[14]) + (h[15] - h[16] + h[17] - h[18]);
+    const float sf = (ps.Fx + ps.Fy) + ps.Fz;
+    const float se = (ps.Sxy + ps.Sxz) + ps.Syz;
+    const float jxe = ps.jxe_xy + ps.jxe_xz, jye = ps.jye_xy + ps.jye_yz, jze = ps.jze_xz + ps.jze_yz;
     // equilibrium parts (rho u u = j u)
     const float uxx = m.jx * m.ux, uyy = m.jy * m.uy, uzz = m.jz * m.uz;
     const float rus = uxx + uyy + uzz;
     const float pxx = 2.f * uxx - uyy - uzz;
     const float pww = uyy - uzz;
+    const float sxyxz = ps.Sxy + ps.Sxz;
+    const float dxyxz = ps.Sxy - ps.Sxz;
     // non-equilibrium moments n_k = (M h)_k - (m_eq,k - (M w)_k)
     const float n1 = (-30.f * h[0] - 11.f * sf + 8.f * se) + 11.f * m.drho - 19.f * rus;
     const float n2 = (12.f * h[0] - 4.f * sf + se) - 3.f * m.drho + 5.5f * rus;
-    const float n4 = (-4.f * (h[1] - h[2]) + jxe) + (2.f / 3.f) * m.jx;
-    const float n6 = (-4.f * (h[3] - h[4]) + jye) + (2.f / 3.f) * m.jy;
-    const float n8 = (-4.f * (h[5] - h[6]) + jze) + (2.f / 3.f) * m.jz;
-    const float n9 = (2.f * Fx - Fy - Fz + Sxy + Sxz - 2.f * Syz) - pxx;
-    const float n10 = (-4.f * Fx + 2.f * Fy + 2.f * Fz + Sxy + Sxz - 2.f * Syz) + 0.5f * pxx;
-    const float n11 = (Fy - Fz + Sxy - Sxz) - pww;
-    const float n12 = (-2.f * Fy + 2.f * Fz + Sxy - Sxz) + 0.5f * pww;
-    const float n13 = (h[7] - h[8] - h[9] + h[10]) - m.jx * m.uy;
-    const float n14 = (h[15] - h[16] - h[17] + h[18]) - m.jy * m.uz;
-    const float n15 = (h[11] - h[12] - h[13] + h[14]) - m.jx * m.uz;
-    const float n16 = h[7] + h[8] - h[9] - h[10] - h[11] - h[12] + h[13] + h[14];
-    const float n17 = -h[7] + h[8] - h[9] + h[10] + h[15] + h[16] - h[17] - h[18];
-    const float n18 = h[11] - h[12] + h[13] - h[14] - h[15] + h[16] - h[17] + h[18];
+    const float n4 = (-4.f * ps.dx1 + jxe) + (2.f / 3.f) * m.jx;
+    const float n6 = (-4.f * ps.dy1 + jye) + (2.f / 3.f) * m.jy;
+    const float n8 = (-4.f * ps.dz1 + jze) + (2.f / 3.f) * m.jz;
+    const float fyz2 = ps.Fy + ps.Fz;
+    const float n9 = (2.f * ps.Fx - fyz2 + sxyxz - 2.f * ps.Syz) - pxx;
+    const float n10 = (-4.f * ps.Fx + 2.f * fyz2 + sxyxz - 2.f * ps.Syz) + 0.5f * pxx;
+    const float fymz = ps.Fy - ps.Fz;
+    const float n11 = (fymz + dxyxz) - pww;
+    const float n12 = (-2.f * fymz + dxyxz) + 0.5f * pww;
+    const float n13 = ps.p13 - m.jx * m.uy;
+    const float n14 = ps.p14 - m.jy * m.uz;
+    const float n15 = ps.p15 - m.jx * m.uz;
+    const float n16 = ps.jxe_xy - ps.jxe_xz;
+    const float n17 = ps.jye_yz - ps.jye_xy;
+    const float n18 = ps.jze_xz - ps.jze_yz;
     float s9 = p.SN[9], s11 = p.SN[11], s13 = p.SN[13], s14 = p.SN[14], s15 = p.SN[15];
     if (MODE == CM_MRT_SMAG) {
         // Pi_neq = Pi(h) - rho u u - (drho / 3) I
         const float third = m.drho * (1.f / 3.f);
-        const float Pxx = (Fx + Sxy + Sxz) - uxx - third;
-        const float Pyy = (Fy + Sxy + Syz) - uyy - third;
-        const float Pzz = (Fz + Sxz + Syz) - uzz - third;
+        const float Pxx = (ps.Fx + sxyxz) - uxx - third;
+        const float Pyy = (ps.Fy + ps.Sxy + ps.Syz) - uyy - third;
+        const float Pzz = (ps.Fz + ps.Sxz + ps.Syz) - uzz - third;
         const float Pxy = n13, Pyz = n14, Pxz = n15;
         const float piF = sqrtf(Pxx * Pxx + Pyy * Pyy + Pzz * Pzz + 2.f * (Pxy * Pxy + Pxz * Pxz + Pyz * Pyz));
         const float nu0 = (1.f / p.omega0 - 0.5f) * (1.f / 3.f);
@@ -322,50 +379,9 @@ __device__ __forceinline__ MacroH collide_h(float h[19], const CollideParams& p)
         s9 = om * (1.f / 36.f); s11 = om * (1.f / 12.f);
         s13 = om * 0.25f; s14 = om * 0.25f; s15 = om * 0.25f;
     }
-    const float g1 = p.SN[1] * n1;
-    const float g2 = p.SN[2] * n2;
-    const float g4 = p.SN[4] * n4;
-    const float g6 = p.SN[6] * n6;
-    const float g8 = p.SN[8] * n8;
-    const float g9 = s9 * n9;
-    const float g10 = p.SN[10] * n10;
-    const float g11 = s11 * n11;
-    const float g12 = p.SN[12] * n12;
-    const float g13 = s13 * n13;
-    const float g14 = s14 * n14;
-    const float g15 = s15 * n15;
-    const float g16 = p.SN[16] * n16;
-    const float g17 = p.SN[17] * n17;
-    const float g18 = p.SN[18] * n18;
-    h[0] -= -30.f * g1 + 12.f * g2;
-    const float face = -11.f * g1 - 4.f * g2;
-    const float fx_ = face + 2.f * g9 - 4.f * g10;
-    h[1] -= fx_ - 4.f * g4;
-    h[2] -= fx_ + 4.f * g4;
-    const float fyz = face - g9 + 2.f * g10;
-    const float fy_ = fyz + g11 - 2.f * g12;
-    const float fz_ = fyz - g11 + 2.f * g12;
-    h[3] -= fy_ - 4.f * g6;
-    h[4] -= fy_ + 4.f * g6;
-    h[5] -= fz_ - 4.f * g8;
-    h[6] -= fz_ + 4.f * g8;
-    const float edge = 8.f * g1 + g2;
-    const float exy = edge + g9 + g10 + g11 + g12;
-    h[7] -= exy + g4 + g6 + g13 + g16 - g17;
-    h[8] -= exy + g4 - g6 - g13 + g16 + g17;
-    h[9] -= exy - g4 + g6 - g13 - g16 - g17;
-    h[10] -= exy - g4 - g6 + g13 - g16 + g17;
-    const float exz = edge + g9 + g10 - g11 - g12;
-    h[11] -= exz + g4 + g8 + g15 - g16 + g18;
-    h[12] -= exz + g4 - g8 - g15 - g16 - g18;
-    h[13] -= exz - g4 + g8 - g15 + g16 + g18;
-    h[14] -= exz - g4 - g8 + g15 + g16 - g18;
-    const float eyz = edge - 2.f * g9 - 2.f * g10;
-    h[15] -= eyz + g6 + g8 + g14 + g17 - g18;
-    h[16] -= eyz + g6 - g8 - g14 + g17 + g18;
-    h[17] -= eyz - g6 + g8 - g14 - g17 - g18;
-    h[18] -= eyz - g6 - g8 + g14 - g17 + g18;
+    apply_minv(h, p.SN[1] * n1, p.SN[2] * n2, p.SN[4] * n4, p.SN[6] * n6, p.SN[8] * n8, s9 * n9,
+               p.SN[10] * n10, s11 * n11, p.SN[12] * n12, s13 * n13, s14 * n14, s15 * n15,
+               p.SN[16] * n16, p.SN[17] * n17, p.SN[18] * n18);
     return m;
 }
-
 }  // namespace fc

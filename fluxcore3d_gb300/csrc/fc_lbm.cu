@@ -537,6 +537,48 @@ __global__ void __launch_bounds__(TBX * TBY, 7) k_fused_step(const FusedArgs a) 
     collide_store<KIND, MODE>(a, idx, i, j, k, h);
 }
 
+// Two cells per thread (rows j and j+1 of the same k): both cells' pulls are in
+// flight before either collision, doubling the bytes a thread keeps in flight.
+template <int KIND, int MODE>
+__device__ __forceinline__ void finish_cell(const FusedArgs& a, int idx, int i, int j, int k, uint8_t fl,
+                                            float h[19]) {
+    if (fl & (CF_DEFER | CF_WRITE_S)) {
+        export_f(a, idx, h);
+        if (fl & CF_DEFER) return;
+    }
+    collide_store<KIND, MODE>(a, idx, i, j, k, h);
+}
+
+template <int KIND, int MODE>
+__global__ void __launch_bounds__(TBX * TBY, 6) k_fused_step2(const FusedArgs a) {
+    const int k = blockIdx.x * TBX + threadIdx.x;
+    const int j0 = blockIdx.y * (2 * TBY) + 2 * threadIdx.y;
+    const int i = blockIdx.z;
+    if (k >= a.g.nz || j0 >= a.g.ny) return;
+    const int j1 = j0 + 1;
+    const bool has1 = j1 < a.g.ny;
+    const int idx0 = (i * a.g.ny + j0) * a.g.nz + k;
+    const int idx1 = idx0 + a.g.nz;
+    const uint8_t fl0 = __ldg(a.flags + idx0);
+    const uint8_t fl1 = has1 ? __ldg(a.flags + idx1) : (uint8_t)CF_SOLID;
+    const bool live0 = !(fl0 & CF_SOLID), live1 = has1 && !(fl1 & CF_SOLID);
+    if (!live0 && (fl0 & (CF_DEFER | CF_WRITE_S))) {
+        float h[19];
+        solid_cell<KIND>(a, idx0, i, j0, k, h);
+        export_f(a, idx0, h);
+    }
+    if (has1 && !live1 && (fl1 & (CF_DEFER | CF_WRITE_S))) {
+        float h[19];
+        solid_cell<KIND>(a, idx1, i, j1, k, h);
+        export_f(a, idx1, h);
+    }
+    float h0[19], h1[19];
+    if (live0) gather_cell<KIND>(a, idx0, i, j0, k, fl0, h0);
+    if (live1) gather_cell<KIND>(a, idx1, i, j1, k, fl1, h1);
+    if (live0) finish_cell<KIND, MODE>(a, idx0, i, j0, k, fl0, h0);
+    if (live1) finish_cell<KIND, MODE>(a, idx1, i, j1, k, fl1, h1);
+}
+
 // Cells that own interpolated-bounce-back links, one thread each, from a
 // compacted ascending cell list: same work as k_fused_step for those cells.
 template <int KIND, int MODE>
@@ -564,6 +606,9 @@ __global__ void __launch_bounds__(128) k_link_cells(const FusedArgs a, const int
 
 inline dim3 cell_grid(const Geo& g) {
     return dim3((unsigned)((g.nz + TBX - 1) / TBX), (unsigned)((g.ny + TBY - 1) / TBY), (unsigned)g.nx);
+}
+inline dim3 cell_grid2(const Geo& g) {
+    return dim3((unsigned)((g.nz + TBX - 1) / TBX), (unsigned)((g.ny + 2 * TBY - 1) / (2 * TBY)), (unsigned)g.nx);
 }
 
 // Rebuild the post-stream FP32 populations (the reference's sim.f) of every
@@ -672,8 +717,9 @@ int dispatch(int storage, int collision, const FusedArgs& a, cudaStream_t st, in
 
 template <int S, int M>
 struct StepLauncher {
-    static int go(const FusedArgs& a, cudaStream_t st, int skip_links, int, int, int) {
+    static int go(const FusedArgs& a, cudaStream_t st, int skip_links, int cells_per_thread, int, int) {
         if (skip_links) k_fused_step<S, M, true><<<cell_grid(a.g), dim3(TBX, TBY), 0, st>>>(a);
+        else if (cells_per_thread == 2) k_fused_step2<S, M><<<cell_grid2(a.g), dim3(TBX, TBY), 0, st>>>(a);
         else k_fused_step<S, M, false><<<cell_grid(a.g), dim3(TBX, TBY), 0, st>>>(a);
         return launch_status();
     }
@@ -926,7 +972,7 @@ int fc_lbm_fused_step(const fc_lbm_step_args* args, void* stream) {
     const int split = args->link_cells != nullptr && args->n_link_cells > 0 && args->separate_link_pass;
     const int phases = args->phase_mask ? args->phase_mask : 3;
     if (phases & 1) {
-        rc = dispatch<StepLauncher>(args->storage, args->collision, a, st, split, 0, 0, 0);
+        rc = dispatch<StepLauncher>(args->storage, args->collision, a, st, split, args->cells_per_thread, 0, 0);
         if (rc) return rc;
     }
     if (!split || !(phases & 2)) return FC_OK;

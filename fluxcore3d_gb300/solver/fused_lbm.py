@@ -198,6 +198,7 @@ class FusedLBM:
         a.has_links = int(self.has_links)
         a.phase_mask = 3
         a.separate_link_pass = int(self.separate_link_pass)
+        a.cells_per_thread = int(getattr(self.sim.cfg, "lbm_cells_per_thread", 1))
         a.link_cells = ptr(self.link_cells)
         a.n_link_cells = 0 if self.link_cells is None else int(self.link_cells.numel())
         a.dev_err = ptr(self.dev_err)

@@ -116,6 +116,7 @@ typedef struct fc_lbm_step_args {
     long long n_link_cells;
     int32_t phase_mask;          /* bit0 main pass, bit1 link-cell pass (0 is read as 3) */
     int32_t separate_link_pass;  /* 1: the main pass skips link cells and a second kernel runs them */
+    int32_t cells_per_thread;    /* 1 or 2 (two rows per thread in the main pass); 0 is read as 1 */
 } fc_lbm_step_args;
 
 /* One full time step for every non-deferred cell. */

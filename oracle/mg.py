@@ -243,3 +243,40 @@ def true_residual(mg: OracleMG, x, b):
     r = (np.asarray(b, np.float64) - mg.mop(lv, np.asarray(x, np.float64))) * m
     mg.dt_ = saved
     return float(np.linalg.norm(r) / (np.linalg.norm(np.asarray(b, np.float64) * m) + 1e-300))
+
+
+def reconstruct(T0, theta, ax, out_idx):
+    """thermal_kernels.cu:61-114: T = T0 + theta with Neumann copies on every face except the inlet."""
+    val = T0 + theta
+    nx, ny, nz = val.shape
+    out = val.copy()
+    for i in range(nx):
+        for j in range(ny):
+            for k in range(nz):
+                s = None
+                if i == nx - 1:
+                    s = (i - 1, j, k)
+                elif i == 0 and (ax != 0 or out_idx == 0):
+                    s = (1, j, k)
+                elif j == ny - 1:
+                    s = (i, j - 1, k)
+                elif j == 0 and (ax != 1 or out_idx == 0):
+                    s = (i, 1, k)
+                elif k == nz - 1:
+                    s = (i, j, k - 1)
+                elif k == 0 and (ax != 2 or out_idx == 0):
+                    s = (i, j, 1)
+                if s is not None:
+                    out[i, j, k] = val[s]
+    return out
+
+
+def thermal_step(mg: OracleMG, T_old, T0, src, mask, dt, tol, max_cycles, ax, out_idx):
+    """One pseudo-time step of thermal_cuda_ext.py:55-201 (fused variant)."""
+    r = mg.dt_
+    m = np.asarray(mask, r)
+    LT0 = mg.L_apply_fine(T0)
+    rhs = m * ((np.asarray(T_old, r) + r(dt) * np.asarray(src, r)) - (np.asarray(T0, r) + r(dt) * LT0))
+    theta0 = m * (np.asarray(T_old, r) - np.asarray(T0, r))
+    theta, info = mg.solve(rhs, theta0, max_cycles=max_cycles, tol=tol)
+    return reconstruct(np.asarray(T0, r), theta * m, ax, out_idx), info

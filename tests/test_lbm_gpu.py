@@ -65,19 +65,20 @@ def test_fused_step_fp32_matches_oracle_small(cuda, collision):
     assert rel_l2(sim.rho.reshape(-1).cpu().numpy(), orc.rho) < 1e-5
 
 
-@pytest.mark.parametrize("storage", ["fp32", "fp16"])
-def test_pin_fin_all_link_modes(cuda, storage):
+@pytest.mark.parametrize("storage,cpt", [("fp32", 1), ("fp16", 1), ("fp32", 2), ("bf16", 2)])
+def test_pin_fin_all_link_modes(cuda, storage, cpt):
     """Small pin-fin heat sink with analytic link fractions: q >= 1/2, q < 1/2 with a second
     fluid node, and q < 1/2 without one all occur; MRT, pressure outlet, sponge."""
     sim = cases.pin_fin(device=cuda, collision="mrt", storage=storage, nx=48, ny=32, nz=40,
                         n_pins=(3, 2), radius=3.5, height=24, base=4, sponge_length=8)
+    sim.cfg.lbm_cells_per_thread = cpt
     d = sim.ibb_data
     ge, fv = d.q_ge_half.bool(), d.ff_valid.bool()
     assert bool(ge.any()) and bool((~ge & fv).any())
     orc = run_pair(sim, 200, real="f32" if storage == "fp32" else "f64")
     N = sim.nx * sim.ny * sim.nz
     e = rel_l2(sim.f.reshape(19, N).cpu().numpy(), orc.f)
-    assert e < (1e-5 if storage == "fp32" else 2e-4), e
+    assert e < {"fp32": 1e-5, "fp16": 2e-4, "bf16": 2e-3}[storage], e
 
 
 def test_fused_step_c1_channel_1000_steps(cuda):

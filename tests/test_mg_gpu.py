@@ -155,3 +155,35 @@ def test_thermal_kernels(cuda):
     flag = THERMAL_CUDA.physics_check(d(T0), 0.0, 0.5)
     assert int(flag) == 1
     assert int(THERMAL_CUDA.physics_check(d(T0), -1.0, 2.0)) == 0
+
+
+def test_thermal_pseudo_time_steps_match_oracle(cuda):
+    """Three fused pseudo-time steps (_temperature_step_mg_fused) on a small heated channel against the
+    oracle's restatement of the same step; fixed cycle count (tol = 0)."""
+    from fluxcore3d_gb300 import case as cases
+    from fluxcore3d_gb300.solver.thermal_cuda_ext import patch_thermal_fused
+    sim = cases.channel_cube(device=cuda, nx=24, ny=16, nz=16, cube=6, cube_x=8, with_links=False)
+    sim.u.fill_(0.02)
+    sim.u[sim.solid_flow] = 0.0
+    src = torch.zeros_like(sim.T)
+    src[sim.solid] = 0.05
+    sim.heat_source = src
+    patch_thermal_fused(sim)
+    ref = omg.OracleMG(sim.k.cpu().numpy(), sim.rho_cp.cpu().numpy(), sim.u.cpu().numpy(), sim.v.cpu().numpy(),
+                       sim.wv.cpu().numpy(), sim._build_update_mask_thermal().cpu().numpy(), 0, 1, 1.0, omega=0.6,
+                       real=np.float32)
+    T = sim.T.cpu().numpy()
+    T0 = sim._build_T_dirichlet_field().cpu().numpy()
+    mask = sim._build_update_mask_thermal().cpu().numpy()
+    for it, dt in enumerate((2.0, 3.0, 4.5)):
+        info = sim._temperature_step_mg(dt, tol=0.0, max_cycles=4)
+        ref.set_dt(dt)
+        T, rinfo = omg.thermal_step(ref, T, T0, src.cpu().numpy(), mask, dt, 0.0, 4, 0, 23)
+        assert info["it"] == rinfo["it"] == 4
+        got = sim.T.cpu().numpy()
+        # theta is carried on top of T0 = 25, so FP32 rounding of T alone is ulp(25) ~ 2e-6: bound the
+        # difference by a few ulps of T plus 1e-5 of the largest temperature rise
+        rise = float(np.abs(T - 25.0).max())
+        assert rise > 1e-2
+        assert float(np.abs(got - T).max()) <= 8 * float(np.spacing(np.float32(32.0))) + 1e-5 * rise, it
+    assert np.isfinite(info["r_rel"])
