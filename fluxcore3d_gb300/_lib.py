@@ -60,6 +60,13 @@ class StepArgs(C.Structure):
         ("phase_mask", C.c_int32),
         ("separate_link_pass", C.c_int32),
         ("cells_per_thread", C.c_int32),
+        ("staging", C.c_int32),
+        ("link_val", C.c_void_p),
+        ("n_link_val", C.c_int64),
+        ("tile_links", C.c_void_p),
+        ("n_tile_links", C.c_int64),
+        ("link_pos", C.c_void_p),
+        ("n_link_pos", C.c_int64),
     ]
 
 
@@ -82,6 +89,7 @@ SIGNATURES: dict[str, tuple] = {
     "fc_lbm_convective_bc_noalloc": (i32, [vp, vp, i32, i32, i32, i32, i32, i32, i32, f32, i32, i32, vp]),
     # lattice, fused
     "fc_lbm_fused_step": (i32, [C.POINTER(StepArgs), vp]),
+    "fc_lbm_tile_links": (C.c_int64, [C.POINTER(StepArgs), vp, C.c_int64, vp, C.c_int64, vp]),
     "fc_lbm_collide_from_f32": (i32, [C.POINTER(StepArgs), i32, i32, vp]),
     "fc_lbm_materialize": (i32, [C.POINTER(StepArgs), vp]),
     "fc_lbm_pin_solid": (i32, [C.POINTER(StepArgs), vp]),

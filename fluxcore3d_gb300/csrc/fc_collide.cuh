@@ -13,6 +13,7 @@
 // integer row coefficients.
 #pragma once
 #include "fc_common.cuh"
+#include "fc_vec.cuh"
 
 namespace fc {
 
@@ -214,170 +215,210 @@ __device__ __forceinline__ Macro collide(float f[19], float feq[19], const Colli
 // for this equilibrium (m_eq = M f_eq evaluated symbolically), so neither f_eq
 // nor M f_eq is formed for MRT.  Returns the macros of the input state.
 // ---------------------------------------------------------------------------
-struct MacroH {
-    float drho, rho, inv_rho, jx, jy, jz, ux, uy, uz;
+template <class V>
+struct MacroV {
+    V drho, rho, inv_rho, jx, jy, jz, ux, uy, uz;
 };
 
 // Shared partial sums of the 19 shifted populations: every conserved and
 // non-conserved moment below is one or two adds away from these.
+template <class V>
 struct PairSums {
-    float Fx, Fy, Fz, dx1, dy1, dz1;        // face pairs: h1+h2, ... and h1-h2, ...
-    float Sxy, Sxz, Syz;                    // edge-plane sums
-    float jxe_xy, jxe_xz, jye_xy, jye_yz, jze_xz, jze_yz;
-    float p13, p14, p15;                    // raw xy, yz, xz second moments
+    V Fx, Fy, Fz, dx1, dy1, dz1;        // face pairs: h1+h2, ... and h1-h2, ...
+    V Sxy, Sxz, Syz;                    // edge-plane sums
+    V jxe_xy, jxe_xz, jye_xy, jye_yz, jze_xz, jze_yz;
+    V p13, p14, p15;                    // raw xy, yz, xz second moments
 };
 
-__device__ __forceinline__ PairSums pair_sums(const float h[19]) {
-    PairSums p;
+template <class V>
+__device__ __forceinline__ PairSums<V> pair_sums(const V h[19]) {
+    PairSums<V> p;
     p.Fx = h[1] + h[2]; p.Fy = h[3] + h[4]; p.Fz = h[5] + h[6];
     p.dx1 = h[1] - h[2]; p.dy1 = h[3] - h[4]; p.dz1 = h[5] - h[6];
-    const float a78 = h[7] + h[8], a910 = h[9] + h[10], d78 = h[7] - h[8], d910 = h[9] - h[10];
-    const float a1112 = h[11] + h[12], a1314 = h[13] + h[14], d1112 = h[11] - h[12], d1314 = h[13] - h[14];
-    const float a1516 = h[15] + h[16], a1718 = h[17] + h[18], d1516 = h[15] - h[16], d1718 = h[17] - h[18];
+    const V a78 = h[7] + h[8], a910 = h[9] + h[10], d78 = h[7] - h[8], d910 = h[9] - h[10];
+    const V a1112 = h[11] + h[12], a1314 = h[13] + h[14], d1112 = h[11] - h[12], d1314 = h[13] - h[14];
+    const V a1516 = h[15] + h[16], a1718 = h[17] + h[18], d1516 = h[15] - h[16], d1718 = h[17] - h[18];
     p.Sxy = a78 + a910; p.jxe_xy = a78 - a910; p.jye_xy = d78 + d910; p.p13 = d78 - d910;
     p.Sxz = a1112 + a1314; p.jxe_xz = a1112 - a1314; p.jze_xz = d1112 + d1314; p.p15 = d1112 - d1314;
     p.Syz = a1516 + a1718; p.jye_yz = a1516 - a1718; p.jze_yz = d1516 + d1718; p.p14 = d1516 - d1718;
     return p;
 }
 
-__device__ __forceinline__ MacroH macros_from(const float h0, const PairSums& p) {
-    MacroH m;
-    m.drho = h0 + ((p.Fx + p.Fy) + p.Fz) + ((p.Sxy + p.Sxz) + p.Syz);
-    m.rho = 1.f + m.drho;
+template <class V>
+__device__ __forceinline__ MacroV<V> macros_from(const V h0, const PairSums<V>& p) {
+    MacroV<V> m;
+    m.drho = h0 + (((p.Fx + p.Fy) + p.Fz) + ((p.Sxy + p.Sxz) + p.Syz));
+    m.rho = m.drho + 1.f;
     m.jx = p.dx1 + (p.jxe_xy + p.jxe_xz);
     m.jy = p.dy1 + (p.jye_xy + p.jye_yz);
     m.jz = p.dz1 + (p.jze_xz + p.jze_yz);
-    m.inv_rho = __frcp_rn(m.rho + 1e-12f);
+    m.inv_rho = rcp(m.rho + 1e-12f);
     m.ux = m.jx * m.inv_rho;
     m.uy = m.jy * m.inv_rho;
     m.uz = m.jz * m.inv_rho;
     return m;
 }
 
-__device__ __forceinline__ MacroH macros_h(const float h[19]) { return macros_from(h[0], pair_sums(h)); }
+template <class V>
+__device__ __forceinline__ MacroV<V> macros_h(const V h[19]) { return macros_from(h[0], pair_sums(h)); }
 
-// h_eq,q = f_eq,q - w_q = w_q (drho + rho (cu + cu^2/2 - 3/2 u.u))
-__device__ __forceinline__ void equilibrium_h(const MacroH& m, float heq[19]) {
-    const float usq = 1.5f * (m.ux * m.ux + m.uy * m.uy + m.uz * m.uz);
-    const float tx = 3.f * m.ux, ty = 3.f * m.uy, tz = 3.f * m.uz;
-#pragma unroll
-    for (int q = 0; q < 19; ++q) {
-        float cu = 0.f;
-        if (cx(q) == 1) cu += tx;
-        if (cx(q) == -1) cu -= tx;
-        if (cy(q) == 1) cu += ty;
-        if (cy(q) == -1) cu -= ty;
-        if (cz(q) == 1) cu += tz;
-        if (cz(q) == -1) cu -= tz;
-        heq[q] = wq(q) * (m.drho + m.rho * (cu + 0.5f * cu * cu - usq));
+// The nine opposite pairs (q, opp(q)) with q the member whose first non-zero
+// velocity component is +1: 1|2 3|4 5|6 7|10 8|9 11|14 12|13 15|18 16|17.
+__host__ __device__ constexpr int pair_first(int p) {
+    return p == 0 ? 1 : p == 1 ? 3 : p == 2 ? 5 : p == 3 ? 7 : p == 4 ? 8 : p == 5 ? 11 : p == 6 ? 12 : p == 7 ? 15 : 16;
+}
+
+// c_q . t for the first member q of a pair (t = 3u)
+template <int Q, class V>
+__device__ __forceinline__ V cu_first(V tx, V ty, V tz) {
+    if (Q == 1) return tx;
+    if (Q == 3) return ty;
+    if (Q == 5) return tz;
+    if (Q == 7) return tx + ty;
+    if (Q == 8) return tx - ty;
+    if (Q == 11) return tx + tz;
+    if (Q == 12) return tx - tz;
+    if (Q == 15) return ty + tz;
+    return ty - tz;   // Q == 16
+}
+
+template <int P, class V>
+struct EqPair {
+    static __device__ __forceinline__ void run(const MacroV<V>& m, V nusq, V tx, V ty, V tz, V heq[19]) {
+        constexpr int q = pair_first(P), o = opp(q);
+        const V cu = cu_first<q>(tx, ty, tz);
+        const V e = fma(0.5f * cu, cu, nusq);
+        heq[q] = wq(q) * fma(m.rho, e + cu, m.drho);
+        heq[o] = wq(q) * fma(m.rho, e - cu, m.drho);
+        EqPair<P + 1, V>::run(m, nusq, tx, ty, tz, heq);
     }
+};
+template <class V>
+struct EqPair<9, V> {
+    static __device__ __forceinline__ void run(const MacroV<V>&, V, V, V, V, V*) {}
+};
+
+// h_eq,q = f_eq,q - w_q = w_q (drho + rho (cu + cu^2/2 - 3/2 u.u)), evaluated per
+// opposite pair from e = cu^2/2 - 3/2 u.u:  h_eq,q = w (drho + rho (e + cu)),
+// h_eq,opp(q) = w (drho + rho (e - cu)).
+template <class V>
+__device__ __forceinline__ void equilibrium_h(const MacroV<V>& m, V heq[19]) {
+    const V nusq = -1.5f * fma(m.ux, m.ux, fma(m.uy, m.uy, m.uz * m.uz));
+    const V tx = 3.f * m.ux, ty = 3.f * m.uy, tz = 3.f * m.uz;
+    heq[0] = wq(0) * fma(m.rho, nusq, m.drho);
+    EqPair<0, V>::run(m, nusq, tx, ty, tz, heq);
 }
 
 // Subtract d_q = sum_k M[k][q] g_k (g_k = S_k n_k / |M_k|^2) from h, with the
 // +-pattern of each edge quartet factored into two pairs of pairs.
-__device__ __forceinline__ void apply_minv(float h[19], float g1, float g2, float g4, float g6, float g8, float g9,
-                                           float g10, float g11, float g12, float g13, float g14, float g15,
-                                           float g16, float g17, float g18) {
-    h[0] -= -30.f * g1 + 12.f * g2;
-    const float face = -11.f * g1 - 4.f * g2;
-    const float fx_ = face + 2.f * g9 - 4.f * g10;
-    h[1] -= fx_ - 4.f * g4;
-    h[2] -= fx_ + 4.f * g4;
-    const float fyz = face - g9 + 2.f * g10;
-    const float fy_ = fyz + g11 - 2.f * g12;
-    const float fz_ = fyz - g11 + 2.f * g12;
-    h[3] -= fy_ - 4.f * g6;
-    h[4] -= fy_ + 4.f * g6;
-    h[5] -= fz_ - 4.f * g8;
-    h[6] -= fz_ + 4.f * g8;
-    const float edge = 8.f * g1 + g2;
+template <class V>
+__device__ __forceinline__ void apply_minv(V h[19], V g1, V g2, V g4, V g6, V g8, V g9, V g10, V g11, V g12,
+                                           V g13, V g14, V g15, V g16, V g17, V g18) {
+    h[0] = h[0] - fma(-30.f, g1, 12.f * g2);
+    const V face = fma(-11.f, g1, -4.f * g2);
+    const V fx_ = fma(2.f, g9, fma(-4.f, g10, face));
+    h[1] = fma(4.f, g4, h[1] - fx_);
+    h[2] = fma(-4.f, g4, h[2] - fx_);
+    const V fyz = fma(2.f, g10, face - g9);
+    const V fy_ = fma(-2.f, g12, fyz + g11);
+    const V fz_ = fma(2.f, g12, fyz - g11);
+    h[3] = fma(4.f, g6, h[3] - fy_);
+    h[4] = fma(-4.f, g6, h[4] - fy_);
+    h[5] = fma(4.f, g8, h[5] - fz_);
+    h[6] = fma(-4.f, g8, h[6] - fz_);
+    const V edge = fma(8.f, g1, g2);
+    const V g910 = g9 + g10, g1112 = g11 + g12;
     {   // xy edges 7..10: exy +- (g4 + g16) +- ((g6 - g17) +- g13)
-        const float exy = edge + g9 + g10 + g11 + g12;
-        const float a = g4 + g16, b = g6 - g17;
-        const float s1 = exy + a, s2 = exy - a, t1 = b + g13, t2 = b - g13;
-        h[7] -= s1 + t1; h[8] -= s1 - t1; h[9] -= s2 + t2; h[10] -= s2 - t2;
+        const V exy = edge + (g910 + g1112);
+        const V a = g4 + g16, b = g6 - g17;
+        const V s1 = exy + a, s2 = exy - a, t1 = b + g13, t2 = b - g13;
+        h[7] = h[7] - (s1 + t1); h[8] = h[8] - (s1 - t1); h[9] = h[9] - (s2 + t2); h[10] = h[10] - (s2 - t2);
     }
     {   // xz edges 11..14: exz +- (g4 - g16) +- ((g8 + g18) +- g15)
-        const float exz = edge + g9 + g10 - g11 - g12;
-        const float a = g4 - g16, b = g8 + g18;
-        const float s1 = exz + a, s2 = exz - a, t1 = b + g15, t2 = b - g15;
-        h[11] -= s1 + t1; h[12] -= s1 - t1; h[13] -= s2 + t2; h[14] -= s2 - t2;
+        const V exz = edge + (g910 - g1112);
+        const V a = g4 - g16, b = g8 + g18;
+        const V s1 = exz + a, s2 = exz - a, t1 = b + g15, t2 = b - g15;
+        h[11] = h[11] - (s1 + t1); h[12] = h[12] - (s1 - t1); h[13] = h[13] - (s2 + t2); h[14] = h[14] - (s2 - t2);
     }
     {   // yz edges 15..18: eyz +- (g6 + g17) +- ((g8 - g18) +- g14)
-        const float eyz = edge - 2.f * g9 - 2.f * g10;
-        const float a = g6 + g17, b = g8 - g18;
-        const float s1 = eyz + a, s2 = eyz - a, t1 = b + g14, t2 = b - g14;
-        h[15] -= s1 + t1; h[16] -= s1 - t1; h[17] -= s2 + t2; h[18] -= s2 - t2;
+        const V eyz = fma(-2.f, g910, edge);
+        const V a = g6 + g17, b = g8 - g18;
+        const V s1 = eyz + a, s2 = eyz - a, t1 = b + g14, t2 = b - g14;
+        h[15] = h[15] - (s1 + t1); h[16] = h[16] - (s1 - t1); h[17] = h[17] - (s2 + t2); h[18] = h[18] - (s2 - t2);
     }
 }
 
-template <int MODE>
-__device__ __forceinline__ MacroH collide_h(float h[19], const CollideParams& p) {
-    const PairSums ps = pair_sums(h);
-    const MacroH m = macros_from(h[0], ps);
+template <int MODE, class V>
+__device__ __forceinline__ MacroV<V> collide_h(V h[19], const CollideParams& p) {
+    const PairSums<V> ps = pair_sums(h);
+    const MacroV<V> m = macros_from(h[0], ps);
     if (MODE == CM_BGK || MODE == CM_TRT) {
-        float heq[19];
+        V heq[19];
         equilibrium_h(m, heq);
         if (MODE == CM_BGK) {
 #pragma unroll
-            for (int q = 0; q < 19; ++q) h[q] = h[q] + p.omega * (heq[q] - h[q]);
+            for (int q = 0; q < 19; ++q) h[q] = fma(p.omega, heq[q] - h[q], h[q]);
         } else {
-            float out[19];
+            // even/odd split per opposite pair: h_q -= w+ (d_q + d_o)/2 + w- (d_q - d_o)/2
+            const float ap = -0.5f * p.omega_plus, am = 0.5f * p.omega_minus;
+            h[0] = fma(-p.omega_plus, h[0] - heq[0], h[0]);
 #pragma unroll
-            for (int q = 0; q < 19; ++q) {
-                const int o = opp(q);
-                const float np_ = 0.5f * ((h[q] - heq[q]) + (h[o] - heq[o]));
-                const float nm_ = 0.5f * ((h[q] - heq[q]) - (h[o] - heq[o]));
-                out[q] = h[q] - p.omega_plus * np_ - p.omega_minus * nm_;
+            for (int pp = 0; pp < 9; ++pp) {
+                const int q = pair_first(pp), o = opp(q);
+                const V dq = h[q] - heq[q], dp = h[o] - heq[o];
+                const V sp = dq + dp, sm = dq - dp;
+                h[q] = fma(ap, sp, fma(-am, sm, h[q]));
+                h[o] = fma(ap, sp, fma(am, sm, h[o]));
             }
-#pragma unroll
-            for (int q = 0; q < 19; ++q) h[q] = out[q];
         }
         return m;
     }
-    const float sf = (ps.Fx + ps.Fy) + ps.Fz;
-    const float se = (ps.Sxy + ps.Sxz) + ps.Syz;
-    const float jxe = ps.jxe_xy + ps.jxe_xz, jye = ps.jye_xy + ps.jye_yz, jze = ps.jze_xz + ps.jze_yz;
+    const V sf = (ps.Fx + ps.Fy) + ps.Fz;
+    const V se = (ps.Sxy + ps.Sxz) + ps.Syz;
+    const V jxe = ps.jxe_xy + ps.jxe_xz, jye = ps.jye_xy + ps.jye_yz, jze = ps.jze_xz + ps.jze_yz;
     // equilibrium parts (rho u u = j u)
-    const float uxx = m.jx * m.ux, uyy = m.jy * m.uy, uzz = m.jz * m.uz;
-    const float rus = uxx + uyy + uzz;
-    const float pxx = 2.f * uxx - uyy - uzz;
-    const float pww = uyy - uzz;
-    const float sxyxz = ps.Sxy + ps.Sxz;
-    const float dxyxz = ps.Sxy - ps.Sxz;
+    const V uxx = m.jx * m.ux, uyy = m.jy * m.uy, uzz = m.jz * m.uz;
+    const V ryz = uyy + uzz;
+    const V rus = uxx + ryz;
+    const V pxx = fma(2.f, uxx, -1.f * ryz);
+    const V pww = uyy - uzz;
+    const V sxyxz = ps.Sxy + ps.Sxz;
+    const V dxyxz = ps.Sxy - ps.Sxz;
     // non-equilibrium moments n_k = (M h)_k - (m_eq,k - (M w)_k)
-    const float n1 = (-30.f * h[0] - 11.f * sf + 8.f * se) + 11.f * m.drho - 19.f * rus;
-    const float n2 = (12.f * h[0] - 4.f * sf + se) - 3.f * m.drho + 5.5f * rus;
-    const float n4 = (-4.f * ps.dx1 + jxe) + (2.f / 3.f) * m.jx;
-    const float n6 = (-4.f * ps.dy1 + jye) + (2.f / 3.f) * m.jy;
-    const float n8 = (-4.f * ps.dz1 + jze) + (2.f / 3.f) * m.jz;
-    const float fyz2 = ps.Fy + ps.Fz;
-    const float n9 = (2.f * ps.Fx - fyz2 + sxyxz - 2.f * ps.Syz) - pxx;
-    const float n10 = (-4.f * ps.Fx + 2.f * fyz2 + sxyxz - 2.f * ps.Syz) + 0.5f * pxx;
-    const float fymz = ps.Fy - ps.Fz;
-    const float n11 = (fymz + dxyxz) - pww;
-    const float n12 = (-2.f * fymz + dxyxz) + 0.5f * pww;
-    const float n13 = ps.p13 - m.jx * m.uy;
-    const float n14 = ps.p14 - m.jy * m.uz;
-    const float n15 = ps.p15 - m.jx * m.uz;
-    const float n16 = ps.jxe_xy - ps.jxe_xz;
-    const float n17 = ps.jye_yz - ps.jye_xy;
-    const float n18 = ps.jze_xz - ps.jze_yz;
-    float s9 = p.SN[9], s11 = p.SN[11], s13 = p.SN[13], s14 = p.SN[14], s15 = p.SN[15];
+    const V n1 = fma(-30.f, h[0], fma(-11.f, sf, fma(8.f, se, fma(11.f, m.drho, -19.f * rus))));
+    const V n2 = fma(12.f, h[0], fma(-4.f, sf, fma(-3.f, m.drho, fma(5.5f, rus, se))));
+    const V n4 = fma(-4.f, ps.dx1, fma(2.f / 3.f, m.jx, jxe));
+    const V n6 = fma(-4.f, ps.dy1, fma(2.f / 3.f, m.jy, jye));
+    const V n8 = fma(-4.f, ps.dz1, fma(2.f / 3.f, m.jz, jze));
+    const V fyz2 = ps.Fy + ps.Fz;
+    const V e9 = fma(-2.f, ps.Syz, sxyxz);
+    const V n9 = fma(2.f, ps.Fx, e9 - fyz2) - pxx;
+    const V n10 = fma(-4.f, ps.Fx, fma(2.f, fyz2, fma(0.5f, pxx, e9)));
+    const V fymz = ps.Fy - ps.Fz;
+    const V n11 = (fymz + dxyxz) - pww;
+    const V n12 = fma(-2.f, fymz, fma(0.5f, pww, dxyxz));
+    const V n13 = fma(-1.f * m.jx, m.uy, ps.p13);
+    const V n14 = fma(-1.f * m.jy, m.uz, ps.p14);
+    const V n15 = fma(-1.f * m.jx, m.uz, ps.p15);
+    const V n16 = ps.jxe_xy - ps.jxe_xz;
+    const V n17 = ps.jye_yz - ps.jye_xy;
+    const V n18 = ps.jze_xz - ps.jze_yz;
+    V s9 = splat<V>(p.SN[9]), s11 = splat<V>(p.SN[11]), s13 = splat<V>(p.SN[13]);
+    V s14 = splat<V>(p.SN[14]), s15 = splat<V>(p.SN[15]);
     if (MODE == CM_MRT_SMAG) {
         // Pi_neq = Pi(h) - rho u u - (drho / 3) I
-        const float third = m.drho * (1.f / 3.f);
-        const float Pxx = (ps.Fx + sxyxz) - uxx - third;
-        const float Pyy = (ps.Fy + ps.Sxy + ps.Syz) - uyy - third;
-        const float Pzz = (ps.Fz + ps.Sxz + ps.Syz) - uzz - third;
-        const float Pxy = n13, Pyz = n14, Pxz = n15;
-        const float piF = sqrtf(Pxx * Pxx + Pyy * Pyy + Pzz * Pzz + 2.f * (Pxy * Pxy + Pxz * Pxz + Pyz * Pyz));
+        const V third = (1.f / 3.f) * m.drho;
+        const V Pxx = ((ps.Fx + sxyxz) - uxx) - third;
+        const V Pyy = ((ps.Fy + (ps.Sxy + ps.Syz)) - uyy) - third;
+        const V Pzz = ((ps.Fz + (ps.Sxz + ps.Syz)) - uzz) - third;
+        const V off = fma(n13, n13, fma(n15, n15, n14 * n14));
+        const V piF = vsqrt(fma(Pxx, Pxx, fma(Pyy, Pyy, fma(Pzz, Pzz, 2.f * off))));
         const float nu0 = (1.f / p.omega0 - 0.5f) * (1.f / 3.f);
-        const float disc = nu0 * nu0 + 4.f * p.Cs_dx2 * (piF * m.inv_rho) * 4.5f;
-        const float nu_eff = 0.5f * (nu0 + sqrtf(fmaxf(disc, nu0 * nu0)));
-        const float om = fminf(1.99f, __frcp_rn(3.f * nu_eff + 0.5f));
-        s9 = om * (1.f / 36.f); s11 = om * (1.f / 12.f);
-        s13 = om * 0.25f; s14 = om * 0.25f; s15 = om * 0.25f;
+        const V disc = fma(18.f * p.Cs_dx2, piF * m.inv_rho, splat<V>(nu0 * nu0));
+        const V nu_eff = 0.5f * (vsqrt(vmax(disc, splat<V>(nu0 * nu0))) + nu0);
+        const V om = vmin(rcp(fma(3.f, nu_eff, splat<V>(0.5f))), 1.99f);
+        s9 = (1.f / 36.f) * om; s11 = (1.f / 12.f) * om;
+        s13 = 0.25f * om; s14 = s13; s15 = s13;
     }
     apply_minv(h, p.SN[1] * n1, p.SN[2] * n2, p.SN[4] * n4, p.SN[6] * n6, p.SN[8] * n8, s9 * n9,
                p.SN[10] * n10, s11 * n11, p.SN[12] * n12, s13 * n13, s14 * n14, s15 * n15,

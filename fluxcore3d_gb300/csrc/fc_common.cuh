@@ -55,6 +55,7 @@ enum Status : int {
 enum DevErr : unsigned {
     DEV_ERR_INDEX = 1u,      // an index read from a table was out of range
     DEV_ERR_NONFINITE = 2u,  // a non-finite value was produced
+    DEV_ERR_TIMEOUT = 4u,    // a bounded wait on an mbarrier gave up (staged copies never landed)
 };
 
 // ---- cell flag byte used by the fused step --------------------------------

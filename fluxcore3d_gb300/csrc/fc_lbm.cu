@@ -21,6 +21,7 @@
 //    which plane_collide finishes them.
 #include "fc_common.cuh"
 #include "fc_collide.cuh"
+#include "fc_fused.cuh"
 #include "../../include/fluxcore3d_gb300.h"
 
 #include <mutex>
@@ -30,11 +31,6 @@ using namespace fc;
 namespace {
 
 constexpr int BLOCK = 256;
-
-__constant__ int c_CX[19] = {0, 1, -1, 0, 0, 0, 0, 1, 1, -1, -1, 1, 1, -1, -1, 0, 0, 0, 0};
-__constant__ int c_CY[19] = {0, 0, 0, 1, -1, 0, 0, 1, -1, 1, -1, 0, 0, 0, 0, 1, 1, -1, -1};
-__constant__ int c_CZ[19] = {0, 0, 0, 0, 0, 1, -1, 0, 0, 0, 0, 1, -1, 1, -1, 1, -1, 1, -1};
-__constant__ int c_OPP[19] = {0, 2, 1, 4, 3, 6, 5, 10, 9, 8, 7, 14, 13, 12, 11, 18, 17, 16, 15};
 
 inline unsigned grid_for(long long n) { return (unsigned)((n + BLOCK - 1) / BLOCK); }
 
@@ -317,202 +313,7 @@ __global__ void __launch_bounds__(BLOCK) k_convective_pass2(
 //  Family 2: fused step
 // ============================================================================
 
-struct Geo {
-    int nx, ny, nz;
-    int px, py, pz;
-    long long N;   // population stride (cells); cell indices themselves fit in 32 bits
-    int nynz;
-};
-
-// Threads map to cells as (k, j, i) = (x, y, z) launch coordinates: a warp
-// covers 32 consecutive k of one row, so every population access of a warp is
-// one contiguous (possibly one-element shifted) run, and i, j are warp-uniform.
-constexpr int TBX = 32, TBY = 4;
-
-__device__ __forceinline__ bool cell_of_thread(const Geo& g, int& i, int& j, int& k, int& idx) {
-    k = blockIdx.x * TBX + threadIdx.x;
-    j = blockIdx.y * TBY + threadIdx.y;
-    i = blockIdx.z;
-    if (k >= g.nz || j >= g.ny) return false;
-    idx = (i * g.ny + j) * g.nz + k;
-    return true;
-}
-
-// Source cell x - c_q of every population: periodic axes wrap, a non-periodic
-// axis that leaves the box makes the cell its own source (stream_pull rule).
-__device__ __forceinline__ void pull_sources(const Geo& g, int i, int j, int k, int idx, int src[19]) {
-    const bool inner = (i > 0) & (i < g.nx - 1) & (j > 0) & (j < g.ny - 1);  // warp-uniform
-    if (inner) {
-        const bool zm_ok = (k > 0) | (g.pz != 0);
-        const bool zp_ok = (k < g.nz - 1) | (g.pz != 0);
-        const int dzm = k > 0 ? -1 : g.nz - 1;          // source k-1 (c_z = +1)
-        const int dzp = k < g.nz - 1 ? 1 : -(g.nz - 1); // source k+1 (c_z = -1)
-#pragma unroll
-        for (int q = 0; q < 19; ++q) {
-            const int base = idx - cx(q) * g.nynz - cy(q) * g.nz;
-            if (cz(q) == 0) src[q] = base;
-            else if (cz(q) == 1) src[q] = zm_ok ? base + dzm : idx;
-            else src[q] = zp_ok ? base + dzp : idx;
-        }
-        return;
-    }
-    const int im = i > 0 ? i - 1 : (g.px ? g.nx - 1 : -1);
-    const int ip = i < g.nx - 1 ? i + 1 : (g.px ? 0 : -1);
-    const int jm = j > 0 ? j - 1 : (g.py ? g.ny - 1 : -1);
-    const int jp = j < g.ny - 1 ? j + 1 : (g.py ? 0 : -1);
-    const int km = k > 0 ? k - 1 : (g.pz ? g.nz - 1 : -1);
-    const int kp = k < g.nz - 1 ? k + 1 : (g.pz ? 0 : -1);
-#pragma unroll
-    for (int q = 0; q < 19; ++q) {
-        const int si = cx(q) == 1 ? im : (cx(q) == -1 ? ip : i);
-        const int sj = cy(q) == 1 ? jm : (cy(q) == -1 ? jp : j);
-        const int sk = cz(q) == 1 ? km : (cz(q) == -1 ? kp : k);
-        src[q] = ((si | sj | sk) < 0) ? idx : (si * g.ny + sj) * g.nz + sk;
-    }
-}
-
-struct FusedArgs {
-    Geo g;
-    const void* pin[19];   // population planes of the previous post-collision buffer
-    void* pout[19];        // population planes of this step's buffer
-    float* f32;
-    float* rho;
-    float* u;
-    float* v;
-    float* w;
-    const uint8_t* flags;
-    const int* link_off;      // per cell: link-cell ordinal (read where the link flag is set)
-    const uint4* link_hdr;    // per link cell: (dir mask, second-node mask, weight offset, 0)
-    const float2* link_w;
-    long long n_links;
-    const int* link_cells;    // optional list for the separate link pass
-    long long n_link_cells;
-    const float* sponge;
-    int sponge_axis;
-    int has_links;
-    CollideParams cp;
-    unsigned* dev_err;
-};
-
-// shifted value h = f - w_q of population q at `cell` of the input buffer
-template <int KIND>
-__device__ __forceinline__ float in_h(const FusedArgs& a, int q, int cell) {
-    using T = typename Store<KIND>::T;
-    const T* p = reinterpret_cast<const T*>(a.pin[q]) + cell;
-    if (KIND == ST_F32) return __ldg(reinterpret_cast<const float*>(p)) - wq(q);
-    if (KIND == ST_F16S) return __half2float(__ldg(reinterpret_cast<const __half*>(p)));
-    return __bfloat162float(__ldg(reinterpret_cast<const __nv_bfloat16*>(p)));
-}
-template <int KIND>
-__device__ __forceinline__ void out_h(const FusedArgs& a, int q, int cell, float h) {
-    using T = typename Store<KIND>::T;
-    T* p = reinterpret_cast<T*>(a.pout[q]) + cell;
-    if (KIND == ST_F32) *reinterpret_cast<float*>(p) = h + wq(q);
-    else if (KIND == ST_F16S) *reinterpret_cast<__half*>(p) = __float2half_rn(h);
-    else *reinterpret_cast<__nv_bfloat16*>(p) = __float2bfloat16_rn(h);
-}
-// Interpolated bounce-back of one link cell (reference lbm_kernels.cu:542-588),
-// evaluated in the pull pass from the previous post-collision buffer.  The cell's
-// header (uint4) holds: x = mask of link directions (bit d), y = mask of links
-// whose second term is the opposite population at x_f - c_d (q < 1/2 with a
-// fluid second node) instead of population d at x_f, z = offset of the cell's
-// (w1, w2) pairs, one per set bit of x in ascending d.  q < 1/2 links without a
-// second node are stored as (w1, w2) = (1, 0).  Directions are unrolled so
-// every population index is a compile-time constant.
-template <int KIND, int D>
-struct LinkDir {
-    static __device__ __forceinline__ void run(const FusedArgs& a, int idx, uint4 hd, float h[19]) {
-        if (hd.x & (1u << D)) {
-            using T = typename Store<KIND>::T;
-            constexpr int O = opp(D);
-            const float2 wt = __ldg(a.link_w + hd.z + __popc(hd.x & ((1u << D) - 1u)));
-            const float fo = in_h<KIND>(a, O, idx) + wq(O);
-            const bool second_ff = (hd.y >> D) & 1u;
-            const T* p2 = second_ff
-                ? reinterpret_cast<const T*>(a.pin[O]) + (idx - (cx(D) * a.g.nynz + cy(D) * a.g.nz + cz(D)))
-                : reinterpret_cast<const T*>(a.pin[D]) + idx;
-            float f2;
-            if (KIND == ST_F32) f2 = __ldg(reinterpret_cast<const float*>(p2));
-            else if (KIND == ST_F16S) f2 = __half2float(__ldg(reinterpret_cast<const __half*>(p2))) + (second_ff ? wq(O) : wq(D));
-            else f2 = __bfloat162float(__ldg(reinterpret_cast<const __nv_bfloat16*>(p2))) + (second_ff ? wq(O) : wq(D));
-            h[D] = (wt.x * fo + wt.y * f2) - wq(D);
-        }
-        LinkDir<KIND, D + 1>::run(a, idx, hd, h);
-    }
-};
-template <int KIND>
-struct LinkDir<KIND, 19> {
-    static __device__ __forceinline__ void run(const FusedArgs&, int, uint4, float*) {}
-};
-
-// Post-stream populations (shifted) of one cell: pull + interpolated bounce-back
-// on the cell's own links.
-template <int KIND>
-__device__ __forceinline__ void gather_cell(const FusedArgs& a, int idx, int i, int j, int k, uint8_t fl,
-                                            float h[19]) {
-    int lc = -1;
-    if (fl & CF_LINK) lc = __ldg(a.link_off + idx);
-    int src[19];
-    pull_sources(a.g, i, j, k, idx, src);
-#pragma unroll
-    for (int q = 0; q < 19; ++q) h[q] = in_h<KIND>(a, q, src[q]);
-    if (fl & CF_LINK) {
-        if (lc < 0 || (long long)lc >= a.n_link_cells) {
-            if (a.dev_err) atomicOr(a.dev_err, DEV_ERR_INDEX);
-            return;
-        }
-        const uint4 hd = __ldg(a.link_hdr + lc);
-        if ((long long)hd.z + __popc(hd.x) > a.n_links) {
-            if (a.dev_err) atomicOr(a.dev_err, DEV_ERR_INDEX);
-            return;
-        }
-        LinkDir<KIND, 1>::run(a, idx, hd, h);
-    }
-}
-
-// Post-stream populations (shifted) of a flow-solid cell as the reference leaves
-// them: w_q after reset_solid when links exist, else the in-cell direction swap
-// of the pulled values (LBM_CHT.py _bounce_back_post_stream).
-template <int KIND>
-__device__ __forceinline__ void solid_cell(const FusedArgs& a, int idx, int i, int j, int k, float h[19]) {
-    if (a.has_links) {
-#pragma unroll
-        for (int q = 0; q < 19; ++q) h[q] = 0.f;
-    } else {
-        int src[19];
-        pull_sources(a.g, i, j, k, idx, src);
-        float t[19];
-#pragma unroll
-        for (int q = 0; q < 19; ++q) t[q] = in_h<KIND>(a, q, src[q]);
-#pragma unroll
-        for (int q = 0; q < 19; ++q) h[q] = t[opp(q)];
-    }
-}
-
-__device__ __forceinline__ void export_f(const FusedArgs& a, int idx, const float h[19]) {
-#pragma unroll
-    for (int q = 0; q < 19; ++q) a.f32[q * a.g.N + idx] = h[q] + wq(q);
-}
-
-template <int KIND, int MODE>
-__device__ __forceinline__ void collide_store(const FusedArgs& a, int idx, int i, int j, int k, float h[19]) {
-    const MacroH m = collide_h<MODE>(h, a.cp);
-    if (a.sponge) {
-        const int c = a.sponge_axis == 0 ? i : (a.sponge_axis == 1 ? j : k);
-        const float sg = __ldg(a.sponge + c);
-        if (sg > 0.f) {
-            float heq[19];
-            equilibrium_h(m, heq);
-#pragma unroll
-            for (int q = 0; q < 19; ++q) h[q] = h[q] - sg * (h[q] - heq[q]);
-        }
-    }
-#pragma unroll
-    for (int q = 0; q < 19; ++q) out_h<KIND>(a, q, idx, h[q]);
-    if (a.rho) {
-        a.rho[idx] = m.rho; a.u[idx] = m.ux; a.v[idx] = m.uy; a.w[idx] = m.uz;
-    }
-}
+// Shared device code of the fused pass: fc_fused.cuh.
 
 template <int KIND, int MODE, bool SKIP_LINKS>
 __global__ void __launch_bounds__(TBX * TBY, 7) k_fused_step(const FusedArgs a) {
@@ -604,6 +405,21 @@ __global__ void __launch_bounds__(128) k_link_cells(const FusedArgs a, const int
     collide_store<KIND, MODE>(a, idx, i, j, k, h);
 }
 
+// Per-step gather of every link's interpolated bounce-back value into link_val,
+// one thread per link cell of the ascending link-cell list.
+template <int KIND>
+__global__ void __launch_bounds__(128) k_link_gather(const FusedArgs a) {
+    const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= a.n_link_cells) return;
+    const int idx = __ldg(a.link_cells + t);
+    const uint4 hd = __ldg(a.link_hdr + t);
+    if (idx < 0 || (long long)idx >= a.g.N || (long long)hd.z + __popc(hd.x) > a.n_links) {
+        if (a.dev_err) atomicOr(a.dev_err, DEV_ERR_INDEX);
+        return;
+    }
+    LinkGather<KIND, 1>::run(a, idx, hd);
+}
+
 inline dim3 cell_grid(const Geo& g) {
     return dim3((unsigned)((g.nz + TBX - 1) / TBX), (unsigned)((g.ny + TBY - 1) / TBY), (unsigned)g.nx);
 }
@@ -689,6 +505,18 @@ int make_fused_args(const fc_lbm_step_args* s, FusedArgs& a) {
     a.link_cells = s->link_cells;
     a.n_link_cells = s->n_link_cells;
     if (a.link_hdr && (reinterpret_cast<uintptr_t>(a.link_hdr) & 15)) return FC_ERR_ARG;
+    a.link_val = s->link_val;
+    a.n_link_val = s->n_link_val;
+    if (a.link_val && (a.n_link_val < a.n_links + 8 || !a.link_cells || a.n_link_cells <= 0))
+        a.link_val = nullptr;   // the gather needs the link-cell list and a padded buffer
+    if (a.link_val && (reinterpret_cast<uintptr_t>(a.link_val) & 15)) return FC_ERR_ARG;
+    a.tile_links = reinterpret_cast<const int4*>(s->tile_links);
+    a.n_tile_links = s->n_tile_links;
+    if (a.tile_links && (reinterpret_cast<uintptr_t>(a.tile_links) & 15)) return FC_ERR_ARG;
+    a.link_pos = s->link_pos;
+    a.n_link_pos = s->n_link_pos;
+    if (a.link_pos && (a.n_link_pos < a.n_links + 8 || (reinterpret_cast<uintptr_t>(a.link_pos) & 15)))
+        a.link_pos = nullptr;
     a.sponge = s->sponge; a.sponge_axis = s->sponge_axis;
     if (a.sponge && (a.sponge_axis < 0 || a.sponge_axis > 2)) return FC_ERR_ARG;
     a.has_links = s->has_links;
@@ -972,11 +800,33 @@ int fc_lbm_fused_step(const fc_lbm_step_args* args, void* stream) {
     const int split = args->link_cells != nullptr && args->n_link_cells > 0 && args->separate_link_pass;
     const int phases = args->phase_mask ? args->phase_mask : 3;
     if (phases & 1) {
-        rc = dispatch<StepLauncher>(args->storage, args->collision, a, st, split, args->cells_per_thread, 0, 0);
+        if (a.link_val && a.n_links > 0) {
+            const unsigned nb = (unsigned)((a.n_link_cells + 127) / 128);
+            switch (args->storage) {
+                case ST_F32: k_link_gather<ST_F32><<<nb, 128, 0, st>>>(a); break;
+                case ST_F16S: k_link_gather<ST_F16S><<<nb, 128, 0, st>>>(a); break;
+                default: k_link_gather<ST_BF16S><<<nb, 128, 0, st>>>(a); break;
+            }
+            rc = launch_status();
+            if (rc) return rc;
+        }
+        rc = FC_ERR_UNSUPPORTED;
+        if (!split && args->staging == 0 && args->cells_per_thread <= 1 && fused_tma_eligible(a, args->storage))
+            rc = launch_fused_tma(a, args->storage, args->collision, st);
+        if (rc == FC_ERR_UNSUPPORTED)
+            rc = dispatch<StepLauncher>(args->storage, args->collision, a, st, split, args->cells_per_thread, 0, 0);
         if (rc) return rc;
     }
     if (!split || !(phases & 2)) return FC_OK;
     return dispatch<LinkCellLauncher>(args->storage, args->collision, a, st, 0, 0, 0, 0);
+}
+
+long long fc_lbm_tile_links(const fc_lbm_step_args* args, int32_t* records, long long cap, uint16_t* link_pos,
+                            long long pos_cap, void* stream) {
+    FusedArgs a;
+    const int rc = make_fused_args(args, a);
+    if (rc) return -rc;
+    return tma_tile_links(a, reinterpret_cast<int4*>(records), cap, link_pos, pos_cap, (cudaStream_t)stream);
 }
 
 int fc_lbm_collide_from_f32(const fc_lbm_step_args* args, int axis, int plane_idx, void* stream) {
@@ -998,6 +848,7 @@ int fc_lbm_materialize(const fc_lbm_step_args* args, void* stream) {
     FusedArgs a;
     int rc = make_fused_args(args, a);
     if (rc) return rc;
+    a.link_val = nullptr;   // links evaluated from pop_in itself, independent of the last gather
     if (!a.f32 || !args->pop_in) return FC_ERR_ARG;
     cudaStream_t st = (cudaStream_t)stream;
     switch (args->storage) {

@@ -24,6 +24,8 @@ Observable behaviour compared with the reference step (solver/lbm_cuda_ext.py:44
 """
 from __future__ import annotations
 
+import ctypes as C
+
 import torch
 
 from .. import _lib
@@ -199,9 +201,37 @@ class FusedLBM:
         a.phase_mask = 3
         a.separate_link_pass = int(self.separate_link_pass)
         a.cells_per_thread = int(getattr(self.sim.cfg, "lbm_cells_per_thread", 1))
+        a.staging = {"tma": 0, "direct": 1}[str(getattr(self.sim.cfg, "lbm_staging", "tma"))]
         a.link_cells = ptr(self.link_cells)
         a.n_link_cells = 0 if self.link_cells is None else int(self.link_cells.numel())
         a.dev_err = ptr(self.dev_err)
+        # per-step gathered link values (storage form), the staged pass's tile records
+        # and the staged-tile element each link value replaces
+        self.link_val = None
+        self.tile_links = None
+        self.link_pos = None
+        if self.has_links and self.n_links > 0:
+            self.link_val = torch.zeros(self.n_links + 8, dtype=STORAGE_DTYPE[self.storage], device=sim.device)
+            a.link_val = ptr(self.link_val)
+            a.n_link_val = self.link_val.numel()
+        nt = 0
+        if sim.device.type == "cuda":
+            nt = int(_lib.lib().fc_lbm_tile_links(C.byref(a), None, 0, None, 0, stream_ptr()))
+        if nt > 0:
+            self.tile_links = torch.zeros((nt, 8), dtype=torch.int32, device=sim.device)
+            pos_ptr, pos_cap = None, 0
+            if self.n_links > 0:
+                self.link_pos = torch.zeros(self.n_links + 8, dtype=torch.int16, device=sim.device)
+                pos_ptr, pos_cap = ptr(self.link_pos), self.link_pos.numel()
+            got = int(_lib.lib().fc_lbm_tile_links(C.byref(a), ptr(self.tile_links), nt, pos_ptr, pos_cap,
+                                                   stream_ptr()))
+            if got != nt:
+                raise RuntimeError(f"fc_lbm_tile_links failed: {got}")
+            a.tile_links = ptr(self.tile_links)
+            a.n_tile_links = nt
+            if self.link_pos is not None:
+                a.link_pos = ptr(self.link_pos)
+                a.n_link_pos = pos_cap
         self.refresh_params()
 
     def refresh_params(self):

@@ -117,10 +117,38 @@ typedef struct fc_lbm_step_args {
     int32_t phase_mask;          /* bit0 main pass, bit1 link-cell pass (0 is read as 3) */
     int32_t separate_link_pass;  /* 1: the main pass skips link cells and a second kernel runs them */
     int32_t cells_per_thread;    /* 1 or 2 (two rows per thread in the main pass); 0 is read as 1 */
+    int32_t staging;             /* 0: main pass stages tiles of rows in shared memory with TMA when the
+                                    grid allows it (nz a multiple of 16 and at most 256, no separate link
+                                    pass, one cell per thread), 1: per-thread global loads always */
+    void* link_val;              /* optional scratch of n_links + 8 elements of the population storage type:
+                                    when set, each step first gathers every link's interpolated bounce-back
+                                    value into it in storage form (one thread per link cell, needs
+                                    link_cells) and both passes read those values */
+    int64_t n_link_val;          /* capacity of link_val in elements */
+    const int32_t* tile_links;   /* optional, from fc_lbm_tile_links: one 8 x int32 record per staged tile
+                                    (link-cell range, link range, per-chunk link offsets); with link_pos it
+                                    lets the staged pass place link values straight into its tiles */
+    int64_t n_tile_links;        /* number of records in tile_links */
+    const uint16_t* link_pos;    /* optional, from fc_lbm_tile_links: per link, the element of the staged
+                                    tile that its value replaces (0xffff: none); n_links + 8 entries */
+    int64_t n_link_pos;          /* capacity of link_pos in entries */
 } fc_lbm_step_args;
 
 /* One full time step for every non-deferred cell. */
 int fc_lbm_fused_step(const fc_lbm_step_args* args, void* stream);
+
+/* Tiles of the TMA-staged main pass for this grid.  With records == NULL
+ * returns the number of tiles (0 when the staged pass does not apply to the
+ * grid).  Otherwise fills records[8 t .. 8 t + 7] for every tile t -- (first
+ * link cell, end link cell, first link, end link) from link_cells / link_hdr,
+ * then eight 16-bit offsets, from the tile's first link, of the first link of
+ * each of its 64-cell chunks -- and, when link_pos is given (pos_cap >=
+ * n_links + 8), the staged-tile element each link's value replaces; returns
+ * the tile count (cap = records that fit), or a negative status.  Both depend
+ * only on the geometry: compute them once after the link tables are built.
+ * No reference counterpart (the reference has no staged pass). */
+long long fc_lbm_tile_links(const fc_lbm_step_args* args, int32_t* records, long long cap, uint16_t* link_pos,
+                            long long pos_cap, void* stream);
 /* Collide cells straight from args->f32: axis < 0 => every fluid cell (start-up),
  * else the plane plane_idx along axis (after that plane's boundary condition). */
 int fc_lbm_collide_from_f32(const fc_lbm_step_args* args, int axis, int plane_idx, void* stream);

@@ -65,13 +65,17 @@ def test_fused_step_fp32_matches_oracle_small(cuda, collision):
     assert rel_l2(sim.rho.reshape(-1).cpu().numpy(), orc.rho) < 1e-5
 
 
-@pytest.mark.parametrize("storage,cpt", [("fp32", 1), ("fp16", 1), ("fp32", 2), ("bf16", 2)])
-def test_pin_fin_all_link_modes(cuda, storage, cpt):
+@pytest.mark.parametrize("storage,cpt,staging", [("fp32", 1, "tma"), ("fp16", 1, "tma"), ("bf16", 1, "tma"),
+                                                 ("fp16", 1, "direct"), ("fp32", 2, "direct"),
+                                                 ("bf16", 2, "direct")])
+def test_pin_fin_all_link_modes(cuda, storage, cpt, staging):
     """Small pin-fin heat sink with analytic link fractions: q >= 1/2, q < 1/2 with a second
-    fluid node, and q < 1/2 without one all occur; MRT, pressure outlet, sponge."""
-    sim = cases.pin_fin(device=cuda, collision="mrt", storage=storage, nx=48, ny=32, nz=40,
+    fluid node, and q < 1/2 without one all occur; MRT, pressure outlet, sponge.  nz = 48 is
+    a partial 32-cell chunk per row for the TMA-staged pass."""
+    sim = cases.pin_fin(device=cuda, collision="mrt", storage=storage, nx=48, ny=32, nz=48,
                         n_pins=(3, 2), radius=3.5, height=24, base=4, sponge_length=8)
     sim.cfg.lbm_cells_per_thread = cpt
+    sim.cfg.lbm_staging = staging
     d = sim.ibb_data
     ge, fv = d.q_ge_half.bool(), d.ff_valid.bool()
     assert bool(ge.any()) and bool((~ge & fv).any())
@@ -79,6 +83,52 @@ def test_pin_fin_all_link_modes(cuda, storage, cpt):
     N = sim.nx * sim.ny * sim.nz
     e = rel_l2(sim.f.reshape(19, N).cpu().numpy(), orc.f)
     assert e < {"fp32": 1e-5, "fp16": 2e-4, "bf16": 2e-3}[storage], e
+
+
+def periodic_box(cuda, collision, storage, nx=40, ny=20, nz=32):
+    """Cube with IBB links in a box periodic along y and z (no walls): fluid cells sit on every
+    k and j boundary, so the staged pass wraps rows inside its tiles and the edge rows take
+    the direct path; ny = 20 leaves a partial last tile."""
+    from fluxcore3d_gb300 import geometry as geo
+    from fluxcore3d_gb300.case import CaseConfig, LatticeCase, stamp_walls
+    cfg = CaseConfig(nx=nx, ny=ny, nz=nz, collision=collision, lbm_storage=storage, domain_walls=[],
+                     outlet_bc_mode="pressure", sponge_length=6)
+    solid = geo.cube_mask((nx, ny, nz), (14, ny // 2, nz // 2), (6, 6, 6), device=cuda)
+    phi = torch.tensor(geo.phi_from_voxels(solid.cpu().numpy()), dtype=torch.float32, device=cuda)
+    ibb = geo.ibb_from_phi_trilinear(solid, phi)
+    return LatticeCase(cfg, 0.05, 0.05 * 6 / 50, solid, stamp_walls(cfg, solid), ibb, device=cuda, seed=0)
+
+
+@pytest.mark.parametrize("collision", ["trt", "mrt"])
+def test_staged_pass_periodic_box_matches_oracle(cuda, collision):
+    sim = periodic_box(cuda, collision, "fp32")
+    sim.cfg.lbm_staging = "tma"
+    orc = run_pair(sim, 150)
+    N = sim.nx * sim.ny * sim.nz
+    assert rel_l2(sim.f.reshape(19, N).cpu().numpy(), orc.f) < 1e-5
+
+
+@pytest.mark.parametrize("storage,collision", [("fp16", "mrt"), ("fp32", "trt"), ("bf16", "mrt_smag"),
+                                               ("fp16", "bgk")])
+def test_staged_pass_bit_identical_to_direct(cuda, storage, collision):
+    """The TMA-staged and the direct main pass run the same per-cell arithmetic on the same
+    values, so their populations and macros agree bit for bit."""
+    out = {}
+    for staging in ("tma", "direct"):
+        sim = periodic_box(cuda, collision, storage)
+        sim.cfg.lbm_staging = staging
+        LBMCUDAUpgrade.patch(sim)
+        for _ in range(60):
+            sim.step(do_thermal=False)
+        torch.cuda.synchronize()
+        assert sim._fc.check_device_error() == 0
+        P = sim._fc.P[sim._fc.cur]
+        out[staging] = (P.view(torch.uint8).cpu().numpy(), P.float().cpu().numpy(), sim.rho.cpu().numpy(),
+                        sim.u.cpu().numpy())
+    assert np.array_equal(out["tma"][0], out["direct"][0]), \
+        float(np.abs(out["tma"][1].astype(np.float64) - out["direct"][1]).max())
+    for a, b in zip(out["tma"][2:], out["direct"][2:]):
+        assert np.array_equal(a, b), float(np.abs(a.astype(np.float64) - b.astype(np.float64)).max())
 
 
 def test_fused_step_c1_channel_1000_steps(cuda):
