@@ -23,6 +23,13 @@ f32 = C.c_float
 f64 = C.c_double
 
 
+class PlaneBC(C.Structure):
+    """Mirror of fc_plane_bc."""
+    _fields_ = [("axis", C.c_int32), ("plane_idx", C.c_int32), ("interior_idx", C.c_int32),
+                ("bc_type", C.c_int32), ("u_in_lat", C.c_float), ("rho_out_lat", C.c_float),
+                ("sign", C.c_int32), ("pad", C.c_int32)]
+
+
 class StepArgs(C.Structure):
     """Mirror of fc_lbm_step_args (include/fluxcore3d_gb300.h)."""
 
@@ -67,6 +74,9 @@ class StepArgs(C.Structure):
         ("n_tile_links", C.c_int64),
         ("link_pos", C.c_void_p),
         ("n_link_pos", C.c_int64),
+        ("link_src", C.c_void_p),
+        ("n_link_src", C.c_int64),
+        ("skip_link_gather", C.c_int32),
     ]
 
 
@@ -89,7 +99,9 @@ SIGNATURES: dict[str, tuple] = {
     "fc_lbm_convective_bc_noalloc": (i32, [vp, vp, i32, i32, i32, i32, i32, i32, i32, f32, i32, i32, vp]),
     # lattice, fused
     "fc_lbm_fused_step": (i32, [C.POINTER(StepArgs), vp]),
-    "fc_lbm_tile_links": (C.c_int64, [C.POINTER(StepArgs), vp, C.c_int64, vp, C.c_int64, vp]),
+    "fc_lbm_link_gather": (i32, [C.POINTER(StepArgs), vp, C.c_int64, i32, vp]),
+    "fc_lbm_planes_zou_he_collide": (i32, [C.POINTER(StepArgs), C.POINTER(PlaneBC), i32, vp]),
+    "fc_lbm_tile_links": (C.c_int64, [C.POINTER(StepArgs), vp, C.c_int64, vp, C.c_int64, vp, C.c_int64, vp]),
     "fc_lbm_collide_from_f32": (i32, [C.POINTER(StepArgs), i32, i32, vp]),
     "fc_lbm_materialize": (i32, [C.POINTER(StepArgs), vp]),
     "fc_lbm_pin_solid": (i32, [C.POINTER(StepArgs), vp]),

@@ -82,6 +82,8 @@ struct FusedArgs {
     long long n_tile_links;
     const uint16_t* link_pos; // per link: element of the staged tile its value replaces (0xffff: none)
     long long n_link_pos;
+    const uint2* link_src;    // per link: population elements it blends (bit 31 of .x: edge direction)
+    long long n_link_src;
     const float* sponge;
     int sponge_axis;
     int has_links;
@@ -280,6 +282,6 @@ bool fused_tma_eligible(const FusedArgs& a, int storage);
 // fills the per-tile records (cap at most) and, with pos != null, the per-link
 // staged-tile elements.  Negative on error.
 long long tma_tile_links(const FusedArgs& a, int4* out, long long cap, uint16_t* pos, long long pos_cap,
-                         cudaStream_t st);
+                         uint2* src, long long src_cap, cudaStream_t st);
 
 }  // namespace fc

@@ -155,8 +155,10 @@ __device__ __forceinline__ long long plane_flat(int axis, int p, int a, int b, i
 // Second-order Hermite tensors Q = c c - I/3 use the reference's 8-digit literals.
 __device__ __forceinline__ float q_diag(int c) { return c != 0 ? 0.66666667f : -0.33333333f; }
 
+// Writes the node's new populations to f and, when out is given, to out too.
 __device__ void zou_he_node(float* __restrict__ f, long long N, long long flat_bc, long long flat_in,
-                            int axis, int plane_idx, int bc_type, float u_in, float rho_out, int sign) {
+                            int axis, int plane_idx, int bc_type, float u_in, float rho_out, int sign,
+                            float* out = nullptr) {
     float fi[19];
 #pragma unroll
     for (int q = 0; q < 19; ++q) fi[q] = f[q * N + flat_bc];
@@ -180,7 +182,11 @@ __device__ void zou_he_node(float* __restrict__ f, long long N, long long flat_b
         uax = (float)known * ((s0 + 2.f * sk) / (rho_bc + 1e-12f) - 1.f);
         if (uax * (float)sign < 0.f) {
 #pragma unroll
-            for (int q = 0; q < 19; ++q) f[q * N + flat_bc] = f[q * N + flat_in];
+            for (int q = 0; q < 19; ++q) {
+                const float v = f[q * N + flat_in];
+                f[q * N + flat_bc] = v;
+                if (out) out[q] = v;
+            }
             return;
         }
         float fin[19];
@@ -215,7 +221,9 @@ __device__ void zou_he_node(float* __restrict__ f, long long N, long long flat_b
         const float sq = q_diag(cx(q)) * Pxx + q_diag(cy(q)) * Pyy + q_diag(cz(q)) * Pzz +
                          2.f * ((float)(cx(q) * cy(q)) * Pxy + (float)(cx(q) * cz(q)) * Pxz +
                                 (float)(cy(q) * cz(q)) * Pyz);
-        f[q * N + flat_bc] = feq[q] + wq(q) * sq * 4.5f;
+        const float v = feq[q] + wq(q) * sq * 4.5f;
+        f[q * N + flat_bc] = v;
+        if (out) out[q] = v;
     }
 }
 
@@ -420,6 +428,54 @@ __global__ void __launch_bounds__(128) k_link_gather(const FusedArgs a) {
     LinkGather<KIND, 1>::run(a, idx, hd);
 }
 
+// The same gather with one thread per link, from the precomputed element
+// pairs: f1 = f_opp(d)(x_f), f2 = the second value; result w1 f1 + w2 f2 - w_d
+// with the rounding of link_value, stored in storage form.
+template <int KIND>
+__global__ void __launch_bounds__(256) k_link_gather_links(const FusedArgs a, const int* __restrict__ subset,
+                                                           long long n_subset, int skip_marked) {
+    using T = typename Store<KIND>::T;
+    long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (subset) {
+        if (t >= n_subset) return;
+        t = __ldg(subset + t);
+        if (t < 0 || t >= a.n_links) {
+            if (a.dev_err) atomicOr(a.dev_err, DEV_ERR_INDEX);
+            return;
+        }
+    } else if (t >= a.n_links) {
+        return;
+    }
+    const uint2 e = __ldg(a.link_src + t);
+    if (skip_marked && (e.y >> 31)) return;
+    const float2 wt = __ldg(a.link_w + t);
+    const unsigned e1 = e.x & 0x7fffffffu, e2 = e.y & 0x7fffffffu;
+    const long long lim = 19LL * a.g.N;
+    if ((long long)e1 >= lim || (long long)e2 >= lim) {
+        if (a.dev_err) atomicOr(a.dev_err, DEV_ERR_INDEX);
+        return;
+    }
+    const float w = (e.x >> 31) ? wq(7) : wq(1);
+    const T* p = reinterpret_cast<const T*>(a.pin[0]);
+    float f1, f2;
+    if (KIND == ST_F32) {
+        f1 = __ldg(reinterpret_cast<const float*>(p) + e1);
+        f2 = __ldg(reinterpret_cast<const float*>(p) + e2);
+    } else if (KIND == ST_F16S) {
+        f1 = __fadd_rn(__half2float(__ldg(reinterpret_cast<const __half*>(p) + e1)), w);
+        f2 = __fadd_rn(__half2float(__ldg(reinterpret_cast<const __half*>(p) + e2)), w);
+    } else {
+        f1 = __fadd_rn(__bfloat162float(__ldg(reinterpret_cast<const __nv_bfloat16*>(p) + e1)), w);
+        f2 = __fadd_rn(__bfloat162float(__ldg(reinterpret_cast<const __nv_bfloat16*>(p) + e2)), w);
+    }
+    const float h = __fsub_rn(__fmaf_rn(wt.x, f1, __fmul_rn(wt.y, f2)), w);
+    T out;
+    if constexpr (KIND == ST_F32) out = __fadd_rn(h, w);
+    else if constexpr (KIND == ST_F16S) out = __float2half_rn(h);
+    else out = __float2bfloat16_rn(h);
+    reinterpret_cast<T*>(a.link_val)[t] = out;
+}
+
 inline dim3 cell_grid(const Geo& g) {
     return dim3((unsigned)((g.nz + TBX - 1) / TBX), (unsigned)((g.ny + TBY - 1) / TBY), (unsigned)g.nx);
 }
@@ -465,6 +521,47 @@ __global__ void __launch_bounds__(BLOCK) k_collide_from_f32(const FusedArgs a, i
     for (int q = 0; q < 19; ++q) h[q] = a.f32[q * a.g.N + idx] - wq(q);
     collide_store<KIND, MODE>(a, idx, i, j, k, h);
 }
+
+// Zou/He and collision of every node of up to FC_MAX_PLANES disjoint planes of
+// one axis: thread t -> plane p with start[p] <= t < start[p + 1].
+struct PlaneSet {
+    int n;
+    fc_plane_bc p[FC_MAX_PLANES];
+    int n1[FC_MAX_PLANES], n2[FC_MAX_PLANES];
+    int start[FC_MAX_PLANES + 1];
+};
+
+template <int KIND, int MODE>
+__global__ void __launch_bounds__(BLOCK) k_planes_zou_he_collide(const FusedArgs a, const PlaneSet ps) {
+    const int t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= ps.start[ps.n]) return;
+    int p = 0;
+    while (p + 1 < ps.n && t >= ps.start[p + 1]) ++p;
+    const fc_plane_bc& pl = ps.p[p];
+    const int u = t - ps.start[p];
+    const int pa = u / ps.n2[p], pb = u - (u / ps.n2[p]) * ps.n2[p];
+    const int idx = (int)plane_flat(pl.axis, pl.plane_idx, pa, pb, a.g.ny, a.g.nz);
+    const long long fi = plane_flat(pl.axis, pl.interior_idx, pa, pb, a.g.ny, a.g.nz);
+    if (a.flags[idx] & CF_SOLID) return;
+    float fv[19];
+    zou_he_node(a.f32, a.g.N, idx, fi, pl.axis, pl.plane_idx, pl.bc_type, pl.u_in_lat, pl.rho_out_lat, pl.sign,
+                fv);
+    const int i = idx / a.g.nynz;
+    const int rem = idx - i * a.g.nynz;
+    const int j = rem / a.g.nz, k = rem - (rem / a.g.nz) * a.g.nz;
+    float h[19];
+#pragma unroll
+    for (int q = 0; q < 19; ++q) h[q] = fv[q] - wq(q);
+    collide_store<KIND, MODE>(a, idx, i, j, k, h);
+}
+
+template <int S, int M>
+struct PlanesLauncher {
+    static int go(const FusedArgs& a, cudaStream_t st, const PlaneSet& ps) {
+        k_planes_zou_he_collide<S, M><<<grid_for(ps.start[ps.n]), BLOCK, 0, st>>>(a, ps);
+        return launch_status();
+    }
+};
 
 // Pin solid cells: populations w_q in the given buffer (shifted => 0), macros (1,0,0,0).
 template <int KIND>
@@ -517,6 +614,11 @@ int make_fused_args(const fc_lbm_step_args* s, FusedArgs& a) {
     a.n_link_pos = s->n_link_pos;
     if (a.link_pos && (a.n_link_pos < a.n_links + 8 || (reinterpret_cast<uintptr_t>(a.link_pos) & 15)))
         a.link_pos = nullptr;
+    a.link_src = reinterpret_cast<const uint2*>(s->link_src);
+    a.n_link_src = s->n_link_src;
+    if (a.link_src && (a.n_link_src < a.n_links || (reinterpret_cast<uintptr_t>(a.link_src) & 7) ||
+                       19LL * a.g.N >= (1LL << 31)))
+        a.link_src = nullptr;
     a.sponge = s->sponge; a.sponge_axis = s->sponge_axis;
     if (a.sponge && (a.sponge_axis < 0 || a.sponge_axis > 2)) return FC_ERR_ARG;
     a.has_links = s->has_links;
@@ -569,6 +671,35 @@ struct CollideF32Launcher {
         return launch_status();
     }
 };
+
+int launch_link_gather(const FusedArgs& a, int storage, cudaStream_t st, const int* subset = nullptr,
+                       long long n_subset = 0, int skip_marked = 0) {
+    if (!a.link_val || a.n_links <= 0) return FC_OK;
+    if (subset && !a.link_src) return FC_ERR_ARG;
+    if (a.link_src) {
+        const long long n = subset ? n_subset : a.n_links;
+        if (n <= 0) return FC_OK;
+        const unsigned nb = (unsigned)((n + 255) / 256);
+        switch (storage) {
+            case ST_F32: k_link_gather_links<ST_F32><<<nb, 256, 0, st>>>(a, subset, n_subset, skip_marked); break;
+            case ST_F16S: k_link_gather_links<ST_F16S><<<nb, 256, 0, st>>>(a, subset, n_subset, skip_marked); break;
+            default: k_link_gather_links<ST_BF16S><<<nb, 256, 0, st>>>(a, subset, n_subset, skip_marked); break;
+        }
+    } else {
+        const unsigned nb = (unsigned)((a.n_link_cells + 127) / 128);
+        switch (storage) {
+            case ST_F32: k_link_gather<ST_F32><<<nb, 128, 0, st>>>(a); break;
+            case ST_F16S: k_link_gather<ST_F16S><<<nb, 128, 0, st>>>(a); break;
+            default: k_link_gather<ST_BF16S><<<nb, 128, 0, st>>>(a); break;
+        }
+    }
+    return launch_status();
+}
+
+template <int S, int M>
+int planes_dispatch(const FusedArgs& a, cudaStream_t st, const PlaneSet& ps) {
+    return PlanesLauncher<S, M>::go(a, st, ps);
+}
 
 }  // namespace
 
@@ -800,14 +931,8 @@ int fc_lbm_fused_step(const fc_lbm_step_args* args, void* stream) {
     const int split = args->link_cells != nullptr && args->n_link_cells > 0 && args->separate_link_pass;
     const int phases = args->phase_mask ? args->phase_mask : 3;
     if (phases & 1) {
-        if (a.link_val && a.n_links > 0) {
-            const unsigned nb = (unsigned)((a.n_link_cells + 127) / 128);
-            switch (args->storage) {
-                case ST_F32: k_link_gather<ST_F32><<<nb, 128, 0, st>>>(a); break;
-                case ST_F16S: k_link_gather<ST_F16S><<<nb, 128, 0, st>>>(a); break;
-                default: k_link_gather<ST_BF16S><<<nb, 128, 0, st>>>(a); break;
-            }
-            rc = launch_status();
+        if (!args->skip_link_gather) {
+            rc = launch_link_gather(a, args->storage, st);
             if (rc) return rc;
         }
         rc = FC_ERR_UNSUPPORTED;
@@ -822,11 +947,56 @@ int fc_lbm_fused_step(const fc_lbm_step_args* args, void* stream) {
 }
 
 long long fc_lbm_tile_links(const fc_lbm_step_args* args, int32_t* records, long long cap, uint16_t* link_pos,
-                            long long pos_cap, void* stream) {
+                            long long pos_cap, uint32_t* link_src, long long src_cap, void* stream) {
     FusedArgs a;
     const int rc = make_fused_args(args, a);
     if (rc) return -rc;
-    return tma_tile_links(a, reinterpret_cast<int4*>(records), cap, link_pos, pos_cap, (cudaStream_t)stream);
+    return tma_tile_links(a, reinterpret_cast<int4*>(records), cap, link_pos, pos_cap,
+                          reinterpret_cast<uint2*>(link_src), src_cap, (cudaStream_t)stream);
+}
+
+int fc_lbm_link_gather(const fc_lbm_step_args* args, const int32_t* subset, long long n_subset, int skip_marked,
+                       void* stream) {
+    FusedArgs a;
+    const int rc = make_fused_args(args, a);
+    if (rc) return rc;
+    if (!args->pop_in || n_subset < 0) return FC_ERR_ARG;
+    return launch_link_gather(a, args->storage, (cudaStream_t)stream, subset, n_subset, skip_marked);
+}
+
+int fc_lbm_planes_zou_he_collide(const fc_lbm_step_args* args, const fc_plane_bc* planes, int n_planes,
+                                 void* stream) {
+    FusedArgs a;
+    const int rc = make_fused_args(args, a);
+    if (rc) return rc;
+    if (!a.f32 || !args->pop_out || !planes || n_planes < 1 || n_planes > FC_MAX_PLANES) return FC_ERR_ARG;
+    PlaneSet ps;
+    ps.n = n_planes;
+    ps.start[0] = 0;
+    for (int p = 0; p < n_planes; ++p) {
+        const fc_plane_bc& pl = planes[p];
+        if (pl.axis != planes[0].axis) return FC_ERR_ARG;            // one axis ...
+        for (int r = 0; r < p; ++r)
+            if (planes[r].plane_idx == pl.plane_idx) return FC_ERR_ARG;   // ... distinct planes
+        if (pl.bc_type != 0 && pl.bc_type != 1) return FC_ERR_ARG;
+        if (plane_dims(pl.axis, a.g.nx, a.g.ny, a.g.nz, &ps.n1[p], &ps.n2[p])) return FC_ERR_ARG;
+        const int na = pl.axis == 0 ? a.g.nx : (pl.axis == 1 ? a.g.ny : a.g.nz);
+        if (pl.plane_idx < 0 || pl.plane_idx >= na || pl.interior_idx < 0 || pl.interior_idx >= na) return FC_ERR_ARG;
+        ps.p[p] = pl;
+        ps.start[p + 1] = ps.start[p] + ps.n1[p] * ps.n2[p];
+    }
+    // a plane whose condition reads a neighbour plane that another condition writes needs the
+    // sequential order: not fused
+    for (int p = 0; p < n_planes; ++p)
+        for (int r = 0; r < n_planes; ++r)
+            if (planes[p].interior_idx == planes[r].plane_idx) return FC_ERR_UNSUPPORTED;
+#define FC_PCASE(S, M) \
+    if (args->storage == S && args->collision == M) return planes_dispatch<S, M>(a, (cudaStream_t)stream, ps);
+    FC_PCASE(ST_F32, CM_BGK) FC_PCASE(ST_F32, CM_TRT) FC_PCASE(ST_F32, CM_MRT) FC_PCASE(ST_F32, CM_MRT_SMAG)
+    FC_PCASE(ST_F16S, CM_BGK) FC_PCASE(ST_F16S, CM_TRT) FC_PCASE(ST_F16S, CM_MRT) FC_PCASE(ST_F16S, CM_MRT_SMAG)
+    FC_PCASE(ST_BF16S, CM_BGK) FC_PCASE(ST_BF16S, CM_TRT) FC_PCASE(ST_BF16S, CM_MRT) FC_PCASE(ST_BF16S, CM_MRT_SMAG)
+#undef FC_PCASE
+    return FC_ERR_ARG;
 }
 
 int fc_lbm_collide_from_f32(const fc_lbm_step_args* args, int axis, int plane_idx, void* stream) {

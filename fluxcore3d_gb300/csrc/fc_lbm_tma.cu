@@ -551,6 +551,32 @@ __global__ void k_link_pos(const FusedArgs a, TileGeo tg, uint16_t* pos) {
     }
 }
 
+// Per-link element pairs of the link gather: f_opp(d) at the link cell, and
+// the second value (f_opp(d) at x_f - c_d, or f_d at x_f); bit 31 of the first
+// marks an edge direction (lattice weight 1/36).
+__global__ void k_link_src(const FusedArgs a, uint2* src) {
+    const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= a.n_link_cells) return;
+    const int idx = __ldg(a.link_cells + t);
+    const uint4 hd = __ldg(a.link_hdr + t);
+    if (idx < 0 || (long long)idx >= a.g.N || (long long)hd.z + __popc(hd.x) > a.n_links) {
+        if (a.dev_err) atomicOr(a.dev_err, DEV_ERR_INDEX);
+        return;
+    }
+    const unsigned N = (unsigned)a.g.N;
+    unsigned rank = 0;
+    for (int d = 1; d < 19; ++d) {
+        if (!(hd.x & (1u << d))) continue;
+        const int o = opp(d);
+        const bool second = (hd.y >> d) & 1u;
+        const int off = cx(d) * a.g.nynz + cy(d) * a.g.nz + cz(d);
+        const unsigned e1 = (unsigned)o * N + (unsigned)idx;
+        const unsigned e2 = second ? (unsigned)o * N + (unsigned)(idx - off) : (unsigned)d * N + (unsigned)idx;
+        src[hd.z + rank] = make_uint2(e1 | (d > 6 ? 0x80000000u : 0u), e2);
+        ++rank;
+    }
+}
+
 // ---------------------------------------------------------------------------
 // host side
 // ---------------------------------------------------------------------------
@@ -636,7 +662,7 @@ bool fused_tma_eligible(const FusedArgs& a, int storage) {
 }
 
 long long tma_tile_links(const FusedArgs& a, int4* out, long long cap, uint16_t* pos, long long pos_cap,
-                         cudaStream_t st) {
+                         uint2* src, long long src_cap, cudaStream_t st) {
     if (!grid_fits(a.g)) return 0;
     const TileGeo tg = tile_geo(a.g, ST_F32);
     if (!out) return tg.n_tiles;
@@ -655,6 +681,14 @@ long long tma_tile_links(const FusedArgs& a, int4* out, long long cap, uint16_t*
     if (pos) {
         if (cudaMemsetAsync(pos, 0xff, sizeof(uint16_t) * (size_t)pos_cap, st) != cudaSuccess) return -FC_ERR_LAUNCH;
         k_link_pos<<<(unsigned)((a.n_link_cells + 127) / 128), 128, 0, st>>>(a, tg, pos);
+        rc = launch_status();
+        if (rc) return -rc;
+    }
+    if (src) {
+        if (src_cap < a.n_links + 8 || (reinterpret_cast<uintptr_t>(src) & 7) || 19LL * a.g.N >= (1LL << 31))
+            return -FC_ERR_ARG;
+        if (cudaMemsetAsync(src, 0, sizeof(uint2) * (size_t)src_cap, st) != cudaSuccess) return -FC_ERR_LAUNCH;
+        k_link_src<<<(unsigned)((a.n_link_cells + 127) / 128), 128, 0, st>>>(a, src);
         rc = launch_status();
         if (rc) return -rc;
     }

@@ -210,21 +210,26 @@ class FusedLBM:
         self.link_val = None
         self.tile_links = None
         self.link_pos = None
+        self.link_src = None
+        N = self.N
         if self.has_links and self.n_links > 0:
             self.link_val = torch.zeros(self.n_links + 8, dtype=STORAGE_DTYPE[self.storage], device=sim.device)
             a.link_val = ptr(self.link_val)
             a.n_link_val = self.link_val.numel()
         nt = 0
         if sim.device.type == "cuda":
-            nt = int(_lib.lib().fc_lbm_tile_links(C.byref(a), None, 0, None, 0, stream_ptr()))
+            nt = int(_lib.lib().fc_lbm_tile_links(C.byref(a), None, 0, None, 0, None, 0, stream_ptr()))
         if nt > 0:
             self.tile_links = torch.zeros((nt, 8), dtype=torch.int32, device=sim.device)
-            pos_ptr, pos_cap = None, 0
+            pos_ptr, pos_cap, src_ptr, src_cap = None, 0, None, 0
             if self.n_links > 0:
                 self.link_pos = torch.zeros(self.n_links + 8, dtype=torch.int16, device=sim.device)
                 pos_ptr, pos_cap = ptr(self.link_pos), self.link_pos.numel()
+                if 19 * N < 2 ** 31:
+                    self.link_src = torch.zeros((self.n_links + 8, 2), dtype=torch.int32, device=sim.device)
+                    src_ptr, src_cap = ptr(self.link_src), self.n_links + 8
             got = int(_lib.lib().fc_lbm_tile_links(C.byref(a), ptr(self.tile_links), nt, pos_ptr, pos_cap,
-                                                   stream_ptr()))
+                                                   src_ptr, src_cap, stream_ptr()))
             if got != nt:
                 raise RuntimeError(f"fc_lbm_tile_links failed: {got}")
             a.tile_links = ptr(self.tile_links)
@@ -232,6 +237,28 @@ class FusedLBM:
             if self.link_pos is not None:
                 a.link_pos = ptr(self.link_pos)
                 a.n_link_pos = pos_cap
+            if self.link_src is not None:
+                a.link_src = ptr(self.link_src)
+                a.n_link_src = src_cap
+        # The link gather for step k+1 may run on a second stream while step k's plane
+        # work runs when no link reads a cell of an inlet/outlet plane.
+        # Links that read a cell of such a plane are marked (bit 31 of their second element)
+        # and gathered after the plane work.
+        self.concurrent_gather = False
+        self._side = None
+        self.late_links = None
+        if self.link_src is not None and self.planes:
+            src = self.link_src[: self.n_links].long()
+            e1 = (src[:, 0] & 0x7FFFFFFF) % N
+            e2 = (src[:, 1] & 0x7FFFFFFF) % N
+            defer = (self.flags.long() & CF_DEFER) != 0
+            late = defer[e1] | defer[e2]
+            if bool(late.any()):
+                self.late_links = torch.nonzero(late).flatten().to(torch.int32).contiguous()
+                marked = self.link_src[: self.n_links, 1].long() | (1 << 31)
+                self.link_src[: self.n_links, 1] = torch.where(late, marked - (1 << 32),
+                                                               self.link_src[: self.n_links, 1].long()).to(torch.int32)
+            self.concurrent_gather = True
         self.refresh_params()
 
     def refresh_params(self):
@@ -287,25 +314,79 @@ class FusedLBM:
         a.pop_out = ptr(self.P[0])
         self._set_macros(self.M[0])
         _lib.call("fc_lbm_collide_from_f32", a, -1, 0, st)
+        if self.concurrent_gather:
+            a.pop_in = ptr(self.P[0])
+            _lib.call("fc_lbm_link_gather", a, None, 0, 0, st)
         self.k = 0
         self.primed = True
 
+    def _plane_set(self):
+        """Fused plane descriptors when every inlet/outlet condition is node-local (Zou/He) on
+        distinct planes of one axis, else None (the sequential reference-order path runs)."""
+        from .lbm_cuda_ext import _bc_plan
+        plan = _bc_plan(self.sim)
+        if not plan or len(plan) > 6 or any(b[0] != "zou_he" for b in plan):
+            return None
+        axes = {b[1] for b in plan}
+        pidx = [b[2] for b in plan]
+        if len(axes) != 1 or len(set(pidx)) != len(pidx) or any(b[3] in pidx for b in plan):
+            return None
+        if sorted((b[1], b[2]) for b in plan) != sorted(self.planes):
+            return None
+        arr = (_lib.PlaneBC * len(plan))()
+        for d, (_, ax, p, ii, code, u, rho, sign, _n1, _n2) in zip(arr, plan):
+            d.axis, d.plane_idx, d.interior_idx, d.bc_type = ax, p, ii, code
+            d.u_in_lat, d.rho_out_lat, d.sign = u, rho, sign
+        return arr
+
+    def _side_stream(self):
+        if self._side is None:
+            self._side = torch.cuda.Stream(device=self.sim.device)
+            self._ev_fork = torch.cuda.Event()
+            self._ev_join = torch.cuda.Event()
+        return self._side
+
     def _enqueue(self, cur, m_out, phase_event=None):
-        """Launch one step's kernels: fused pass P[cur] -> P[1-cur], then the plane BCs."""
+        """Launch one step's kernels: fused pass P[cur] -> P[1-cur], then the plane BCs (and,
+        concurrently with those, the next step's link gather)."""
         sim, a = self.sim, self.args
         st = stream_ptr()
         a.pop_in = ptr(self.P[cur])
         a.pop_out = ptr(self.P[1 - cur])
         a.f32 = ptr(sim.f)
         self._set_macros(m_out)
+        a.skip_link_gather = 1 if self.concurrent_gather else 0
         _lib.call("fc_lbm_fused_step", a, st)
+        a.skip_link_gather = 0
         if phase_event is not None:
             phase_event.record()
+        if self.concurrent_gather:
+            main = torch.cuda.current_stream()
+            side = self._side_stream()
+            self._ev_fork.record(main)
+            side.wait_event(self._ev_fork)
+            a.pop_in = ptr(self.P[1 - cur])   # the next step's input
+            _lib.call("fc_lbm_link_gather", a, None, 0, 1, side.cuda_stream)
+            a.pop_in = ptr(self.P[cur])
+            self._ev_join.record(side)
         if self.planes:
-            from .lbm_cuda_ext import _apply_flow_bcs_cuda
-            _apply_flow_bcs_cuda(sim)
-            for ax, pidx in self.planes:
-                _lib.call("fc_lbm_collide_from_f32", a, ax, pidx, st)
+            ps = self._plane_set()
+            rc = 3
+            if ps is not None:
+                rc = _lib.lib().fc_lbm_planes_zou_he_collide(C.byref(a), ps, len(ps), st)
+                if rc not in (0, 3):
+                    _lib.check(rc, "fc_lbm_planes_zou_he_collide")
+            if rc != 0:
+                from .lbm_cuda_ext import _apply_flow_bcs_cuda
+                _apply_flow_bcs_cuda(sim)
+                for ax, pidx in self.planes:
+                    _lib.call("fc_lbm_collide_from_f32", a, ax, pidx, st)
+        if self.concurrent_gather:
+            if self.late_links is not None:
+                a.pop_in = ptr(self.P[1 - cur])
+                _lib.call("fc_lbm_link_gather", a, ptr(self.late_links), self.late_links.numel(), 0, st)
+                a.pop_in = ptr(self.P[cur])
+            torch.cuda.current_stream().wait_event(self._ev_join)
 
     def _graph(self, cur):
         """CUDA graph of one step without macro output, captured on first use (per parity)."""
@@ -344,6 +425,7 @@ class FusedLBM:
             if mask == 2 and not (a.n_link_cells and a.separate_link_pass):
                 continue
             a.phase_mask = mask
+            a.skip_link_gather = 1 if self.concurrent_gather else 0
             ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(n)]
             cur = self.cur
             for e0, e1 in ev:
@@ -357,6 +439,7 @@ class FusedLBM:
             torch.cuda.synchronize()
             out[name] = sum(e0.elapsed_time(e1) for e0, e1 in ev) / n
         a.phase_mask = 3
+        a.skip_link_gather = 0
         return out
 
     def sync_f(self):

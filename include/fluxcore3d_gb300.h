@@ -132,6 +132,14 @@ typedef struct fc_lbm_step_args {
     const uint16_t* link_pos;    /* optional, from fc_lbm_tile_links: per link, the element of the staged
                                     tile that its value replaces (0xffff: none); n_links + 8 entries */
     int64_t n_link_pos;          /* capacity of link_pos in entries */
+    const uint32_t* link_src;    /* optional, from fc_lbm_tile_links: per link two population element
+                                    indices (q N + cell) of the values it blends, the first with bit 31 set
+                                    for an edge direction (bit 31 of the second: caller's mark, see
+                                    fc_lbm_link_gather); lets the gather run one thread per link */
+    int64_t n_link_src;          /* capacity of link_src in links (2 entries each) */
+    int32_t skip_link_gather;    /* 1: fc_lbm_fused_step does not run the link gather; the caller runs
+                                    fc_lbm_link_gather for this step's input beforehand (e.g. on a second
+                                    stream while the previous step's plane work runs) */
 } fc_lbm_step_args;
 
 /* One full time step for every non-deferred cell. */
@@ -144,11 +152,40 @@ int fc_lbm_fused_step(const fc_lbm_step_args* args, void* stream);
  * then eight 16-bit offsets, from the tile's first link, of the first link of
  * each of its 64-cell chunks -- and, when link_pos is given (pos_cap >=
  * n_links + 8), the staged-tile element each link's value replaces; returns
- * the tile count (cap = records that fit), or a negative status.  Both depend
- * only on the geometry: compute them once after the link tables are built.
+ * the tile count (cap = records that fit), or a negative status.  With
+ * link_src (src_cap >= n_links + 8 links, grid below 113 M cells) it also
+ * fills the per-link element pairs of the link gather.  All of it depends
+ * only on the geometry: compute it once after the link tables are built.
  * No reference counterpart (the reference has no staged pass). */
 long long fc_lbm_tile_links(const fc_lbm_step_args* args, int32_t* records, long long cap, uint16_t* link_pos,
-                            long long pos_cap, void* stream);
+                            long long pos_cap, uint32_t* link_src, long long src_cap, void* stream);
+/* The per-step link gather of fc_lbm_fused_step on its own: interpolated
+ * bounce-back values from args->pop_in into args->link_val, for every link
+ * (subset == NULL; with skip_marked, links whose link_src second index has
+ * bit 31 set are left out) or for the n_subset links listed in subset.  A
+ * caller marks the links that read cells of inlet/outlet planes, gathers the
+ * rest concurrently with the previous step's plane work and the marked ones
+ * after it.  No reference counterpart (the reference evaluates links inside
+ * its IBB kernel). */
+int fc_lbm_link_gather(const fc_lbm_step_args* args, const int32_t* subset, long long n_subset, int skip_marked,
+                       void* stream);
+
+/* One inlet/outlet plane with a node-local (Zou/He) boundary condition. */
+typedef struct {
+    int32_t axis, plane_idx, interior_idx, bc_type;   /* bc_type 0 velocity, 1 pressure (as fc_lbm_zou_he_bc) */
+    float u_in_lat, rho_out_lat;
+    int32_t sign, pad;
+} fc_plane_bc;
+#define FC_MAX_PLANES 6
+/* Zou/He on up to FC_MAX_PLANES planes of one axis (distinct plane indices),
+ * each node's boundary condition on args->f32 followed by its collision into
+ * args->pop_out: fc_lbm_zou_he_bc on every plane in order and then
+ * fc_lbm_collide_from_f32 on every plane, in one launch (the conditions are
+ * node-local and the planes disjoint, so the per-node order is the same).
+ * Fusion of reference lbm_kernels.cu:791-969 with the plane collision. */
+int fc_lbm_planes_zou_he_collide(const fc_lbm_step_args* args, const fc_plane_bc* planes, int n_planes,
+                                 void* stream);
+
 /* Collide cells straight from args->f32: axis < 0 => every fluid cell (start-up),
  * else the plane plane_idx along axis (after that plane's boundary condition). */
 int fc_lbm_collide_from_f32(const fc_lbm_step_args* args, int axis, int plane_idx, void* stream);

@@ -131,6 +131,34 @@ def test_staged_pass_bit_identical_to_direct(cuda, storage, collision):
         assert np.array_equal(a, b), float(np.abs(a.astype(np.float64) - b.astype(np.float64)).max())
 
 
+def test_fused_planes_and_concurrent_gather_bit_identical(cuda, monkeypatch):
+    """Fused Zou/He + collision of the inlet/outlet planes (one launch) and the next step's link
+    gather on a second stream give the same bits as the reference-order plane sequence with the
+    gather inside the step."""
+    from fluxcore3d_gb300.solver.fused_lbm import FusedLBM
+    out = {}
+    for mode in ("fused", "sequential"):
+        sim = cases.pin_fin(device=cuda, collision="mrt", storage="fp16", nx=48, ny=32, nz=48,
+                            n_pins=(3, 2), radius=3.5, height=24, base=4, sponge_length=8)
+        if mode == "sequential":
+            monkeypatch.setattr(FusedLBM, "_plane_set", lambda self: None)
+        LBMCUDAUpgrade.patch(sim)
+        if mode == "sequential":
+            sim._fc.concurrent_gather = False
+        else:
+            assert sim._fc.concurrent_gather and sim._fc._plane_set() is not None
+        for _ in range(40):
+            sim.step(do_thermal=False)
+        sim.sync_f()
+        torch.cuda.synchronize()
+        assert sim._fc.check_device_error() == 0
+        P = sim._fc.P[sim._fc.cur]
+        out[mode] = (P.view(torch.uint8).cpu().numpy(), sim.f.cpu().numpy(), sim.rho.cpu().numpy())
+        monkeypatch.undo()
+    for a, b in zip(out["fused"], out["sequential"]):
+        assert np.array_equal(a, b)
+
+
 def test_fused_step_c1_channel_1000_steps(cuda):
     """Plain method, small channel (64x32x32, BGK FP32, convective outlet, cube IBB): 1000 steps."""
     sim = cases.channel_cube(device=cuda, collision="bgk")
