@@ -96,6 +96,26 @@ class ClockSampler:
                 "reasons": sorted(reasons), "samples": len(sm)}
 
 
+KERNEL = {
+    "tma": "k_fused_tma<FP16 shifted, MRT> (TMA-staged tiles: pull + link slots + packed collide of cell pairs + sponge)",
+    "direct": "k_fused_step<FP16 shifted, MRT> (per-thread pull + bounce-back + collide + sponge)",
+}
+PROFILE = os.path.join(os.path.dirname(os.path.abspath(__file__)), "profiles",
+                       "k_fused_tma_fp16_mrt_pinfin_256x128x128.md")
+
+
+def profiled_traffic(args):
+    """DRAM bytes (read + write) of one launch of the dominant kernel, from the committed ncu
+    summary of this workload (line 'dram_bytes_per_launch: N'), or (None, reason)."""
+    default = (args.nx, args.ny, args.nz, args.collision, args.staging) == (256, 128, 128, "mrt", "tma")
+    if not default or not os.path.exists(PROFILE):
+        return None, "no ncu capture of this configuration"
+    for line in open(PROFILE):
+        if line.startswith("dram_bytes_per_launch:"):
+            return int(line.split(":")[1].strip()), os.path.relpath(PROFILE, os.path.dirname(PROFILE) + "/..")
+    return None, "no dram_bytes_per_launch line in the ncu summary"
+
+
 def dist_env():
     ws = int(os.environ.get("WORLD_SIZE", "1"))
     rank = int(os.environ.get("RANK", "0"))
@@ -109,6 +129,8 @@ def make_case(device, storage, args):
                         nz=args.nz)
     sim.cfg.macro_stride = args.macro_stride
     sim.cfg.lbm_cells_per_thread = getattr(args, "cells_per_thread", 1)
+    sim.cfg.lbm_staging = getattr(args, "staging", "tma")
+    sim.cfg.lbm_link_pass = getattr(args, "link_pass", "inline")
     return sim
 
 
@@ -213,7 +235,7 @@ def cpu_baseline_sample(args):
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=400)
+    ap.add_argument("--steps", type=int, default=2000)
     ap.add_argument("--warmup", type=int, default=20)
     ap.add_argument("--impl", default="fluxcore3d_gb300")
     ap.add_argument("--collision", default="mrt")
@@ -222,6 +244,10 @@ def main():
     ap.add_argument("--nz", type=int, default=128)
     ap.add_argument("--macro-stride", type=int, default=100)
     ap.add_argument("--cells-per-thread", type=int, default=1, choices=(1, 2))
+    ap.add_argument("--staging", default="tma", choices=("tma", "direct"),
+                    help="main pass: TMA-staged tiles (default) or per-thread global loads")
+    ap.add_argument("--link-pass", default="inline", choices=("inline", "separate"),
+                    help="link cells inside the main pass (default) or in their own kernel (direct pass only)")
     ap.add_argument("--cpu-steps", type=int, default=3)
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
@@ -273,15 +299,14 @@ def main():
         traffic = lbm_traffic(sim, sim._fc, sbytes)
         err = sim._fc.check_device_error()
         passes = sim._fc.time_passes(max(20, min(args.steps, 200)))
-        from fluxcore3d_gb300.solver.lbm_cuda_ext import _bc_plan
-        per_step = 1 + (1 if sim._fc.link_cells is not None else 0) + \
-            sum(2 if b[0] == "convective" else 1 for b in _bc_plan(sim)) + len(sim._fc.planes)
+        per_step = sim._fc.launches_per_step()
         results[storage] = dict(total_ms=total_ms, passes=passes, traffic=traffic, clocks=clocks, launches=per_step,
                                 N=sim.nx * sim.ny * sim.nz, planes=len(sim._fc.planes),
                                 links=sim._fc.n_links, err=err)
         del sim
     r = results[storages[0]]
     N = r["N"]
+    traffic, traffic_src = profiled_traffic(args)
     mlups = N * args.steps / (r["total_ms"] / 1e3) / 1e6 * ws
     tr, ps = r["traffic"], r["passes"]
     achieved = tr["main"] / (ps["main"] / 1e3) / 1e9
@@ -312,8 +337,9 @@ def main():
                    "collision": args.collision, "macro_stride": args.macro_stride,
                    "l2_flush": "inputs larger than L2 (2 x 159 MB populations)", "parallelism": "replicas"},
         "roofline": {"bound": "hbm", "achieved": round(achieved, 1), "peak": hbm_peak, "unit": "GB/s",
-                     "frac": round(achieved / hbm_peak, 4), "traffic": None,
-                     "kernel": "k_fused_step<FP16 shifted, MRT> (pull + bounce-back + collide + sponge)",
+                     "frac": round(achieved / hbm_peak, 4), "traffic": traffic,
+                     "kernel": KERNEL[args.staging],
+                     "traffic_source": traffic_src,
                      "kernel_ms": round(ps["main"], 5),
                      "algorithmic_bytes": tr["main"], "peak_kind": peak_kind,
                      "link_pass": {"ms": round(ps.get("links", 0.0), 5), "algorithmic_bytes": tr["links"],

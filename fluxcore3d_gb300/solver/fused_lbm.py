@@ -339,6 +339,21 @@ class FusedLBM:
             d.u_in_lat, d.rho_out_lat, d.sign = u, rho, sign
         return arr
 
+    def launches_per_step(self) -> int:
+        """Kernels one step launches (main pass, link gathers, link-cell pass, plane work)."""
+        n = 1
+        if self.link_val is not None:
+            n += 1 + (1 if self.late_links is not None and self.concurrent_gather else 0)
+        if self.separate_link_pass and self.link_cells is not None:
+            n += 1
+        if self.planes:
+            if self._plane_set() is not None:
+                n += 1
+            else:
+                from .lbm_cuda_ext import _bc_plan
+                n += sum(2 if b[0] == "convective" else 1 for b in _bc_plan(self.sim)) + len(self.planes)
+        return n
+
     def _side_stream(self):
         if self._side is None:
             self._side = torch.cuda.Stream(device=self.sim.device)
