@@ -110,6 +110,7 @@ SIGNATURES: dict[str, tuple] = {
     "fc_mg_jacobi": (i32, [vp, vp, vp, vp, i64, vp]),
     "fc_mg_apply_L": (i32, [vp] * 9 + [f32, i32, i32, i32, i32, i32, vp]),
     "fc_mg_smooth": (i32, [vp] * 11 + [f32, i32, i32, i32, i32, i32, vp]),
+    "fc_mg_smooth_small": (i32, [vp] * 10 + [f32, i32, i32, i32, i32, i32, i32, i32, vp]),
     "fc_mg_smooth_from_zero": (i32, [vp, vp, vp, i64, vp]),
     "fc_mg_residual_restrict": (i32, [vp] * 10 + [f32, i32, i32, i32, i32, i32, vp, i32, i32, i32, vp]),
     "fc_mg_prolong_correct": (i32, [vp, vp, vp, i32, i32, i32, i32, i32, i32, f32, vp]),
@@ -123,7 +124,12 @@ SIGNATURES: dict[str, tuple] = {
     "fc_vec_dot": (i32, [i32, vp, vp, i64, vp, vp, i64, vp, vp]),
     "fc_vec_axpby": (i32, [i32, vp, vp, i64, f64, vp, vp, f64, vp, vp]),
     "fc_vec_convert": (i32, [i32, vp, vp, i64, vp, f64, vp]),
+    "fc_vec_dot2_workspace_bytes": (C.c_int64, [C.c_int64]),
+    "fc_vec_dot2": (i32, [i32, vp, vp, vp, C.c_int64, vp, C.c_int64, vp, vp]),
+    "fc_bicgstab_p": (i32, [i32, vp, vp, vp, C.c_int64, vp, vp]),
+    "fc_bicgstab_xr": (i32, [i32, vp, vp, vp, vp, C.c_int64, vp, i32, vp, C.c_int64, vp]),
     "fc_mg_mop_f64": (i32, [vp] * 8 + [f64, i32, i32, i32, i32, i32, vp, vp, vp, vp]),
+    "fc_mg_mop_f32": (i32, [vp] * 8 + [f32, i32, i32, i32, i32, i32, vp, vp, vp, vp]),
     # thermal
     "fc_thermal_rhs": (i32, [vp] * 7 + [f32, i64, vp]),
     "fc_thermal_reconstruct": (i32, [vp, vp, vp, i32, i32, i32, i32, i32, vp]),

@@ -63,52 +63,149 @@ __global__ void __launch_bounds__(BLOCK) k_axpby(T* __restrict__ y, const T* __r
     if (i >= n) return;
     double a = ha;
     if (da_num) a *= *da_num / (da_den ? *da_den : 1.0);
-    double r = a * (double)x[i] + hb * (double)y[i];
-    if (mask) r *= (double)mask[i];
+    double r = a * (double)x[i];
+    if (hb != 0.0) r += hb * (double)y[i];   // beta 0: y is not read (it may be uninitialised)
+    if (mask && mask[i] == 0.f) r = 0.0;
     y[i] = (T)r;
 }
 
+// (the mask holds 0 / 1, so it selects; scale 1 skips the multiply: FP64 operations
+// per element are expensive on this part)
 template <typename S, typename D>
 __global__ void __launch_bounds__(BLOCK) k_convert(D* __restrict__ d, const S* __restrict__ s, long long n,
                                                    const float* __restrict__ mask, double scale) {
     const long long i = (long long)blockIdx.x * BLOCK + threadIdx.x;
     if (i >= n) return;
-    double v = (double)s[i] * scale;
-    if (mask) v *= (double)mask[i];
-    d[i] = (D)v;
+    D v;
+    if (scale == 1.0) v = (D)s[i];
+    else v = (D)((double)s[i] * scale);
+    if (mask && mask[i] == 0.f) v = (D)0;
+    d[i] = v;
 }
 
 struct Lvl { int nx, ny, nz, ax, out_idx; };
 __device__ __forceinline__ int lowg(const Lvl& g, int a) { return (g.ax == a && g.out_idx != 0) ? 0 : 1; }
 
-// y = M(x) = x + dt L(x) in FP64 (optionally masked, optionally r = b - M(x))
-__global__ void __launch_bounds__(BLOCK) k_mop_f64(const double* __restrict__ x, const float* __restrict__ aE,
+// y = M(x) = x + dt L(x) in the vectors' precision T (optionally masked, optionally r = b - M(x))
+template <typename T>
+__global__ void __launch_bounds__(BLOCK) k_mop_t(const T* __restrict__ x, const float* __restrict__ aE,
                                                    const float* __restrict__ aW, const float* __restrict__ aN,
                                                    const float* __restrict__ aS, const float* __restrict__ aU,
                                                    const float* __restrict__ aD, const float* __restrict__ diagL,
-                                                   double dt, Lvl g, const double* __restrict__ b,
-                                                   const float* __restrict__ mask, double* __restrict__ y) {
+                                                   T dt, Lvl g, const T* __restrict__ b,
+                                                   const float* __restrict__ mask, T* __restrict__ y) {
     const long long n = (long long)g.nx * g.ny * g.nz;
     const long long idx = (long long)blockIdx.x * BLOCK + threadIdx.x;
     if (idx >= n) return;
     const long long nynz = (long long)g.ny * g.nz;
-    const int i = (int)(idx / nynz);
-    const int rr = (int)(idx - i * nynz);
-    const int j = rr / g.nz, k = rr - (rr / g.nz) * g.nz;
+    const int i = (int)idx / (int)nynz;
+    const int rr = (int)idx - i * (int)nynz;
+    const int j = rr / g.nz, k = rr - j * g.nz;
     const int iE = i < g.nx - 1 ? i + 1 : i - 1, iW = i > 0 ? i - 1 : lowg(g, 0);
     const int jN = j < g.ny - 1 ? j + 1 : j - 1, jS = j > 0 ? j - 1 : lowg(g, 1);
     const int kU = k < g.nz - 1 ? k + 1 : k - 1, kD = k > 0 ? k - 1 : lowg(g, 2);
-    const double xc = x[idx];
-    const double L = (double)diagL[idx] * xc - (double)aE[idx] * x[iE * nynz + (long long)j * g.nz + k] -
-                     (double)aW[idx] * x[iW * nynz + (long long)j * g.nz + k] -
-                     (double)aN[idx] * x[i * nynz + (long long)jN * g.nz + k] -
-                     (double)aS[idx] * x[i * nynz + (long long)jS * g.nz + k] -
-                     (double)aU[idx] * x[i * nynz + (long long)j * g.nz + kU] -
-                     (double)aD[idx] * x[i * nynz + (long long)j * g.nz + kD];
-    double m = xc + dt * L;
+    const T xc = x[idx];
+    const T L = (T)diagL[idx] * xc - (T)aE[idx] * x[iE * nynz + (long long)j * g.nz + k] -
+                (T)aW[idx] * x[iW * nynz + (long long)j * g.nz + k] -
+                (T)aN[idx] * x[i * nynz + (long long)jN * g.nz + k] -
+                (T)aS[idx] * x[i * nynz + (long long)jS * g.nz + k] -
+                (T)aU[idx] * x[i * nynz + (long long)j * g.nz + kU] -
+                (T)aD[idx] * x[i * nynz + (long long)j * g.nz + kD];
+    T m = xc + dt * L;
     if (b) m = b[idx] - m;
-    if (mask) m *= (double)mask[idx];
+    if (mask && mask[idx] == 0.f) m = (T)0;
     y[idx] = m;
+}
+
+// ---- BiCGSTAB recurrences with device scalars (slot layout in the header) ----
+// The scalars are formed once by a one-thread kernel, so vector kernels never
+// divide (FP64 division per element would dominate: GB300's FP64 rate is low).
+enum BicgSlot { SL_RHO_NEW = 0, SL_RHO_OLD = 1, SL_ALPHA = 2, SL_OMEGA = 3, SL_RV = 4, SL_TS = 5, SL_TT = 6,
+                SL_RR = 7, SL_BETA = 8 };
+
+// stage 0: beta = (rho_new / rho_old) (alpha / omega) (0 when undefined)
+// stage 1: alpha = rho_new / (r_hat, v)
+// stage 2: omega = (t, s) / (t, t), rho_old = rho_new
+__global__ void k_bicg_scalars(double* __restrict__ sc, int stage) {
+    if (threadIdx.x != 0 || blockIdx.x != 0) return;
+    if (stage == 0) {
+        const double ro = sc[SL_RHO_OLD], om = sc[SL_OMEGA];
+        sc[SL_BETA] = (ro != 0.0 && om != 0.0) ? (sc[SL_RHO_NEW] / ro) * (sc[SL_ALPHA] / om) : 0.0;
+    } else if (stage == 1) {
+        const double rv = sc[SL_RV];
+        sc[SL_ALPHA] = rv != 0.0 ? sc[SL_RHO_NEW] / rv : 0.0;
+    } else {
+        const double tt = sc[SL_TT];
+        sc[SL_OMEGA] = tt > 0.0 ? sc[SL_TS] / tt : 0.0;
+        sc[SL_RHO_OLD] = sc[SL_RHO_NEW];
+    }
+}
+
+// p = r + beta (p - omega v)
+template <typename T>
+__global__ void __launch_bounds__(BLOCK) k_bicg_p(T* __restrict__ p, const T* __restrict__ r,
+                                                  const T* __restrict__ v, long long n,
+                                                  const double* __restrict__ sc) {
+    const long long i = (long long)blockIdx.x * BLOCK + threadIdx.x;
+    if (i >= n) return;
+    const T beta = (T)sc[SL_BETA], om = (T)sc[SL_OMEGA];
+    const T p1 = -om * v[i] + p[i];
+    p[i] = r[i] + beta * p1;
+}
+
+// stage 0: r -= alpha w; x += alpha u
+// stage 1: x += omega u; r -= omega w; part = per-block (r, r) in FP64
+template <typename T>
+__global__ void __launch_bounds__(BLOCK) k_bicg_xr(T* __restrict__ x, T* __restrict__ r, const T* __restrict__ u,
+                                                   const T* __restrict__ w, long long n,
+                                                   const double* __restrict__ sc, int stage,
+                                                   double* __restrict__ part) {
+    __shared__ double sh[BLOCK];
+    const T a = (T)sc[stage == 0 ? SL_ALPHA : SL_OMEGA];
+    double s = 0.0;
+    for (long long i = (long long)blockIdx.x * BLOCK + threadIdx.x; i < n; i += (long long)gridDim.x * BLOCK) {
+        const T ri = -a * w[i] + r[i];
+        r[i] = ri;
+        x[i] = a * u[i] + x[i];
+        if (stage == 1) s += (double)ri * (double)ri;
+    }
+    if (stage == 1) {
+        sh[threadIdx.x] = s;
+        __syncthreads();
+        for (int st = BLOCK / 2; st > 0; st >>= 1) {
+            if ((int)threadIdx.x < st) sh[threadIdx.x] += sh[threadIdx.x + st];
+            __syncthreads();
+        }
+        if (threadIdx.x == 0) part[blockIdx.x] = sh[0];
+    }
+}
+
+// (x, y1) and (x, y2) in one pass, FP64 accumulation: partials [0, nb) and [nb, 2 nb)
+template <typename T>
+__global__ void __launch_bounds__(BLOCK) k_dot2_part(const T* __restrict__ x, const T* __restrict__ y1,
+                                                     const T* __restrict__ y2, long long n,
+                                                     double* __restrict__ part) {
+    __shared__ double sa[BLOCK], sb[BLOCK];
+    double a = 0.0, b = 0.0;
+    for (long long i = (long long)blockIdx.x * BLOCK + threadIdx.x; i < n; i += (long long)gridDim.x * BLOCK) {
+        const double xi = (double)x[i];
+        a += xi * (double)y1[i];
+        b += xi * (double)y2[i];
+    }
+    sa[threadIdx.x] = a;
+    sb[threadIdx.x] = b;
+    __syncthreads();
+    for (int st = BLOCK / 2; st > 0; st >>= 1) {
+        if ((int)threadIdx.x < st) {
+            sa[threadIdx.x] += sa[threadIdx.x + st];
+            sb[threadIdx.x] += sb[threadIdx.x + st];
+        }
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) {
+        part[blockIdx.x] = sa[0];
+        part[gridDim.x + blockIdx.x] = sb[0];
+    }
 }
 
 }  // namespace
@@ -169,16 +266,92 @@ int fc_vec_convert(int kind, void* dst, const void* src, long long n, const floa
     return launch_status();
 }
 
+long long fc_vec_dot2_workspace_bytes(long long n) {
+    if (n < 0) return -1;
+    return (long long)(2 * red_blocks(n) + 2) * (long long)sizeof(double);
+}
+
+int fc_vec_dot2(int is_f64, const void* x, const void* y1, const void* y2, long long n, void* workspace,
+                long long workspace_bytes, double* result2, void* stream) {
+    if (!x || !y1 || !y2 || !result2 || !workspace || n < 0) return FC_ERR_ARG;
+    if (workspace_bytes < fc_vec_dot2_workspace_bytes(n)) return FC_ERR_ARG;
+    const unsigned nb = red_blocks(n);
+    double* part = reinterpret_cast<double*>(workspace);
+    cudaStream_t st = (cudaStream_t)stream;
+    if (is_f64)
+        k_dot2_part<double><<<nb, BLOCK, 0, st>>>((const double*)x, (const double*)y1, (const double*)y2, n, part);
+    else
+        k_dot2_part<float><<<nb, BLOCK, 0, st>>>((const float*)x, (const float*)y1, (const float*)y2, n, part);
+    int rc = launch_status();
+    if (rc) return rc;
+    k_sum<<<1, BLOCK, 0, st>>>(part, (int)nb, result2);
+    rc = launch_status();
+    if (rc) return rc;
+    k_sum<<<1, BLOCK, 0, st>>>(part + nb, (int)nb, result2 + 1);
+    return launch_status();
+}
+
+int fc_bicgstab_p(int is_f64, void* p, const void* r, const void* v, long long n, double* scalars, void* stream) {
+    if (!p || !r || !v || !scalars || n < 0) return FC_ERR_ARG;
+    cudaStream_t st = (cudaStream_t)stream;
+    k_bicg_scalars<<<1, 32, 0, st>>>(scalars, 0);
+    int rc = launch_status();
+    if (rc || n == 0) return rc;
+    if (is_f64)
+        k_bicg_p<double><<<grid_for(n), BLOCK, 0, st>>>((double*)p, (const double*)r, (const double*)v, n, scalars);
+    else
+        k_bicg_p<float><<<grid_for(n), BLOCK, 0, st>>>((float*)p, (const float*)r, (const float*)v, n, scalars);
+    return launch_status();
+}
+
+int fc_bicgstab_xr(int is_f64, void* x, void* r, const void* u, const void* w, long long n, double* scalars,
+                   int stage, void* workspace, long long workspace_bytes, void* stream) {
+    if (!x || !r || !u || !w || !scalars || n < 0 || (stage != 0 && stage != 1)) return FC_ERR_ARG;
+    if (stage == 1 && (!workspace || workspace_bytes < fc_vec_workspace_bytes(n))) return FC_ERR_ARG;
+    cudaStream_t st = (cudaStream_t)stream;
+    k_bicg_scalars<<<1, 32, 0, st>>>(scalars, stage == 0 ? 1 : 2);
+    int rc = launch_status();
+    if (rc) return rc;
+    const unsigned nb = red_blocks(n);
+    double* part = reinterpret_cast<double*>(workspace);
+    if (is_f64)
+        k_bicg_xr<double><<<nb, BLOCK, 0, st>>>((double*)x, (double*)r, (const double*)u, (const double*)w, n,
+                                                scalars, stage, part);
+    else
+        k_bicg_xr<float><<<nb, BLOCK, 0, st>>>((float*)x, (float*)r, (const float*)u, (const float*)w, n, scalars,
+                                               stage, part);
+    rc = launch_status();
+    if (rc) return rc;
+    if (stage == 1) {
+        k_sum<<<1, BLOCK, 0, st>>>(part, (int)nb, scalars + SL_RR);
+        rc = launch_status();
+    }
+    return rc;
+}
+
 // y = M(x) (b == NULL) or y = b - M(x); optionally multiplied by mask.  FP64 vectors, FP32 coefficients.
 int fc_mg_mop_f64(const double* x, const float* aE, const float* aW, const float* aN, const float* aS,
                   const float* aU, const float* aD, const float* diagL, double dt, int nx, int ny, int nz, int ax,
                   int out_idx, const double* b, const float* mask, double* y, void* stream) {
     if (!x || !y || !aE || !aW || !aN || !aS || !aU || !aD || !diagL || nx < 2 || ny < 2 || nz < 2 || ax < 0 || ax > 2)
         return FC_ERR_ARG;
-    if (x == y) return FC_ERR_ARG;
+    if (x == y || (long long)nx * ny * nz >= (1LL << 31)) return FC_ERR_ARG;
     Lvl g{nx, ny, nz, ax, out_idx};
-    k_mop_f64<<<grid_for((long long)nx * ny * nz), BLOCK, 0, (cudaStream_t)stream>>>(x, aE, aW, aN, aS, aU, aD, diagL,
-                                                                                      dt, g, b, mask, y);
+    k_mop_t<double><<<grid_for((long long)nx * ny * nz), BLOCK, 0, (cudaStream_t)stream>>>(
+        x, aE, aW, aN, aS, aU, aD, diagL, dt, g, b, mask, y);
+    return launch_status();
+}
+
+// The same operator on FP32 vectors (the inner solve of the mixed-precision solver).
+int fc_mg_mop_f32(const float* x, const float* aE, const float* aW, const float* aN, const float* aS,
+                  const float* aU, const float* aD, const float* diagL, float dt, int nx, int ny, int nz, int ax,
+                  int out_idx, const float* b, const float* mask, float* y, void* stream) {
+    if (!x || !y || !aE || !aW || !aN || !aS || !aU || !aD || !diagL || nx < 2 || ny < 2 || nz < 2 || ax < 0 || ax > 2)
+        return FC_ERR_ARG;
+    if (x == y || (long long)nx * ny * nz >= (1LL << 31)) return FC_ERR_ARG;
+    Lvl g{nx, ny, nz, ax, out_idx};
+    k_mop_t<float><<<grid_for((long long)nx * ny * nz), BLOCK, 0, (cudaStream_t)stream>>>(
+        x, aE, aW, aN, aS, aU, aD, diagL, dt, g, b, mask, y);
     return launch_status();
 }
 

@@ -66,10 +66,12 @@ __device__ __forceinline__ T apply_L(const Coef& a, const T* __restrict__ x, con
            (T)__ldg(a.aD + n.c) * x[n.d];
 }
 
+// (levels hold fewer than 2^31 cells: 32-bit index arithmetic)
 __device__ __forceinline__ void coords(const Lvl& g, long long idx, int& i, int& j, int& k) {
+    const int id = (int)idx;
     const int nynz = g.ny * g.nz;
-    i = (int)(idx / nynz);
-    const int r = (int)(idx - (long long)i * nynz);
+    i = id / nynz;
+    const int r = id - i * nynz;
     j = r / g.nz;
     k = r - j * g.nz;
 }
@@ -128,6 +130,43 @@ __global__ void __launch_bounds__(BLOCK) k_smooth_zero(float* __restrict__ xo, c
     xo[idx] = 0.f + inv[idx] * (b[idx] - 0.f);
 }
 
+// All sweeps of a level small enough for one CTA (the coarsest level): the
+// iterate ping-pongs in shared memory, each sweep the same arithmetic as
+// k_smooth (the first one as k_smooth_zero when starting from zero).
+constexpr int SMALL_THREADS = 1024;
+constexpr int SMALL_MAX_CELLS = 6144;   // 2 x 24 KB of shared memory, below the 48 KB default
+
+__global__ void __launch_bounds__(SMALL_THREADS) k_smooth_small(float* __restrict__ x, const float* __restrict__ b,
+                                                               const float* __restrict__ inv, Coef a, float dt,
+                                                               Lvl g, int n_sweeps, int from_zero) {
+    extern __shared__ float xs[];
+    const int n = g.nx * g.ny * g.nz;
+    float* cur = xs;
+    float* nxt = xs + n;
+    int s0 = 0;
+    for (int c = threadIdx.x; c < n; c += blockDim.x) {
+        if (from_zero) cur[c] = 0.f + inv[c] * (b[c] - 0.f);
+        else cur[c] = x[c];
+    }
+    if (from_zero) s0 = 1;
+    __syncthreads();
+    for (int sw = s0; sw < n_sweeps; ++sw) {
+        for (int c = threadIdx.x; c < n; c += blockDim.x) {
+            int i, j, k;
+            coords(g, c, i, j, k);
+            const Nb7 nb = nb7(g, i, j, k);
+            const float tc = cur[c];
+            const float lo = tc + dt * apply_L<float>(a, cur, nb, tc);
+            nxt[c] = tc + __ldg(inv + c) * (__ldg(b + c) - lo);
+        }
+        __syncthreads();
+        float* t = cur;
+        cur = nxt;
+        nxt = t;
+    }
+    for (int c = threadIdx.x; c < n; c += blockDim.x) x[c] = cur[c];
+}
+
 // coarse b = mean over each 2x2x2 block of r = mask * (b - M x); fine cells
 // beyond the even-cropped extent do not contribute (view(...).mean semantics)
 __global__ void __launch_bounds__(BLOCK) k_residual_restrict(const float* __restrict__ x, const float* __restrict__ b,
@@ -135,9 +174,10 @@ __global__ void __launch_bounds__(BLOCK) k_residual_restrict(const float* __rest
                                                              float* __restrict__ bc, int cx, int cy, int cz) {
     const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
     if (t >= (long long)cx * cy * cz) return;
-    const int ic = (int)(t / ((long long)cy * cz));
-    const int rr = (int)(t - (long long)ic * cy * cz);
-    const int jc = rr / cz, kc = rr - (rr / cz) * cz;
+    const int cyz = cy * cz;
+    const int ic = (int)t / cyz;
+    const int rr = (int)t - ic * cyz;
+    const int jc = rr / cz, kc = rr - jc * cz;
     float s = 0.f;
 #pragma unroll
     for (int di = 0; di < 2; ++di)
@@ -170,9 +210,10 @@ __global__ void __launch_bounds__(BLOCK) k_prolong_correct(float* __restrict__ x
                                                            int cx, int cy, int cz, float alpha) {
     const long long idx = (long long)blockIdx.x * blockDim.x + threadIdx.x;
     if (idx >= (long long)nx * ny * nz) return;
-    const int i = (int)(idx / ((long long)ny * nz));
-    const int r = (int)(idx - (long long)i * ny * nz);
-    const int j = r / nz, k = r - (r / nz) * nz;
+    const int nyz = ny * nz;
+    const int i = (int)idx / nyz;
+    const int r = (int)idx - i * nyz;
+    const int j = r / nz, k = r - j * nz;
     int i0, i1, j0, j1, k0, k1;
     float li, lj, lk;
     src_coord(i, nx, cx, i0, i1, li);
@@ -289,6 +330,7 @@ __global__ void __launch_bounds__(BLOCK) k_inv_diag(const float* __restrict__ di
 
 int level_ok(const Lvl& g) {
     if (g.nx < 2 || g.ny < 2 || g.nz < 2) return FC_ERR_ARG;
+    if ((long long)g.nx * g.ny * g.nz >= (1LL << 31)) return FC_ERR_ARG;
     if (g.ax < 0 || g.ax > 2) return FC_ERR_ARG;
     return FC_OK;
 }
@@ -331,6 +373,20 @@ int fc_mg_smooth(const float* x_in, float* x_out, const float* b, const float* i
     if (level_ok(g) || !x_in || !x_out || x_in == x_out || !b || !inv_diagM) return FC_ERR_ARG;
     Coef a{aE, aW, aN, aS, aU, aD, diagL};
     k_smooth<<<grid_for((long long)nx * ny * nz), BLOCK, 0, (cudaStream_t)stream>>>(x_in, x_out, b, inv_diagM, a, dt, g);
+    return launch_status();
+}
+
+int fc_mg_smooth_small(float* x, const float* b, const float* inv_diagM, const float* aE, const float* aW,
+                       const float* aN, const float* aS, const float* aU, const float* aD, const float* diagL,
+                       float dt, int nx, int ny, int nz, int ax, int out_idx, int n_sweeps, int from_zero,
+                       void* stream) {
+    Lvl g{nx, ny, nz, ax, out_idx};
+    if (level_ok(g) || !x || !b || !inv_diagM || n_sweeps < 1) return FC_ERR_ARG;
+    const long long n = (long long)nx * ny * nz;
+    if (n > SMALL_MAX_CELLS) return FC_ERR_UNSUPPORTED;
+    Coef a{aE, aW, aN, aS, aU, aD, diagL};
+    k_smooth_small<<<1, SMALL_THREADS, 2 * n * sizeof(float), (cudaStream_t)stream>>>(x, b, inv_diagM, a, dt, g,
+                                                                                     n_sweeps, from_zero != 0);
     return launch_status();
 }
 

@@ -254,6 +254,179 @@ def _vcycle_pc(mg_solver) -> Callable[[Tensor, Tensor], None]:
     return apply
 
 
+class _GraphVcyclePC:
+    """The V-cycle preconditioner r64 -> z64 replayed from one CUDA graph per (r64, z64) buffer
+    pair (two conversions and the ~40 launches of a 5-level V-cycle become one launch).  The
+    graphs are recaptured whenever the hierarchy or dt changes, since both are baked into them."""
+
+    def __init__(self, mg):
+        self.mg = mg
+        self.eager = _vcycle_pc(mg)
+        self.graphs = {}
+        self.key = None
+
+    def _version(self):
+        mg = self.mg
+        return (id(mg._levels), mg._dt_cache, tuple(lv["x"].data_ptr() for lv in mg._levels))
+
+    def __call__(self, r64: Tensor, z64: Tensor) -> None:
+        ver = self._version()
+        if ver != self.key:
+            self.graphs.clear()
+            self.key = ver
+        k = (r64.data_ptr(), z64.data_ptr())
+        g = self.graphs.get(k)
+        if g is None:
+            g = torch.cuda.CUDAGraph()
+            with torch.cuda.graph(g):
+                self.eager(r64, z64)
+            self.graphs[k] = g
+        g.replay()
+
+
+def _graph_pc(mg) -> _GraphVcyclePC:
+    pc = getattr(mg, "_fc_graph_pc", None)
+    if pc is None:
+        pc = _GraphVcyclePC(mg)
+        mg._fc_graph_pc = pc
+    return pc
+
+
+def _bicg_work(mg, shape, dtype, dev) -> dict:
+    """Work vectors and device scalars of the device-resident BiCGSTAB (kept on the solver so
+    the preconditioner graphs, keyed by buffer, are reused from one solve to the next)."""
+    key = "_fc_bicg64" if dtype == torch.float64 else "_fc_bicg32"
+    W = getattr(mg, key, None)
+    if W is None or W["r"].shape != tuple(shape):
+        n = int(torch.tensor(shape).prod())
+        W = {name: torch.zeros(shape, dtype=dtype, device=dev) for name in ("r", "r_hat", "p", "v", "ph", "sh", "t")}
+        W["sc"] = torch.zeros(9, dtype=torch.float64, device=dev)
+        W["init"] = torch.tensor([0, 1, 1, 1, 0, 0, 0, 0, 0], dtype=torch.float64, device=dev)
+        W["ws"] = torch.empty(int(_lib.call("fc_vec_dot2_workspace_bytes", n)), dtype=torch.uint8, device=dev)
+        W["host"] = torch.zeros(4, dtype=torch.float64).pin_memory()
+        W["ev"] = [torch.cuda.Event() for _ in range(4)]
+        setattr(mg, key, W)
+    return W
+
+
+def _bicg_solve(mg, V: _Vec, b: Tensor, x: Tensor, bnorm: float, tol: float, max_it: int, mask: Tensor) -> dict:
+    """Right-preconditioned BiCGSTAB on FP64 or FP32 vectors (the dtype of b and x) with the
+    recurrence scalars on the device (fused update kernels, graph-replayed V-cycles) and the
+    convergence test one iteration late: the host reads iteration k-1's residual norm while
+    iteration k is queued, then confirms with the true residual in the vectors' precision
+    (restarting from it if the recursive residual drifted).  x is updated in place."""
+    f64 = b.dtype == torch.float64
+    n = V.n
+    W = _bicg_work(mg, tuple(b.shape), b.dtype, b.device)
+    r, r_hat, p, v, ph, sh, t, sc = (W[k] for k in ("r", "r_hat", "p", "v", "ph", "sh", "t", "sc"))
+    ws = W["ws"]
+    pc = _graph_pc(mg)
+    st = stream_ptr()
+    lv0 = mg._levels[0]
+    nx, ny, nz = lv0["shape"]
+    mop_name = "fc_mg_mop_f64" if f64 else "fc_mg_mop_f32"
+    dt = float(mg._dt_cache)
+    cps = mg._cptrs(lv0)
+
+    def mop(xv, yv, bv=None):
+        _lib.call(mop_name, ptr(xv), *cps, dt, nx, ny, nz, mg.ax, lv0["out_idx"], ptr(bv), ptr(mask), ptr(yv), st)
+
+    def dot_into(a_, b_, slot):
+        _lib.call("fc_vec_dot", 0 if f64 else 1, ptr(a_), ptr(b_), n, None, ptr(ws), ws.numel(),
+                  ptr(sc[slot:slot + 1]), st)
+
+    def true_res() -> float:
+        mop(x, t, b)
+        dot_into(t, t, 7)
+        return math.sqrt(max(float(sc[7].item()), 0.0)) / bnorm
+
+    def restart():
+        mop(x, r, b)                                  # r = b - A x
+        r_hat.copy_(r)
+        p.zero_()
+        v.zero_()
+        sc.copy_(W["init"])                           # rho_old = alpha = omega = 1
+
+    restart()
+    thr = (tol * bnorm) ** 2
+    hist = []
+    converged = False
+    it = 0
+    k = int(f64)
+    while it < max_it:
+        it += 1
+        dot_into(r_hat, r, 0)                                                      # rho_new
+        _lib.call("fc_bicgstab_p", k, ptr(p), ptr(r), ptr(v), n, ptr(sc), st)     # p = r + beta (p - omega v)
+        pc(p, ph)
+        mop(ph, v)
+        dot_into(r_hat, v, 4)
+        _lib.call("fc_bicgstab_xr", k, ptr(x), ptr(r), ptr(ph), ptr(v), n, ptr(sc), 0, ptr(ws), ws.numel(), st)
+        pc(r, sh)
+        mop(sh, t)
+        _lib.call("fc_vec_dot2", k, ptr(t), ptr(r), ptr(t), n, ptr(ws), ws.numel(), ptr(sc[5:7]), st)
+        _lib.call("fc_bicgstab_xr", k, ptr(x), ptr(r), ptr(sh), ptr(t), n, ptr(sc), 1, ptr(ws), ws.numel(), st)
+        slot = it % 4
+        W["host"][slot:slot + 1].copy_(sc[7:8], non_blocking=True)
+        W["ev"][slot].record()
+        if it == 1:
+            continue
+        prev = (it - 1) % 4
+        W["ev"][prev].synchronize()
+        rr = float(W["host"][prev])
+        if not math.isfinite(rr):
+            break
+        hist.append(math.sqrt(max(rr, 0.0)) / bnorm)
+        if rr < thr:
+            if true_res() < tol:                       # iteration `it` has run too
+                converged = True
+                break
+            restart()
+    res = true_res()
+    return {"converged": converged and res < tol, "it": it, "res_rel": res, "history": hist}
+
+
+def bicgstab_mg_mixed(mg_solver, b: Tensor, x0: Optional[Tensor] = None, tol: float = 1e-8, max_it: int = 300,
+                      inner_tol: float = 1e-4, inner_max: int = 80) -> Tuple[Tensor, dict]:
+    """Mixed-precision solve to an FP64 relative residual `tol`: FP64 iterative refinement
+    (r = b - A x in FP64, x += e) around an FP32 BiCGSTAB on A e = r / |r| preconditioned by the
+    FP32 V-cycle, each inner solve to `inner_tol`.  Only the refinement residuals touch FP64
+    arithmetic, which on GB300 runs far below the FP32 rate."""
+    lv0 = mg_solver._levels[0]
+    mask = lv0["mask_f"]
+    V = _vec(mg_solver)
+    dev = b.device
+    f64 = dict(dtype=torch.float64, device=dev)
+    b64 = torch.empty(lv0["shape"], **f64)
+    V.convert(b64, b.contiguous(), mask)
+    x = torch.zeros(lv0["shape"], **f64)
+    if x0 is not None:
+        V.convert(x, x0.contiguous(), mask)
+    bnorm = math.sqrt(V.dot(b64, b64, 0)) + 1e-300
+    r64 = torch.empty_like(x)
+    t64 = torch.empty_like(x)
+    r32 = torch.empty(lv0["shape"], dtype=torch.float32, device=dev)
+    e32 = torch.zeros_like(r32)
+    total = 0
+    outer = 0
+    hist = []
+    res = float("inf")
+    while True:
+        V.mop64(x, r64, b=b64, mask=mask)              # r = b - A x  (FP64)
+        rn = math.sqrt(V.dot(r64, r64, 11))
+        res = rn / bnorm
+        hist.append(res)
+        if res < tol or total >= max_it or not math.isfinite(res) or outer >= 12:
+            break
+        V.convert(r32, r64, mask, scale=1.0 / rn)      # unit right-hand side in FP32
+        e32.zero_()
+        info = _bicg_solve(mg_solver, V, r32, e32, 1.0, inner_tol, min(inner_max, max_it - total), mask)
+        total += info["it"]
+        V.convert(t64, e32, mask, scale=rn)
+        V.axpby(x, t64, 1.0)                            # x += e
+        outer += 1
+    return x, {"converged": res < tol, "it": total, "outer": outer, "res_rel": res, "history": hist}
+
+
 def _true_res(V: _Vec, x64, b64, mask, tmp64) -> float:
     V.mop64(x64, tmp64, b=b64, mask=mask)
     return math.sqrt(V.dot(tmp64, tmp64, 10))
@@ -272,9 +445,12 @@ def bicgstab_mg_f64(mg_solver, b: Tensor, x0: Optional[Tensor] = None, tol: floa
     x = torch.zeros(lv0["shape"], **f64)
     if x0 is not None:
         V.convert(x, x0.contiguous(), mask)
+    bnorm = math.sqrt(V.dot(b64, b64, 0)) + 1e-300
+    if precond is None and b.is_cuda:
+        info = _bicg_solve(mg_solver, V, b64, x, bnorm, tol, max_it, mask)
+        return x, info
     r = torch.empty_like(x)
     V.mop64(x, r, b=b64, mask=mask)
-    bnorm = math.sqrt(V.dot(b64, b64, 0)) + 1e-300
     r_hat = r.clone()
     p = torch.zeros_like(x)
     v = torch.zeros_like(x)

@@ -193,8 +193,13 @@ class NLevelGeometricMGSolver:
         nx, ny, nz = lv["shape"]
         dt = float(self._dt_cache)
         st = stream_ptr()
-        cur, alt = lv["x"], lv["Lo"]
         cp = self._cptrs(lv)
+        if nx * ny * nz <= 6144:
+            # a small level (the coarsest) runs all its sweeps in one single-CTA launch
+            _lib.call("fc_mg_smooth_small", ptr(lv["x"]), ptr(lv["b_buf"]), ptr(lv["inv_diagM"]), *cp, dt, nx, ny,
+                      nz, self.ax, lv["out_idx"], int(n_sweeps), int(from_zero), st)
+            return
+        cur, alt = lv["x"], lv["Lo"]
         start = 0
         if from_zero:
             _lib.call("fc_mg_smooth_from_zero", ptr(alt), ptr(lv["b_buf"]), ptr(lv["inv_diagM"]), cur.numel(), st)

@@ -215,6 +215,15 @@ int fc_mg_smooth(const float* x_in, float* x_out, const float* b, const float* i
                  const float* aW, const float* aN, const float* aS, const float* aU, const float* aD,
                  const float* diagL, float dt, int nx, int ny, int nz, int ax, int out_idx, void* stream);
 /* the first sweep from a zero guess (nlevel_mg_cuda.py:297 zero + first smooth): x_out = invD b */
+/* All n_sweeps damped-Jacobi sweeps of a level of at most 6144 cells in one
+ * single-CTA launch (the iterate stays in shared memory); the same arithmetic
+ * as fc_mg_smooth_from_zero (from_zero) followed by fc_mg_smooth, so the
+ * coarsest-level solve of the V-cycle (nlevel_mg_cuda.py:271-307, n_coarse
+ * sweeps) is one launch instead of n_coarse.  Status 3 for a larger level. */
+int fc_mg_smooth_small(float* x, const float* b, const float* inv_diagM, const float* aE, const float* aW,
+                       const float* aN, const float* aS, const float* aU, const float* aD, const float* diagL,
+                       float dt, int nx, int ny, int nz, int ax, int out_idx, int n_sweeps, int from_zero,
+                       void* stream);
 int fc_mg_smooth_from_zero(float* x_out, const float* b, const float* inv_diagM, long long n, void* stream);
 /* replaces the residual + _restrict_into pair (nlevel_mg_cuda.py:289-295, :521-528); c* = n* / 2 */
 int fc_mg_residual_restrict(const float* x, const float* b, const float* mask, const float* aE, const float* aW,
@@ -256,9 +265,31 @@ int fc_vec_axpby(int is_f64, void* y, const void* x, long long n, double alpha_h
 /* dst = scale * src (* mask); kind 0 f32->f64, 1 f64->f32, 2 f32->f32, 3 f64->f64 */
 int fc_vec_convert(int kind, void* dst, const void* src, long long n, const float* mask, double scale, void* stream);
 /* y = M(x) or y = b - M(x) in FP64 with the FP32 fine-level coefficients; optional mask */
+/* Fused steps of BiCGSTAB (bicgstab_mg_f64 with FP64 vectors, the inner solve of
+ * bicgstab_mg_mixed with FP32 vectors: is_f64) with the recurrence scalars in
+ * device memory, so an iteration needs no host round trip (the reference's
+ * bicgstab_mg, mg_pcg.py:103-175, reads every scalar on the host).
+ * scalars[9] (FP64): 0 rho_new, 1 rho_old, 2 alpha, 3 omega, 4 (r_hat, v),
+ * 5 (t, s), 6 (t, t), 7 (r, r), 8 beta.
+ *   fc_bicgstab_p:  beta = (rho_new/rho_old)(alpha/omega); p = r + beta (p - omega v)
+ *   fc_bicgstab_xr: stage 0: alpha = rho_new/(r_hat, v); r -= alpha w; x += alpha u
+ *                   stage 1: omega = (t, s)/(t, t); rho_old = rho_new; x += omega u;
+ *                            r -= omega w; scalars[7] = (r, r)
+ *   fc_vec_dot2:    result2[0] = (x, y1), result2[1] = (x, y2) in one pass (FP64) */
+long long fc_vec_dot2_workspace_bytes(long long n);
+int fc_vec_dot2(int is_f64, const void* x, const void* y1, const void* y2, long long n, void* workspace,
+                long long workspace_bytes, double* result2, void* stream);
+int fc_bicgstab_p(int is_f64, void* p, const void* r, const void* v, long long n, double* scalars, void* stream);
+int fc_bicgstab_xr(int is_f64, void* x, void* r, const void* u, const void* w, long long n, double* scalars,
+                   int stage, void* workspace, long long workspace_bytes, void* stream);
 int fc_mg_mop_f64(const double* x, const float* aE, const float* aW, const float* aN, const float* aS,
                   const float* aU, const float* aD, const float* diagL, double dt, int nx, int ny, int nz, int ax,
                   int out_idx, const double* b, const float* mask, double* y, void* stream);
+/* fc_mg_mop_f64 on FP32 vectors (FP32 arithmetic): the operator of the inner
+ * FP32 BiCGSTAB of bicgstab_mg_mixed. */
+int fc_mg_mop_f32(const float* x, const float* aE, const float* aW, const float* aN, const float* aS,
+                  const float* aU, const float* aD, const float* diagL, float dt, int nx, int ny, int nz, int ax,
+                  int out_idx, const float* b, const float* mask, float* y, void* stream);
 
 /* ---------------------------------------------------------------------------
  * Thermal pseudo-time step (the THERMAL_CUDA module surface)

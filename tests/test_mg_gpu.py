@@ -93,6 +93,41 @@ def test_vcycle_solve_matches_oracle(cuda, shape):
     assert info["it"] == ir["it"] == 8
 
 
+@pytest.mark.parametrize("shape,from_zero", [((24, 16, 16), False), ((24, 16, 16), True), ((12, 8, 8), True),
+                                              ((10, 6, 4), False)])
+def test_small_level_smoother_equals_sweep_sequence(cuda, shape, from_zero):
+    """fc_mg_smooth_small (all sweeps in one CTA) gives the same bits as fc_mg_smooth_from_zero +
+    fc_mg_smooth launched once per sweep."""
+    from fluxcore3d_gb300 import _lib
+    from fluxcore3d_gb300._torch import ptr, stream_ptr
+    prob = problem(shape)
+    mg, _ = both(prob)
+    lv = mg._levels[0]
+    nx, ny, nz = lv["shape"]
+    rng = np.random.default_rng(5)
+    x0 = torch.tensor(rng.random(lv["shape"]).astype(np.float32), device="cuda")
+    lv["b_buf"].copy_(torch.tensor(prob[-1], device="cuda"))
+    cp = mg._cptrs(lv)
+    dt = float(mg._dt_cache)
+    n = 7
+    xa = x0.clone()
+    _lib.call("fc_mg_smooth_small", ptr(xa), ptr(lv["b_buf"]), ptr(lv["inv_diagM"]), *cp, dt, nx, ny, nz, mg.ax,
+              lv["out_idx"], n, int(from_zero), stream_ptr())
+    cur, alt = x0.clone(), torch.empty_like(x0)
+    start = 0
+    if from_zero:
+        _lib.call("fc_mg_smooth_from_zero", ptr(alt), ptr(lv["b_buf"]), ptr(lv["inv_diagM"]), cur.numel(),
+                  stream_ptr())
+        cur, alt = alt, cur
+        start = 1
+    for _ in range(start, n):
+        _lib.call("fc_mg_smooth", ptr(cur), ptr(alt), ptr(lv["b_buf"]), ptr(lv["inv_diagM"]), *cp, dt, nx, ny, nz,
+                  mg.ax, lv["out_idx"], stream_ptr())
+        cur, alt = alt, cur
+    torch.cuda.synchronize()
+    assert np.array_equal(xa.cpu().numpy(), cur.cpu().numpy())
+
+
 def test_bicgstab_and_pcg_dropins_match_oracle(cuda):
     prob = problem()
     mg, ref = both(prob)
@@ -115,6 +150,9 @@ def test_certified_solvers_reach_1e8(cuda):
     x2, i2 = mg_pcg.fgmres_mg_f64(mg, b, tol=1e-8, max_it=200, restart=30)
     assert i2["converged"], i2
     assert omg.true_residual(ref, x2.cpu().numpy(), prob[-1]) < 2e-8
+    x3, i3 = mg_pcg.bicgstab_mg_mixed(mg, b, tol=1e-8, max_it=300)
+    assert i3["converged"] and i3["outer"] >= 2, i3
+    assert omg.true_residual(ref, x3.cpu().numpy(), prob[-1]) < 2e-8
 
 
 def test_thermal_kernels(cuda):
