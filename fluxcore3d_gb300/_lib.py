@@ -110,6 +110,7 @@ SIGNATURES: dict[str, tuple] = {
     "fc_mg_jacobi": (i32, [vp, vp, vp, vp, i64, vp]),
     "fc_mg_apply_L": (i32, [vp] * 9 + [f32, i32, i32, i32, i32, i32, vp]),
     "fc_mg_smooth": (i32, [vp] * 11 + [f32, i32, i32, i32, i32, i32, vp]),
+    "fc_mg_smooth_first2": (i32, [vp] * 10 + [f32, i32, i32, i32, i32, i32, vp]),
     "fc_mg_smooth_small": (i32, [vp] * 10 + [f32, i32, i32, i32, i32, i32, i32, i32, vp]),
     "fc_mg_smooth_from_zero": (i32, [vp, vp, vp, i64, vp]),
     "fc_mg_residual_restrict": (i32, [vp] * 10 + [f32, i32, i32, i32, i32, i32, vp, i32, i32, i32, vp]),

@@ -10,6 +10,8 @@
 #include "fc_common.cuh"
 #include "../../include/fluxcore3d_gb300.h"
 
+#include <type_traits>
+
 using namespace fc;
 
 namespace {
@@ -22,17 +24,23 @@ inline unsigned red_blocks(long long n) {
     return (unsigned)(b < MAX_BLOCKS ? (b < 1 ? 1 : b) : MAX_BLOCKS);
 }
 
+// Each thread's strided partial sum is kept in FP32 when both vectors are FP32
+// (a dozen terms per thread at the sizes used; promoting every element to FP64
+// would cost more than the memory traffic on this part), in FP64 otherwise;
+// partials are combined in FP64 in a fixed order.
 template <typename A, typename B>
 __global__ void __launch_bounds__(BLOCK) k_dot_part(const A* __restrict__ x, const B* __restrict__ y, long long n,
                                                     const float* __restrict__ w, double* __restrict__ part) {
     __shared__ double sh[BLOCK];
-    double s = 0.0;
+    constexpr bool F32 = sizeof(A) == 4 && sizeof(B) == 4;
+    using Acc = typename std::conditional<F32, float, double>::type;
+    Acc s = 0;
     for (long long i = (long long)blockIdx.x * BLOCK + threadIdx.x; i < n; i += (long long)gridDim.x * BLOCK) {
-        double t = (double)x[i] * (double)y[i];
-        if (w) t *= (double)w[i];
+        Acc t = (Acc)x[i] * (Acc)y[i];
+        if (w) t *= (Acc)w[i];
         s += t;
     }
-    sh[threadIdx.x] = s;
+    sh[threadIdx.x] = (double)s;
     __syncthreads();
     for (int st = BLOCK / 2; st > 0; st >>= 1) {
         if ((int)threadIdx.x < st) sh[threadIdx.x] += sh[threadIdx.x + st];
@@ -71,14 +79,14 @@ __global__ void __launch_bounds__(BLOCK) k_axpby(T* __restrict__ y, const T* __r
 
 // (the mask holds 0 / 1, so it selects; scale 1 skips the multiply: FP64 operations
 // per element are expensive on this part)
-template <typename S, typename D>
+template <typename S, typename D, bool SCALED>
 __global__ void __launch_bounds__(BLOCK) k_convert(D* __restrict__ d, const S* __restrict__ s, long long n,
                                                    const float* __restrict__ mask, double scale) {
     const long long i = (long long)blockIdx.x * BLOCK + threadIdx.x;
     if (i >= n) return;
     D v;
-    if (scale == 1.0) v = (D)s[i];
-    else v = (D)((double)s[i] * scale);
+    if (SCALED) v = (D)((double)s[i] * scale);
+    else v = (D)s[i];
     if (mask && mask[i] == 0.f) v = (D)0;
     d[i] = v;
 }
@@ -162,15 +170,15 @@ __global__ void __launch_bounds__(BLOCK) k_bicg_xr(T* __restrict__ x, T* __restr
                                                    double* __restrict__ part) {
     __shared__ double sh[BLOCK];
     const T a = (T)sc[stage == 0 ? SL_ALPHA : SL_OMEGA];
-    double s = 0.0;
+    T s = 0;
     for (long long i = (long long)blockIdx.x * BLOCK + threadIdx.x; i < n; i += (long long)gridDim.x * BLOCK) {
         const T ri = -a * w[i] + r[i];
         r[i] = ri;
         x[i] = a * u[i] + x[i];
-        if (stage == 1) s += (double)ri * (double)ri;
+        if (stage == 1) s += ri * ri;
     }
     if (stage == 1) {
-        sh[threadIdx.x] = s;
+        sh[threadIdx.x] = (double)s;
         __syncthreads();
         for (int st = BLOCK / 2; st > 0; st >>= 1) {
             if ((int)threadIdx.x < st) sh[threadIdx.x] += sh[threadIdx.x + st];
@@ -186,14 +194,14 @@ __global__ void __launch_bounds__(BLOCK) k_dot2_part(const T* __restrict__ x, co
                                                      const T* __restrict__ y2, long long n,
                                                      double* __restrict__ part) {
     __shared__ double sa[BLOCK], sb[BLOCK];
-    double a = 0.0, b = 0.0;
+    T a = 0, b = 0;   // per-thread partials in the vectors' precision (as k_dot_part)
     for (long long i = (long long)blockIdx.x * BLOCK + threadIdx.x; i < n; i += (long long)gridDim.x * BLOCK) {
-        const double xi = (double)x[i];
-        a += xi * (double)y1[i];
-        b += xi * (double)y2[i];
+        const T xi = x[i];
+        a += xi * y1[i];
+        b += xi * y2[i];
     }
-    sa[threadIdx.x] = a;
-    sb[threadIdx.x] = b;
+    sa[threadIdx.x] = (double)a;
+    sb[threadIdx.x] = (double)b;
     __syncthreads();
     for (int st = BLOCK / 2; st > 0; st >>= 1) {
         if ((int)threadIdx.x < st) {
@@ -256,13 +264,19 @@ int fc_vec_convert(int kind, void* dst, const void* src, long long n, const floa
     if (n == 0) return FC_OK;
     cudaStream_t st = (cudaStream_t)stream;
     const unsigned g = grid_for(n);
+#define FC_CONV(K, S, D)                                                                                     \
+    case K:                                                                                                 \
+        if (scale == 1.0) k_convert<S, D, false><<<g, BLOCK, 0, st>>>((D*)dst, (const S*)src, n, mask, scale); \
+        else k_convert<S, D, true><<<g, BLOCK, 0, st>>>((D*)dst, (const S*)src, n, mask, scale);              \
+        break;
     switch (kind) {
-        case 0: k_convert<float, double><<<g, BLOCK, 0, st>>>((double*)dst, (const float*)src, n, mask, scale); break;
-        case 1: k_convert<double, float><<<g, BLOCK, 0, st>>>((float*)dst, (const double*)src, n, mask, scale); break;
-        case 2: k_convert<float, float><<<g, BLOCK, 0, st>>>((float*)dst, (const float*)src, n, mask, scale); break;
-        case 3: k_convert<double, double><<<g, BLOCK, 0, st>>>((double*)dst, (const double*)src, n, mask, scale); break;
+        FC_CONV(0, float, double)
+        FC_CONV(1, double, float)
+        FC_CONV(2, float, float)
+        FC_CONV(3, double, double)
         default: return FC_ERR_ARG;
     }
+#undef FC_CONV
     return launch_status();
 }
 

@@ -130,6 +130,24 @@ __global__ void __launch_bounds__(BLOCK) k_smooth_zero(float* __restrict__ xo, c
     xo[idx] = 0.f + inv[idx] * (b[idx] - 0.f);
 }
 
+// The first two sweeps from a zero guess in one pass: x1 = invD b is formed on
+// the fly for the cell and its six neighbours, then x2 = x1 + invD (b - M x1).
+__global__ void __launch_bounds__(BLOCK) k_smooth_first2(float* __restrict__ xo, const float* __restrict__ b,
+                                                         const float* __restrict__ inv, Coef a, float dt, Lvl g) {
+    const long long idx = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (idx >= (long long)g.nx * g.ny * g.nz) return;
+    int i, j, k;
+    coords(g, idx, i, j, k);
+    const Nb7 nb = nb7(g, i, j, k);
+    auto x1 = [&](long long q) { return 0.f + __ldg(inv + q) * (__ldg(b + q) - 0.f); };
+    const float tc = x1(nb.c);
+    const float L = __ldg(a.diagL + nb.c) * tc - __ldg(a.aE + nb.c) * x1(nb.e) - __ldg(a.aW + nb.c) * x1(nb.w) -
+                    __ldg(a.aN + nb.c) * x1(nb.n) - __ldg(a.aS + nb.c) * x1(nb.s) - __ldg(a.aU + nb.c) * x1(nb.u) -
+                    __ldg(a.aD + nb.c) * x1(nb.d);
+    const float lo = tc + dt * L;
+    xo[idx] = tc + __ldg(inv + idx) * (__ldg(b + idx) - lo);
+}
+
 // All sweeps of a level small enough for one CTA (the coarsest level): the
 // iterate ping-pongs in shared memory, each sweep the same arithmetic as
 // k_smooth (the first one as k_smooth_zero when starting from zero).
@@ -150,19 +168,48 @@ __global__ void __launch_bounds__(SMALL_THREADS) k_smooth_small(float* __restric
     }
     if (from_zero) s0 = 1;
     __syncthreads();
-    for (int sw = s0; sw < n_sweeps; ++sw) {
-        for (int c = threadIdx.x; c < n; c += blockDim.x) {
+    if (n <= SMALL_THREADS) {
+        // one cell per thread: its coefficients and neighbour offsets stay in registers
+        const int c = threadIdx.x;
+        const bool act = c < n;
+        Nb7 nb{0, 0, 0, 0, 0, 0, 0};
+        float dg = 0.f, ae = 0.f, aw = 0.f, an = 0.f, as = 0.f, au = 0.f, ad = 0.f, iv = 0.f, bc = 0.f;
+        if (act) {
             int i, j, k;
             coords(g, c, i, j, k);
-            const Nb7 nb = nb7(g, i, j, k);
-            const float tc = cur[c];
-            const float lo = tc + dt * apply_L<float>(a, cur, nb, tc);
-            nxt[c] = tc + __ldg(inv + c) * (__ldg(b + c) - lo);
+            nb = nb7(g, i, j, k);
+            dg = __ldg(a.diagL + c); ae = __ldg(a.aE + c); aw = __ldg(a.aW + c); an = __ldg(a.aN + c);
+            as = __ldg(a.aS + c); au = __ldg(a.aU + c); ad = __ldg(a.aD + c);
+            iv = __ldg(inv + c); bc = __ldg(b + c);
         }
-        __syncthreads();
-        float* t = cur;
-        cur = nxt;
-        nxt = t;
+        for (int sw = s0; sw < n_sweeps; ++sw) {
+            if (act) {
+                const float tc = cur[c];
+                const float L = dg * tc - ae * cur[nb.e] - aw * cur[nb.w] - an * cur[nb.n] - as * cur[nb.s] -
+                                au * cur[nb.u] - ad * cur[nb.d];
+                const float lo = tc + dt * L;
+                nxt[c] = tc + iv * (bc - lo);
+            }
+            __syncthreads();
+            float* t = cur;
+            cur = nxt;
+            nxt = t;
+        }
+    } else {
+        for (int sw = s0; sw < n_sweeps; ++sw) {
+            for (int c = threadIdx.x; c < n; c += blockDim.x) {
+                int i, j, k;
+                coords(g, c, i, j, k);
+                const Nb7 nb = nb7(g, i, j, k);
+                const float tc = cur[c];
+                const float lo = tc + dt * apply_L<float>(a, cur, nb, tc);
+                nxt[c] = tc + __ldg(inv + c) * (__ldg(b + c) - lo);
+            }
+            __syncthreads();
+            float* t = cur;
+            cur = nxt;
+            nxt = t;
+        }
     }
     for (int c = threadIdx.x; c < n; c += blockDim.x) x[c] = cur[c];
 }
@@ -387,6 +434,17 @@ int fc_mg_smooth_small(float* x, const float* b, const float* inv_diagM, const f
     Coef a{aE, aW, aN, aS, aU, aD, diagL};
     k_smooth_small<<<1, SMALL_THREADS, 2 * n * sizeof(float), (cudaStream_t)stream>>>(x, b, inv_diagM, a, dt, g,
                                                                                      n_sweeps, from_zero != 0);
+    return launch_status();
+}
+
+int fc_mg_smooth_first2(float* x_out, const float* b, const float* inv_diagM, const float* aE, const float* aW,
+                        const float* aN, const float* aS, const float* aU, const float* aD, const float* diagL,
+                        float dt, int nx, int ny, int nz, int ax, int out_idx, void* stream) {
+    Lvl g{nx, ny, nz, ax, out_idx};
+    if (level_ok(g) || !x_out || !b || !inv_diagM || x_out == b) return FC_ERR_ARG;
+    Coef a{aE, aW, aN, aS, aU, aD, diagL};
+    k_smooth_first2<<<grid_for((long long)nx * ny * nz), BLOCK, 0, (cudaStream_t)stream>>>(x_out, b, inv_diagM, a,
+                                                                                         dt, g);
     return launch_status();
 }
 

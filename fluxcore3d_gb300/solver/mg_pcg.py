@@ -293,84 +293,108 @@ def _graph_pc(mg) -> _GraphVcyclePC:
 
 
 def _bicg_work(mg, shape, dtype, dev) -> dict:
-    """Work vectors and device scalars of the device-resident BiCGSTAB (kept on the solver so
-    the preconditioner graphs, keyed by buffer, are reused from one solve to the next)."""
+    """Work vectors and device scalars of the device-resident BiCGSTAB, kept on the solver
+    object so the captured iteration graphs (which bake their addresses) are reused from one
+    solve to the next."""
     key = "_fc_bicg64" if dtype == torch.float64 else "_fc_bicg32"
     W = getattr(mg, key, None)
     if W is None or W["r"].shape != tuple(shape):
         n = int(torch.tensor(shape).prod())
-        W = {name: torch.zeros(shape, dtype=dtype, device=dev) for name in ("r", "r_hat", "p", "v", "ph", "sh", "t")}
+        W = {name: torch.zeros(shape, dtype=dtype, device=dev)
+             for name in ("x", "b", "r", "r_hat", "p", "v", "ph", "sh", "t")}
         W["sc"] = torch.zeros(9, dtype=torch.float64, device=dev)
         W["init"] = torch.tensor([0, 1, 1, 1, 0, 0, 0, 0, 0], dtype=torch.float64, device=dev)
         W["ws"] = torch.empty(int(_lib.call("fc_vec_dot2_workspace_bytes", n)), dtype=torch.uint8, device=dev)
-        W["host"] = torch.zeros(4, dtype=torch.float64).pin_memory()
-        W["ev"] = [torch.cuda.Event() for _ in range(4)]
+        W["host"] = torch.zeros(2, dtype=torch.float64).pin_memory()
+        W["ev"] = [torch.cuda.Event() for _ in range(2)]
+        W["graphs"] = {}
         setattr(mg, key, W)
     return W
 
 
 def _bicg_solve(mg, V: _Vec, b: Tensor, x: Tensor, bnorm: float, tol: float, max_it: int, mask: Tensor) -> dict:
     """Right-preconditioned BiCGSTAB on FP64 or FP32 vectors (the dtype of b and x) with the
-    recurrence scalars on the device (fused update kernels, graph-replayed V-cycles) and the
-    convergence test one iteration late: the host reads iteration k-1's residual norm while
-    iteration k is queued, then confirms with the true residual in the vectors' precision
-    (restarting from it if the recursive residual drifted).  x is updated in place."""
+    recurrence scalars on the device.  One iteration -- two V-cycles, two operator applies,
+    three reductions and the fused updates -- is replayed from a CUDA graph; two graphs
+    alternate the pinned slot that receives the iteration's residual norm, and the host tests
+    iteration k-1's norm while iteration k runs, then confirms with the true residual in the
+    vectors' precision (restarting from it if the recursive residual drifted).  x is updated
+    in place."""
     f64 = b.dtype == torch.float64
     n = V.n
     W = _bicg_work(mg, tuple(b.shape), b.dtype, b.device)
-    r, r_hat, p, v, ph, sh, t, sc = (W[k] for k in ("r", "r_hat", "p", "v", "ph", "sh", "t", "sc"))
+    xw, bw, r, r_hat, p, v, ph, sh, t, sc = (W[k] for k in ("x", "b", "r", "r_hat", "p", "v", "ph", "sh", "t",
+                                                            "sc"))
     ws = W["ws"]
-    pc = _graph_pc(mg)
-    st = stream_ptr()
+    pc = _graph_pc(mg).eager
     lv0 = mg._levels[0]
     nx, ny, nz = lv0["shape"]
     mop_name = "fc_mg_mop_f64" if f64 else "fc_mg_mop_f32"
     dt = float(mg._dt_cache)
     cps = mg._cptrs(lv0)
+    k = int(f64)
 
     def mop(xv, yv, bv=None):
-        _lib.call(mop_name, ptr(xv), *cps, dt, nx, ny, nz, mg.ax, lv0["out_idx"], ptr(bv), ptr(mask), ptr(yv), st)
+        _lib.call(mop_name, ptr(xv), *cps, dt, nx, ny, nz, mg.ax, lv0["out_idx"], ptr(bv), ptr(mask), ptr(yv),
+                  stream_ptr())
 
     def dot_into(a_, b_, slot):
         _lib.call("fc_vec_dot", 0 if f64 else 1, ptr(a_), ptr(b_), n, None, ptr(ws), ws.numel(),
-                  ptr(sc[slot:slot + 1]), st)
+                  ptr(sc[slot:slot + 1]), stream_ptr())
 
-    def true_res() -> float:
-        mop(x, t, b)
-        dot_into(t, t, 7)
-        return math.sqrt(max(float(sc[7].item()), 0.0)) / bnorm
-
-    def restart():
-        mop(x, r, b)                                  # r = b - A x
-        r_hat.copy_(r)
-        p.zero_()
-        v.zero_()
-        sc.copy_(W["init"])                           # rho_old = alpha = omega = 1
-
-    restart()
-    thr = (tol * bnorm) ** 2
-    hist = []
-    converged = False
-    it = 0
-    k = int(f64)
-    while it < max_it:
-        it += 1
+    def iteration(slot):
+        st = stream_ptr()
         dot_into(r_hat, r, 0)                                                      # rho_new
         _lib.call("fc_bicgstab_p", k, ptr(p), ptr(r), ptr(v), n, ptr(sc), st)     # p = r + beta (p - omega v)
         pc(p, ph)
         mop(ph, v)
         dot_into(r_hat, v, 4)
-        _lib.call("fc_bicgstab_xr", k, ptr(x), ptr(r), ptr(ph), ptr(v), n, ptr(sc), 0, ptr(ws), ws.numel(), st)
+        _lib.call("fc_bicgstab_xr", k, ptr(xw), ptr(r), ptr(ph), ptr(v), n, ptr(sc), 0, ptr(ws), ws.numel(), st)
         pc(r, sh)
         mop(sh, t)
         _lib.call("fc_vec_dot2", k, ptr(t), ptr(r), ptr(t), n, ptr(ws), ws.numel(), ptr(sc[5:7]), st)
-        _lib.call("fc_bicgstab_xr", k, ptr(x), ptr(r), ptr(sh), ptr(t), n, ptr(sc), 1, ptr(ws), ws.numel(), st)
-        slot = it % 4
+        _lib.call("fc_bicgstab_xr", k, ptr(xw), ptr(r), ptr(sh), ptr(t), n, ptr(sc), 1, ptr(ws), ws.numel(), st)
         W["host"][slot:slot + 1].copy_(sc[7:8], non_blocking=True)
+
+    gkey = (id(mg._levels), dt, tuple(lv["x"].data_ptr() for lv in mg._levels), mask.data_ptr())
+    graphs = W["graphs"].get(gkey)
+    if graphs is None:
+        W["graphs"].clear()
+        graphs = []
+        for slot in range(2):
+            g = torch.cuda.CUDAGraph()
+            with torch.cuda.graph(g):
+                iteration(slot)
+            graphs.append(g)
+        W["graphs"][gkey] = graphs
+
+    def true_res() -> float:
+        mop(xw, t, bw)
+        dot_into(t, t, 7)
+        return math.sqrt(max(float(sc[7].item()), 0.0)) / bnorm
+
+    def restart():
+        mop(xw, r, bw)                                # r = b - A x
+        r_hat.copy_(r)
+        p.zero_()
+        v.zero_()
+        sc.copy_(W["init"])                           # rho_old = alpha = omega = 1
+
+    bw.copy_(b)
+    xw.copy_(x)
+    restart()
+    thr = (tol * bnorm) ** 2
+    hist = []
+    converged = False
+    it = 0
+    while it < max_it:
+        it += 1
+        slot = it % 2
+        graphs[slot].replay()
         W["ev"][slot].record()
         if it == 1:
             continue
-        prev = (it - 1) % 4
+        prev = 1 - slot
         W["ev"][prev].synchronize()
         rr = float(W["host"][prev])
         if not math.isfinite(rr):
@@ -382,6 +406,7 @@ def _bicg_solve(mg, V: _Vec, b: Tensor, x: Tensor, bnorm: float, tol: float, max
                 break
             restart()
     res = true_res()
+    x.copy_(xw)
     return {"converged": converged and res < tol, "it": it, "res_rel": res, "history": hist}
 
 

@@ -201,7 +201,13 @@ class NLevelGeometricMGSolver:
             return
         cur, alt = lv["x"], lv["Lo"]
         start = 0
-        if from_zero:
+        if from_zero and n_sweeps >= 2:
+            # sweeps 1 and 2 from the zero guess in one pass
+            _lib.call("fc_mg_smooth_first2", ptr(alt), ptr(lv["b_buf"]), ptr(lv["inv_diagM"]), *cp, dt, nx, ny, nz,
+                      self.ax, lv["out_idx"], st)
+            cur, alt = alt, cur
+            start = 2
+        elif from_zero:
             _lib.call("fc_mg_smooth_from_zero", ptr(alt), ptr(lv["b_buf"]), ptr(lv["inv_diagM"]), cur.numel(), st)
             cur, alt = alt, cur
             start = 1

@@ -215,6 +215,13 @@ int fc_mg_smooth(const float* x_in, float* x_out, const float* b, const float* i
                  const float* aW, const float* aN, const float* aS, const float* aU, const float* aD,
                  const float* diagL, float dt, int nx, int ny, int nz, int ax, int out_idx, void* stream);
 /* the first sweep from a zero guess (nlevel_mg_cuda.py:297 zero + first smooth): x_out = invD b */
+/* The first two damped-Jacobi sweeps from a zero guess in one pass (x1 = invD b
+ * is formed on the fly for the cell and its neighbours): the pre-smoothing of
+ * a V-cycle level entered with a zero guess (nlevel_mg_cuda.py:271-307,
+ * n_pre = 2) in one launch instead of fc_mg_smooth_from_zero + fc_mg_smooth. */
+int fc_mg_smooth_first2(float* x_out, const float* b, const float* inv_diagM, const float* aE, const float* aW,
+                        const float* aN, const float* aS, const float* aU, const float* aD, const float* diagL,
+                        float dt, int nx, int ny, int nz, int ax, int out_idx, void* stream);
 /* All n_sweeps damped-Jacobi sweeps of a level of at most 6144 cells in one
  * single-CTA launch (the iterate stays in shared memory); the same arithmetic
  * as fc_mg_smooth_from_zero (from_zero) followed by fc_mg_smooth, so the

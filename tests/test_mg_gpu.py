@@ -128,6 +128,29 @@ def test_small_level_smoother_equals_sweep_sequence(cuda, shape, from_zero):
     assert np.array_equal(xa.cpu().numpy(), cur.cpu().numpy())
 
 
+def test_first_two_sweeps_fused(cuda):
+    """fc_mg_smooth_first2 equals fc_mg_smooth_from_zero followed by one fc_mg_smooth (same
+    arithmetic; FMA contraction may differ, so within a few FP32 ulps)."""
+    from fluxcore3d_gb300 import _lib
+    from fluxcore3d_gb300._torch import ptr, stream_ptr
+    prob = problem((40, 24, 20))
+    mg, _ = both(prob)
+    lv = mg._levels[0]
+    nx, ny, nz = lv["shape"]
+    lv["b_buf"].copy_(torch.tensor(prob[-1], device="cuda"))
+    cp = mg._cptrs(lv)
+    dt = float(mg._dt_cache)
+    fused = torch.empty_like(lv["x"])
+    _lib.call("fc_mg_smooth_first2", ptr(fused), ptr(lv["b_buf"]), ptr(lv["inv_diagM"]), *cp, dt, nx, ny, nz,
+              mg.ax, lv["out_idx"], stream_ptr())
+    x1, x2 = torch.empty_like(fused), torch.empty_like(fused)
+    _lib.call("fc_mg_smooth_from_zero", ptr(x1), ptr(lv["b_buf"]), ptr(lv["inv_diagM"]), x1.numel(), stream_ptr())
+    _lib.call("fc_mg_smooth", ptr(x1), ptr(x2), ptr(lv["b_buf"]), ptr(lv["inv_diagM"]), *cp, dt, nx, ny, nz,
+              mg.ax, lv["out_idx"], stream_ptr())
+    torch.cuda.synchronize()
+    assert rel(fused.cpu().numpy(), x2.cpu().numpy()) < 1e-6
+
+
 def test_bicgstab_and_pcg_dropins_match_oracle(cuda):
     prob = problem()
     mg, ref = both(prob)
