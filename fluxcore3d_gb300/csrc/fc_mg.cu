@@ -273,6 +273,49 @@ __global__ void __launch_bounds__(BLOCK) k_prolong_correct(float* __restrict__ x
     x[idx] = (x[idx] + alpha * e) * __ldg(mask + idx);
 }
 
+// Exact 2:1 coarsening on every axis (nf = 2 nc): the align_corners = False
+// source coordinate is 0.5 i - 0.25 exactly, so i = 2m gives (m - 1, m, 0.75)
+// (m = 0: (0, 0, 0) after the clamp at 0) and i = 2m + 1 gives (m, m + 1, 0.25)
+// (m + 1 clamped to nc - 1) -- the same values src_coord computes.  3D launch:
+// x = k, y = j, z = i, so no index division.
+__device__ __forceinline__ void src_2to1(int i, int nc, int& i0, int& i1, float& l1) {
+    const int m = i >> 1;
+    if (i & 1) {
+        i0 = m;
+        i1 = m + 1 < nc ? m + 1 : m;
+        l1 = 0.25f;
+    } else if (m == 0) {
+        i0 = 0;
+        i1 = nc > 1 ? 1 : 0;
+        l1 = 0.f;
+    } else {
+        i0 = m - 1;
+        i1 = m;
+        l1 = 0.75f;
+    }
+}
+
+__global__ void __launch_bounds__(BLOCK) k_prolong_2to1(float* __restrict__ x, const float* __restrict__ xc,
+                                                        const float* __restrict__ mask, int nx, int ny, int nz,
+                                                        int cx, int cy, int cz, float alpha) {
+    const int k = blockIdx.x * 64 + (threadIdx.x & 63);
+    const int j = blockIdx.y * 4 + (threadIdx.x >> 6);
+    const int i = blockIdx.z;
+    if (k >= nz || j >= ny) return;
+    const int idx = (i * ny + j) * nz + k;
+    int i0, i1, j0, j1, k0, k1;
+    float li, lj, lk;
+    src_2to1(i, cx, i0, i1, li);
+    src_2to1(j, cy, j0, j1, lj);
+    src_2to1(k, cz, k0, k1, lk);
+    const float hi = 1.f - li, hj = 1.f - lj, hk = 1.f - lk;
+    const int p0 = i0 * cy * cz, p1 = i1 * cy * cz, r0 = j0 * cz, r1 = j1 * cz;
+    auto X = [&](int p, int r, int c) { return __ldg(xc + p + r + c); };
+    const float e = hi * (hj * (hk * X(p0, r0, k0) + lk * X(p0, r0, k1)) + lj * (hk * X(p0, r1, k0) + lk * X(p0, r1, k1))) +
+                    li * (hj * (hk * X(p1, r0, k0) + lk * X(p1, r0, k1)) + lj * (hk * X(p1, r1, k0) + lk * X(p1, r1, k1)));
+    x[idx] = (x[idx] + alpha * e) * __ldg(mask + idx);
+}
+
 // per-block partial sums of (w * (b - M x))^2 in FP64, w = mask or 1
 __global__ void __launch_bounds__(BLOCK) k_residual_sq(const float* __restrict__ x, const float* __restrict__ b,
                                                        const float* __restrict__ mask, Coef a, float dt, Lvl g,
@@ -471,8 +514,14 @@ int fc_mg_residual_restrict(const float* x, const float* b, const float* mask, c
 int fc_mg_prolong_correct(float* x, const float* x_coarse, const float* mask, int nx, int ny, int nz, int cx,
                           int cy, int cz, float alpha, void* stream) {
     if (!x || !x_coarse || !mask || nx < 1 || ny < 1 || nz < 1 || cx < 1 || cy < 1 || cz < 1) return FC_ERR_ARG;
-    k_prolong_correct<<<grid_for((long long)nx * ny * nz), BLOCK, 0, (cudaStream_t)stream>>>(
-        x, x_coarse, mask, nx, ny, nz, cx, cy, cz, alpha);
+    if ((long long)nx * ny * nz >= (1LL << 31)) return FC_ERR_ARG;
+    if (nx == 2 * cx && ny == 2 * cy && nz == 2 * cz) {
+        const dim3 grid((unsigned)((nz + 63) / 64), (unsigned)((ny + 3) / 4), (unsigned)nx);
+        k_prolong_2to1<<<grid, BLOCK, 0, (cudaStream_t)stream>>>(x, x_coarse, mask, nx, ny, nz, cx, cy, cz, alpha);
+    } else {
+        k_prolong_correct<<<grid_for((long long)nx * ny * nz), BLOCK, 0, (cudaStream_t)stream>>>(
+            x, x_coarse, mask, nx, ny, nz, cx, cy, cz, alpha);
+    }
     return launch_status();
 }
 

@@ -267,7 +267,8 @@ class _GraphVcyclePC:
 
     def _version(self):
         mg = self.mg
-        return (id(mg._levels), mg._dt_cache, tuple(lv["x"].data_ptr() for lv in mg._levels))
+        return (id(mg._levels), mg._dt_cache, tuple(lv["x"].data_ptr() for lv in mg._levels), mg.n_pre, mg.n_post,
+                mg.n_coarse)
 
     def __call__(self, r64: Tensor, z64: Tensor) -> None:
         ver = self._version()
@@ -356,7 +357,8 @@ def _bicg_solve(mg, V: _Vec, b: Tensor, x: Tensor, bnorm: float, tol: float, max
         _lib.call("fc_bicgstab_xr", k, ptr(xw), ptr(r), ptr(sh), ptr(t), n, ptr(sc), 1, ptr(ws), ws.numel(), st)
         W["host"][slot:slot + 1].copy_(sc[7:8], non_blocking=True)
 
-    gkey = (id(mg._levels), dt, tuple(lv["x"].data_ptr() for lv in mg._levels), mask.data_ptr())
+    gkey = (id(mg._levels), dt, tuple(lv["x"].data_ptr() for lv in mg._levels), mask.data_ptr(), mg.n_pre,
+            mg.n_post, mg.n_coarse)
     graphs = W["graphs"].get(gkey)
     if graphs is None:
         W["graphs"].clear()
