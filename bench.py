@@ -363,6 +363,8 @@ def main():
         try:
             th = thermal_run(args, dev)
             if th:
+                if th.get("mixed_bicgstab_ms"):
+                    th["mixed_speedup_over_plain"] = round(th["plain_bicgstab_ms"] / th["mixed_bicgstab_ms"], 3)
                 line["thermal"] = th
         except ImportError:
             pass
