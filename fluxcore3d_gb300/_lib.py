@@ -155,6 +155,14 @@ SIGNATURES: dict[str, tuple] = {
     "fc_nn_mse_workspace_bytes": (i64, [i64]),
     "fc_nn_mse_grad": (i32, [vp, i32, vp, vp, i64, vp, vp, i64, vp]),
     "fc_nn_adam": (i32, [vp, vp, vp, vp, vp, i64, i32, i32, f32, f32, f32, f32, i32, f32, vp]),
+    # geometry set-up
+    "fc_geom_edt_workspace_bytes": (i64, [i32, i32, i32]),
+    "fc_geom_signed_edt": (i32, [vp, i32, i32, i32, f64, vp, vp, i64, vp]),
+    "fc_ibb_links_workspace_bytes": (i64, [i32, i32, i32]),
+    "fc_ibb_count_links": (i32, [vp, i32, i32, i32, vp, i64, vp, vp]),
+    "fc_ibb_build_links": (i32, [vp, i32, i32, i32, vp, i64, i64, vp, vp, vp, vp, vp, vp, vp]),
+    "fc_ibb_q_from_sdf": (i32, [vp, i32, i32, i32, f32, f32, f32, f64, i32, vp, vp, i64, vp, vp, vp, vp, vp, vp]),
+    "fc_ibb_weights_from_q": (i32, [vp, i64, vp, vp, vp, vp]),
 }
 
 STATUS_TEXT = {1: "bad argument", 2: "CUDA launch failure", 3: "unsupported combination",

@@ -221,8 +221,7 @@ def channel_cube(device="cuda", collision="bgk", storage="fp32", nx=64, ny=32, n
     solid = geo.cube_mask((nx, ny, nz), (cube_x, ny // 2, nz // 2), (cube, cube, cube), device=device)
     ibb = None
     if with_links:
-        phi = torch.tensor(geo.phi_from_voxels(solid.cpu().numpy()), dtype=torch.float32, device=device)
-        ibb = geo.ibb_from_phi_trilinear(solid, phi)
+        ibb = geo.ibb_from_voxels(solid)
     sf = stamp_walls(cfg, solid)
     return LatticeCase(cfg, u, u * cube / Re, solid, sf, ibb, device=device, seed=seed)
 

@@ -1,15 +1,20 @@
 """Voxel geometry and interpolated-bounce-back (Bouzidi) link data.
 
 `IBBData` has the field layout of the reference's pre_post/sdf_tracing.py:9-18.
-`build_links_from_mask` follows sdf_tracing.py:20-85: a link is a fluid cell
-x_f whose neighbour x_f + c_q (q = 1..18, no wrap) is solid; the arrays are
-concatenated over q = 1..18 with cells in row-major order inside each q, and
-x_ff = x_f - c_q is the second fluid node (valid when inside the box and fluid).
-`bfl_weights_from_q` follows sdf_tracing.py:188-205.
-`q_from_sdf_trilinear` restates bfl_q_from_sdf / sdf_trilinear
-(sdf_tracing.py:89-184): 6 coarse samples along the link and 10 bisections of
-the trilinearly interpolated level set, each operation rounded separately in
-FP32 as the reference's elementwise torch ops are.
+The set-up runs on the device through the library's geometry kernels:
+
+* `signed_distance` -- the voxel SDF of build_phi_from_voxel_mask_mm
+  (sdf_tracing.py:312-340): exact Euclidean distance to the nearest cell of the
+  other kind times the pitch, negative in the solid, FP32 equal bit for bit to
+  the host scipy.ndimage.distance_transform_edt result the reference casts.
+* `build_links` -- build_links_from_mask_gpu (sdf_tracing.py:20-85): a link is a
+  fluid cell x_f whose neighbour x_f + c_q (q = 1..18, no wrap) is solid; the
+  arrays are grouped by q = 1..18 with cells in row-major order inside each q,
+  and x_ff = x_f - c_q is the second fluid node (valid when inside the box and
+  fluid).
+* `ibb_from_phi` -- build_ibb_from_sdf_gpu's fractions (bfl_q_from_sdf /
+  sdf_trilinear, sdf_tracing.py:89-184: 6 coarse samples and 10 bisections of
+  the trilinear level set in FP32) and bfl_weights_from_q (:188-205).
 
 The synthetic heat-sink geometries (cube channel, pin fin, gyroid, random
 spheres) are generated here on the device; their link fractions come either
@@ -23,6 +28,9 @@ from dataclasses import dataclass
 
 import numpy as np
 import torch
+
+from . import _lib
+from ._torch import ptr, stream_ptr
 
 C_NP = np.array([[0, 0, 0], [1, 0, 0], [-1, 0, 0], [0, 1, 0], [0, -1, 0], [0, 0, 1], [0, 0, -1],
                  [1, 1, 0], [1, -1, 0], [-1, 1, 0], [-1, -1, 0], [1, 0, 1], [1, 0, -1], [-1, 0, 1],
@@ -43,138 +51,98 @@ class IBBData:
     ff_valid: torch.Tensor
 
 
-def build_links_from_mask(solid: torch.Tensor):
-    nx, ny, nz = solid.shape
-    dev = solid.device
-    fluid = ~solid
-    I = torch.arange(nx, device=dev).view(nx, 1, 1).expand(nx, ny, nz)
-    J = torch.arange(ny, device=dev).view(1, ny, 1).expand(nx, ny, nz)
-    K = torch.arange(nz, device=dev).view(1, 1, nz).expand(nx, ny, nz)
-    flats, dirs, ffs, oks = [], [], [], []
-    for q in range(1, 19):
-        cx, cy, cz = (int(v) for v in C_NP[q])
-        nb = torch.zeros_like(solid)
-        # neighbour x + c (no wrap)
-        xs = slice(max(0, -cx), nx - max(0, cx))
-        ys = slice(max(0, -cy), ny - max(0, cy))
-        zs = slice(max(0, -cz), nz - max(0, cz))
-        xd = slice(max(0, cx), nx - max(0, -cx))
-        yd = slice(max(0, cy), ny - max(0, -cy))
-        zd = slice(max(0, cz), nz - max(0, -cz))
-        nb[xs, ys, zs] = solid[xd, yd, zd]
-        m = fluid & nb
-        if not bool(m.any()):
-            continue
-        i, j, k = I[m], J[m], K[m]
-        flat = (i * (ny * nz) + j * nz + k).to(torch.int64)
-        iff, jff, kff = i - cx, j - cy, k - cz
-        inb = (iff >= 0) & (iff < nx) & (jff >= 0) & (jff < ny) & (kff >= 0) & (kff < nz)
-        ok = inb.clone()
-        ok[inb] = fluid[iff[inb], jff[inb], kff[inb]]
-        fff = (iff.clamp(0, nx - 1) * (ny * nz) + jff.clamp(0, ny - 1) * nz + kff.clamp(0, nz - 1)).to(torch.int64)
-        flats.append(flat)
-        dirs.append(torch.full_like(flat, q))
-        ffs.append(fff)
-        oks.append(ok)
-    if not flats:
-        e = torch.zeros(0, dtype=torch.int64, device=dev)
-        return e, e.clone(), e.clone(), e.clone(), torch.zeros(0, dtype=torch.bool, device=dev)
-    fluid_flat = torch.cat(flats)
-    dir_i = torch.cat(dirs)
-    ff_flat = torch.cat(ffs)
-    ff_valid = torch.cat(oks)
-    dir_opp = torch.as_tensor(OPP_NP, device=dev)[dir_i]
+def _mask_u8(solid: torch.Tensor) -> torch.Tensor:
+    if not isinstance(solid, torch.Tensor) or solid.dim() != 3:
+        raise ValueError("solid must be a (nx, ny, nz) tensor")
+    if not solid.is_cuda:
+        raise RuntimeError("geometry set-up runs on a CUDA device: move the solid mask to the GPU")
+    return solid.contiguous().to(torch.uint8)
+
+
+def _check_errword(err: torch.Tensor, what: str) -> None:
+    e = int(err.item())
+    if e:
+        raise RuntimeError(f"{what}: device error word {e:#x} (link index out of range)")
+
+
+def signed_distance(solid: torch.Tensor, pitch: float = 1.0) -> torch.Tensor:
+    """Signed distance of a voxel mask (positive in fluid) times `pitch`, FP32 on the mask's
+    device: build_phi_from_voxel_mask_mm (sdf_tracing.py:312-340)."""
+    s = _mask_u8(solid)
+    nx, ny, nz = s.shape
+    L = _lib.lib()
+    ws = torch.empty(max(1, int(L.fc_geom_edt_workspace_bytes(nx, ny, nz))), dtype=torch.uint8, device=s.device)
+    phi = torch.empty((nx, ny, nz), dtype=torch.float32, device=s.device)
+    _lib.call("fc_geom_signed_edt", ptr(s), nx, ny, nz, float(pitch), ptr(phi), ptr(ws), ws.numel(), stream_ptr())
+    return phi
+
+
+def build_links(solid: torch.Tensor):
+    """(fluid_flat, dir_i, dir_opp, ff_flat, ff_valid) of build_links_from_mask_gpu (sdf_tracing.py:20-85),
+    int64 / bool on the mask's device, in the reference's order."""
+    s = _mask_u8(solid)
+    nx, ny, nz = s.shape
+    dev = s.device
+    L = _lib.lib()
+    ws = torch.empty(int(L.fc_ibb_links_workspace_bytes(nx, ny, nz)), dtype=torch.uint8, device=dev)
+    total = torch.zeros(1, dtype=torch.int64, device=dev)
+    st = stream_ptr()
+    _lib.call("fc_ibb_count_links", ptr(s), nx, ny, nz, ptr(ws), ws.numel(), ptr(total), st)
+    n = int(total.item())
+    out = [torch.empty(n, dtype=torch.int64, device=dev) for _ in range(4)]
+    ff_valid = torch.empty(n, dtype=torch.bool, device=dev)
+    err = torch.zeros(1, dtype=torch.int32, device=dev)
+    _lib.call("fc_ibb_build_links", ptr(s), nx, ny, nz, ptr(ws), ws.numel(), n, *(ptr(t) for t in out),
+              ptr(ff_valid), ptr(err), st)
+    _check_errword(err, "fc_ibb_build_links")
+    fluid_flat, dir_i, dir_opp, ff_flat = out
     return fluid_flat, dir_i, dir_opp, ff_flat, ff_valid
 
 
 def bfl_weights_from_q(q: torch.Tensor):
-    ge = q >= 0.5
-    qg = torch.where(ge, q, torch.ones_like(q))
-    w1_ge = 1.0 / (2.0 * qg)
-    w2_ge = 1.0 - w1_ge
-    ql = torch.where(~ge, q, 0.25 * torch.ones_like(q))
-    w1_lt = 2.0 * ql
-    w2_lt = 1.0 - 2.0 * ql
-    return ge, torch.where(ge, w1_ge, w1_lt), torch.where(ge, w2_ge, w2_lt)
+    """(q >= 1/2, w1, w2) of bfl_weights_from_q (sdf_tracing.py:188-205) for FP32 fractions on the GPU."""
+    if not q.is_cuda:
+        raise RuntimeError("q must be on CUDA")
+    q = q.contiguous().to(torch.float32)
+    n = q.numel()
+    ge = torch.empty(n, dtype=torch.bool, device=q.device)
+    w1 = torch.empty(n, dtype=torch.float32, device=q.device)
+    w2 = torch.empty(n, dtype=torch.float32, device=q.device)
+    _lib.call("fc_ibb_weights_from_q", ptr(q), n, ptr(ge), ptr(w1), ptr(w2), stream_ptr())
+    return ge, w1, w2
 
 
-def _trilinear(phi: torch.Tensor, origin: torch.Tensor, dx: float, x: torch.Tensor) -> torch.Tensor:
-    g = (x - origin) / dx
-    gx = g[..., 0].clamp(0.0, phi.shape[0] - 1.001)
-    gy = g[..., 1].clamp(0.0, phi.shape[1] - 1.001)
-    gz = g[..., 2].clamp(0.0, phi.shape[2] - 1.001)
-    i0, j0, k0 = gx.floor().long(), gy.floor().long(), gz.floor().long()
-    fx, fy, fz = gx - i0.to(gx.dtype), gy - j0.to(gy.dtype), gz - k0.to(gz.dtype)
-    i1 = (i0 + 1).clamp_max(phi.shape[0] - 1)
-    j1 = (j0 + 1).clamp_max(phi.shape[1] - 1)
-    k1 = (k0 + 1).clamp_max(phi.shape[2] - 1)
-    c000, c100 = phi[i0, j0, k0], phi[i1, j0, k0]
-    c010, c110 = phi[i0, j1, k0], phi[i1, j1, k0]
-    c001, c101 = phi[i0, j0, k1], phi[i1, j0, k1]
-    c011, c111 = phi[i0, j1, k1], phi[i1, j1, k1]
-    a00 = c000 + fx * (c100 - c000)
-    a10 = c010 + fx * (c110 - c010)
-    a01 = c001 + fx * (c101 - c001)
-    a11 = c011 + fx * (c111 - c011)
-    b0 = a00 + fy * (a10 - a00)
-    b1 = a01 + fy * (a11 - a01)
-    return b0 + fz * (b1 - b0)
-
-
-def q_from_sdf_trilinear(phi, origin, dx, x0, d, L, n_coarse: int = 6, n_bisect: int = 10):
-    n = x0.shape[0]
-    tv = torch.linspace(0.0, 1.0, steps=n_coarse + 1, device=x0.device, dtype=x0.dtype)
-    t = tv[None, :] * L[:, None]
-    xs = x0[:, None, :] + t[:, :, None] * d[:, None, :]
-    ph = _trilinear(phi, origin, dx, xs.reshape(-1, 3)).reshape(n, -1)
-    s = ph > 0
-    cross = s[:, :-1] & (~s[:, 1:])
-    q = torch.full((n,), 0.5, device=x0.device, dtype=x0.dtype)
-    anyc = cross.any(dim=1)
-    if bool(anyc.any()):
-        idx = cross.float().argmax(dim=1).long()
-        lo = t.gather(1, idx[:, None]).squeeze(1)
-        hi = t.gather(1, (idx + 1)[:, None]).squeeze(1)
-        for _ in range(n_bisect):
-            mid = 0.5 * (lo + hi)
-            pm = _trilinear(phi, origin, dx, x0 + mid[:, None] * d)
-            lo = torch.where(pm > 0, mid, lo)
-            hi = torch.where(pm > 0, hi, mid)
-        q = torch.where(anyc, hi / (L + 1e-30), q)
-    return q
-
-
-def phi_from_voxels(solid: np.ndarray, pitch: float = 1.0) -> np.ndarray:
-    """Signed distance of a voxel mask (positive in fluid): exact Euclidean
-    distance transform, as build_phi_from_voxel_mask_mm (sdf_tracing.py:312-340)."""
-    from scipy.ndimage import distance_transform_edt
-    s = solid.astype(bool)
-    out = distance_transform_edt(~s) * pitch
-    inn = distance_transform_edt(s) * pitch
-    phi = out
-    phi[s] = -inn[s]
-    return phi
-
-
-def ibb_from_phi_trilinear(solid: torch.Tensor, phi: torch.Tensor, pitch: float = 1.0,
-                           origin=(0.0, 0.0, 0.0)) -> IBBData:
-    """Links of `solid` with q from the trilinear level set `phi` (build_ibb_from_sdf_gpu semantics)."""
-    dev = solid.device
+def ibb_from_phi(solid: torch.Tensor, phi: torch.Tensor, pitch: float = 1.0, origin=(0.0, 0.0, 0.0),
+                 return_q: bool = False, host_division: bool = False):
+    """Links of `solid` with fractions from the trilinear level set `phi` (build_ibb_from_sdf_gpu,
+    sdf_tracing.py:208-259; the fluid cell (i,j,k) sits at origin + pitch*(i,j,k)).  `origin` holds
+    the three FP32 coordinates of the domain origin.  The grid coordinate (x - origin) / pitch is
+    rounded as torch rounds it on a CUDA device (times the FP32 reciprocal of the pitch), or as on
+    the CPU (one division) with host_division=True; the two agree for power-of-two pitches."""
+    ff, di, do, fff, fv = build_links(solid)
     nx, ny, nz = solid.shape
-    ff, di, do, fff, fv = build_links_from_mask(solid)
-    org = torch.tensor(origin, device=dev, dtype=torch.float32)
-    i = (ff // (ny * nz)).to(torch.float32)
-    j = ((ff // nz) % ny).to(torch.float32)
-    k = (ff % nz).to(torch.float32)
-    x0 = torch.stack([i, j, k], dim=1) * float(pitch) + org[None, :]
-    c = torch.tensor(C_NP, device=dev, dtype=torch.float32)
-    draw = c[di]
-    cn = torch.linalg.norm(draw, dim=1)
-    d = draw / (cn[:, None] + 1e-30)
-    L = float(pitch) * cn
-    q = q_from_sdf_trilinear(phi.to(dev, torch.float32), org, float(pitch), x0, d, L)
-    ge, w1, w2 = bfl_weights_from_q(q)
-    return IBBData(int(ff.numel()), ff, di, do, ge, w1.float(), w2.float(), fff, fv)
+    if tuple(phi.shape) != (nx, ny, nz):
+        raise ValueError("phi must have the shape of solid")
+    ph = phi.to(device=ff.device, dtype=torch.float32).contiguous()
+    n = ff.numel()
+    dev = ff.device
+    ge = torch.empty(n, dtype=torch.bool, device=dev)
+    w1 = torch.empty(n, dtype=torch.float32, device=dev)
+    w2 = torch.empty(n, dtype=torch.float32, device=dev)
+    q = torch.empty(n, dtype=torch.float32, device=dev) if return_q else None
+    err = torch.zeros(1, dtype=torch.int32, device=dev)
+    ox, oy, oz = (float(np.float32(v)) for v in origin)
+    _lib.call("fc_ibb_q_from_sdf", ptr(ph), nx, ny, nz, ox, oy, oz, float(pitch), int(bool(host_division)),
+              ptr(ff), ptr(di), n, ptr(q),
+              ptr(ge), ptr(w1), ptr(w2), ptr(err), stream_ptr())
+    _check_errword(err, "fc_ibb_q_from_sdf")
+    ibb = IBBData(int(n), ff, di, do, ge, w1, w2, fff, fv)
+    return (ibb, q) if return_q else ibb
+
+
+def ibb_from_voxels(solid: torch.Tensor, pitch: float = 1.0, origin=(0.0, 0.0, 0.0)) -> IBBData:
+    """Voxel SDF then links and fractions: build_phi_from_voxel_mask_mm followed by build_ibb_from_sdf_gpu."""
+    return ibb_from_phi(solid, signed_distance(solid, pitch), pitch, origin)
 
 
 def ibb_from_level_set(solid: torch.Tensor, levelset, n_bisect: int = 40) -> IBBData:
@@ -182,7 +150,7 @@ def ibb_from_level_set(solid: torch.Tensor, levelset, n_bisect: int = 40) -> IBB
     solid, G(cell centre) > 0 <=> solid), refined by FP64 bisection to the exact crossing."""
     dev = solid.device
     nx, ny, nz = solid.shape
-    ff, di, do, fff, fv = build_links_from_mask(solid)
+    ff, di, do, fff, fv = build_links(solid)
     i = (ff // (ny * nz)).to(torch.float64)
     j = ((ff // nz) % ny).to(torch.float64)
     k = (ff % nz).to(torch.float64)
@@ -197,7 +165,7 @@ def ibb_from_level_set(solid: torch.Tensor, levelset, n_bisect: int = 40) -> IBB
         lo = torch.where(inside, lo, mid)
     q = hi.clamp(1e-6, 1.0).to(torch.float32)
     ge, w1, w2 = bfl_weights_from_q(q)
-    return IBBData(int(ff.numel()), ff, di, do, ge, w1.float(), w2.float(), fff, fv)
+    return IBBData(int(ff.numel()), ff, di, do, ge, w1, w2, fff, fv)
 
 
 # --------------------------------------------------------------------------

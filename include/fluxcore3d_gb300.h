@@ -366,6 +366,41 @@ int fc_nn_mse_grad(const float* y, int C, const float* target, const float* mask
 int fc_nn_adam(float* w, const float* g, float* m, float* v, void* w_bf16, long long n, int kpad, int kvalid,
                float lr, float beta1, float beta2, float eps, int step, float grad_scale, void* stream);
 
+/* ---------------------------------------------------------------------------
+ * Geometry set-up for interpolated bounce-back (device side).
+ * solid: uint8 0/1 per cell, flat = i*ny*nz + j*nz + k.
+ * ------------------------------------------------------------------------- */
+/* Signed Euclidean distance of a voxel mask, positive in fluid, times pitch:
+ * replaces build_phi_from_voxel_mask_mm (pre_post/sdf_tracing.py:312-340), which
+ * runs scipy.ndimage.distance_transform_edt on the host.  phi equals
+ * float32(scipy distance * pitch) bit for bit.  Workspace: one int32 per cell.
+ * Limits: nz <= 4096, nx, ny <= 6144 (status 3 beyond). */
+long long fc_geom_edt_workspace_bytes(int nx, int ny, int nz);
+int fc_geom_signed_edt(const uint8_t* solid, int nx, int ny, int nz, double pitch, float* phi, void* workspace,
+                       long long workspace_bytes, void* stream);
+/* Boundary links of build_links_from_mask_gpu (sdf_tracing.py:20-85), same order
+ * (grouped by q = 1..18, row-major inside each q).  Two calls: count writes the
+ * total to the DEVICE word *n_links (and per-block offsets to the workspace);
+ * build fills the five arrays (n_links entries each) from the same workspace. */
+long long fc_ibb_links_workspace_bytes(int nx, int ny, int nz);
+int fc_ibb_count_links(const uint8_t* solid, int nx, int ny, int nz, void* workspace, long long workspace_bytes,
+                       long long* n_links, void* stream);
+int fc_ibb_build_links(const uint8_t* solid, int nx, int ny, int nz, const void* workspace, long long workspace_bytes,
+                       long long n_links, long long* fluid_flat, long long* dir_i, long long* dir_opp,
+                       long long* ff_flat, uint8_t* ff_valid, unsigned* err, void* stream);
+/* Bouzidi fraction per link from the trilinear level set phi (bfl_q_from_sdf +
+ * sdf_trilinear, sdf_tracing.py:89-184; 6 coarse samples, 10 bisections; the
+ * fluid cell at origin + pitch*(i,j,k)) and the weights of bfl_weights_from_q
+ * (:188-205).  true_div = 0: (x - origin)/dx as torch evaluates it on a CUDA
+ * device (times the FP32 reciprocal); 1: as on the CPU (one division).
+ * q may be NULL.  err: device word, DEV_ERR_INDEX on a bad link. */
+int fc_ibb_q_from_sdf(const float* phi, int nx, int ny, int nz, float origin_x, float origin_y, float origin_z,
+                      double dx, int true_div, const long long* fluid_flat, const long long* dir_i, long long n_links,
+                      float* q, uint8_t* q_ge_half, float* w_i, float* w_second, unsigned* err, void* stream);
+/* bfl_weights_from_q (sdf_tracing.py:188-205) alone, for fractions computed elsewhere */
+int fc_ibb_weights_from_q(const float* q, long long n_links, uint8_t* q_ge_half, float* w_i, float* w_second,
+                          void* stream);
+
 #ifdef __cplusplus
 }
 #endif

@@ -12,6 +12,9 @@ use them).  Fixtures written (all small .npz files):
                       interpolated bounce-back + reset (LBM_CHT._interp_bounce_back_from_post)
   ibb_links.npz       build_ibb_from_sdf_gpu link arrays and q on a cube and on a
                       crop of fluxcore3D_web/Heatsink.npz (phi from build_phi_from_voxel_mask_mm)
+  ibb_pitch.npz       the same with a non-unit pitch, a shifted voxel origin and a
+                      non-zero offset_ijk, and the fractions q themselves (captured
+                      from bfl_q_from_sdf); written alone by `--only ibb_pitch`
   mg_solve.npz        NLevelGeometricMGSolver (torch fallback, float64): coefficients,
                       L_apply_fine, V-cycle solve, pcg_mg and bicgstab_mg results
 """
@@ -158,5 +161,59 @@ def main(ref_root: str):
     print("golden fixtures written to", HERE)
 
 
+def ibb_pitch(ref_root: str):
+    """Voxel SDF, link arrays, weights and fractions at pitches 0.37 and 0.5 (torch CPU path)."""
+    os.environ["PYTHONDONTWRITEBYTECODE"] = "1"
+    sys.dont_write_bytecode = True
+    _stub_modules()
+    sys.path.insert(0, ref_root)
+    import torch
+    import LBM_CHT as R
+    from pre_post import sdf_tracing as SDF
+
+    captured = {}
+    orig_q = SDF.bfl_q_from_sdf
+
+    def capture_q(*a, **kw):
+        q = orig_q(*a, **kw)
+        captured["q"] = q
+        return q
+    SDF.bfl_q_from_sdf = capture_q
+    hs = np.load(os.path.join(ref_root, "fluxcore3D_web", "Heatsink.npz"))["voxel_solid"].astype(bool)
+    crop = np.zeros((30, 26, 22), bool)
+    crop[3:27, 2:24, 0:18] = hs[10:34, 20:42, 0:18]
+    I, J, K = np.indices((24, 20, 18))
+    balls = ((I - 9.3) ** 2 + (J - 8.1) ** 2 + (K - 7.7) ** 2 < 5.2 ** 2) | \
+            ((I - 17.6) ** 2 + (J - 13.2) ** 2 + (K - 10.4) ** 2 < 3.9 ** 2)
+    out = {}
+    cases = (("crop", crop, 0.37, (1.5, -2.25, 0.125), (2, 1, 3)),
+             ("balls", balls, 0.5, (-0.75, 0.3, 4.0), (0, 2, 1)))
+    for name, solid, pitch, vo, off in cases:
+        s = types.SimpleNamespace(device=torch.device("cpu"), nx=solid.shape[0], ny=solid.shape[1],
+                                  nz=solid.shape[2])
+        s.solid = torch.from_numpy(solid)
+        s.phi = SDF.build_phi_from_voxel_mask_mm(solid, pitch, device="cpu")
+        SDF.build_ibb_from_sdf_gpu(s, voxel_origin_mm=vo, pitch_mm=pitch, offset_ijk=off,
+                                   c_np=R.LBMCHT3D_Torch.c_np, opp_np=R.LBMCHT3D_Torch.opp_np)
+        d = s.ibb_data
+        out[f"{name}_solid"] = solid
+        out[f"{name}_phi"] = s.phi.numpy()
+        out[f"{name}_pitch"] = np.float64(pitch)
+        out[f"{name}_voxel_origin"] = np.array(vo, np.float64)
+        out[f"{name}_offset_ijk"] = np.array(off, np.int64)
+        out[f"{name}_q"] = captured["q"].numpy()
+        for k in ("fluid_flat", "dir_i", "dir_opp", "q_ge_half", "w_i", "w_second", "ff_flat", "ff_valid"):
+            out[f"{name}_{k}"] = getattr(d, k).numpy()
+    SDF.bfl_q_from_sdf = orig_q
+    np.savez_compressed(os.path.join(HERE, "ibb_pitch.npz"), **out)
+    print("ibb_pitch.npz written to", HERE)
+
+
 if __name__ == "__main__":
-    main(sys.argv[1] if len(sys.argv) > 1 else "/root/reference")
+    args = [a for a in sys.argv[1:] if not a.startswith("--")]
+    root = args[0] if args else "/root/reference"
+    if "--only" in sys.argv and sys.argv[sys.argv.index("--only") + 1] == "ibb_pitch":
+        ibb_pitch(root)
+    else:
+        main(root)
+        ibb_pitch(root)

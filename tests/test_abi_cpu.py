@@ -63,13 +63,21 @@ def test_face_roles_table():
     assert periodic_flags(cfg) == (False, True, False)
 
 
-def test_link_table_groups_links_by_cell():
+def oracle_ibb(solid: np.ndarray, phi: np.ndarray):
+    """IBBData on CPU tensors from the geometry oracle (host-side table tests need no GPU)."""
     from fluxcore3d_gb300 import geometry as geo
+    from oracle import geometry as og
+    r = og.ibb_from_sdf(solid, phi)
+    t = {k: torch.from_numpy(np.ascontiguousarray(v)) for k, v in r.items()}
+    return geo.IBBData(int(r["fluid_flat"].size), t["fluid_flat"], t["dir_i"], t["dir_opp"], t["q_ge_half"],
+                       t["w_i"], t["w_second"], t["ff_flat"], t["ff_valid"])
+
+
+def test_link_table_groups_links_by_cell():
     from fluxcore3d_gb300.solver.fused_lbm import build_link_table
     d = np.load(os.path.join(ROOT, "tests", "golden", "ibb_links.npz"))
     solid = torch.from_numpy(d["heatsink_solid"])
-    phi = torch.from_numpy(d["heatsink_phi"]).to(torch.float32)
-    ibb = geo.ibb_from_phi_trilinear(solid, phi)
+    ibb = oracle_ibb(d["heatsink_solid"], d["heatsink_phi"])
     nx, ny, nz = solid.shape
     t = build_link_table(ibb, solid.to(torch.uint8).reshape(-1), nx, ny, nz)
     assert t["n_links"] == ibb.n_links and int(t["counts"].sum()) == ibb.n_links
@@ -104,9 +112,9 @@ def test_link_table_groups_links_by_cell():
 def test_link_table_rejects_inconsistent_data():
     from fluxcore3d_gb300 import geometry as geo
     from fluxcore3d_gb300.solver.fused_lbm import build_link_table
+    from oracle import geometry as og
     solid = geo.cube_mask((8, 8, 8), (4, 4, 4), (2, 2, 2))
-    phi = torch.tensor(geo.phi_from_voxels(solid.numpy()), dtype=torch.float32)
-    ibb = geo.ibb_from_phi_trilinear(solid, phi)
+    ibb = oracle_ibb(solid.numpy(), og.signed_edt(solid.numpy()))
     bad = geo.IBBData(ibb.n_links, ibb.fluid_flat, ibb.dir_i, ibb.dir_i.clone(), ibb.q_ge_half, ibb.w_i,
                       ibb.w_second, ibb.ff_flat, ibb.ff_valid)
     with pytest.raises(ValueError):
@@ -118,7 +126,7 @@ def test_fused_engine_flags_and_sponge_profile_on_cpu_state():
     from fluxcore3d_gb300 import case as cases
     from fluxcore3d_gb300.solver.fused_lbm import FusedLBM
     sim = cases.channel_cube(device="cpu", nx=20, ny=8, nz=8, cube=4, cube_x=8, sponge_length=5,
-                             outlet="pressure")
+                             outlet="pressure", with_links=False)
     sim._solid_u8 = sim.solid_flow.to(torch.uint8)
     fc = FusedLBM(sim)
     fl = fc.flags.view(20, 8, 8)

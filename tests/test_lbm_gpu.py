@@ -94,8 +94,7 @@ def periodic_box(cuda, collision, storage, nx=40, ny=20, nz=32):
     cfg = CaseConfig(nx=nx, ny=ny, nz=nz, collision=collision, lbm_storage=storage, domain_walls=[],
                      outlet_bc_mode="pressure", sponge_length=6)
     solid = geo.cube_mask((nx, ny, nz), (14, ny // 2, nz // 2), (6, 6, 6), device=cuda)
-    phi = torch.tensor(geo.phi_from_voxels(solid.cpu().numpy()), dtype=torch.float32, device=cuda)
-    ibb = geo.ibb_from_phi_trilinear(solid, phi)
+    ibb = geo.ibb_from_voxels(solid)
     return LatticeCase(cfg, 0.05, 0.05 * 6 / 50, solid, stamp_walls(cfg, solid), ibb, device=cuda, seed=0)
 
 

@@ -71,26 +71,58 @@ def test_ibb_and_reset_match_reference_exactly():
 
 @pytest.mark.parametrize("name", ["cube", "heatsink"])
 def test_link_list_and_q_bit_exact(name):
-    """The link list (order included) and the Bouzidi weights equal the reference's bit for bit."""
-    from fluxcore3d_gb300 import geometry as geo
+    """The oracle's link list (order included) and Bouzidi weights equal the reference's bit for bit,
+    in both ways of rounding (x - origin) / dx (they agree at pitch 1)."""
+    from oracle import geometry as og
     d = load("ibb_links.npz")
-    solid = torch.from_numpy(d[f"{name}_solid"])
-    phi = torch.from_numpy(d[f"{name}_phi"]).to(torch.float32)
-    ibb = geo.ibb_from_phi_trilinear(solid, phi)
-    for k in ("fluid_flat", "dir_i", "dir_opp", "ff_flat"):
-        assert np.array_equal(getattr(ibb, k).numpy(), d[f"{name}_{k}"]), k
-    for k in ("q_ge_half", "ff_valid"):
-        assert np.array_equal(getattr(ibb, k).numpy(), d[f"{name}_{k}"]), k
-    assert np.array_equal(ibb.w_i.numpy().view(np.uint32), d[f"{name}_w_i"].view(np.uint32))
-    assert np.array_equal(ibb.w_second.numpy().view(np.uint32), d[f"{name}_w_second"].view(np.uint32))
+    for mode in ("reciprocal", "divide"):
+        r = og.ibb_from_sdf(d[f"{name}_solid"], d[f"{name}_phi"], 1.0, scalar_div=mode)
+        for k in ("fluid_flat", "dir_i", "dir_opp", "ff_flat", "q_ge_half", "ff_valid"):
+            assert np.array_equal(r[k], d[f"{name}_{k}"]), k
+        for k in ("w_i", "w_second"):
+            assert np.array_equal(r[k].view(np.uint32), d[f"{name}_{k}"].view(np.uint32)), k
+
+
+@pytest.mark.parametrize("name", ["crop", "balls"])
+def test_fractions_at_non_unit_pitch_match_reference(name):
+    """Pitch 0.37 / 0.5 with a shifted origin: the oracle's CPU-rounding mode reproduces the
+    reference's torch-CPU q, weights and phi exactly."""
+    from oracle import geometry as og
+    d = load("ibb_pitch.npz")
+    pitch = float(d[f"{name}_pitch"])
+    org = (d[f"{name}_voxel_origin"].astype(np.float32)
+           - np.float32(pitch) * d[f"{name}_offset_ijk"].astype(np.float32))
+    phi = og.signed_edt(d[f"{name}_solid"], pitch)
+    assert np.array_equal(phi.view(np.uint32), d[f"{name}_phi"].view(np.uint32))
+    r = og.ibb_from_sdf(d[f"{name}_solid"], d[f"{name}_phi"], pitch, org, scalar_div="divide")
+    for k in ("fluid_flat", "dir_i", "dir_opp", "ff_flat", "q_ge_half", "ff_valid"):
+        assert np.array_equal(r[k], d[f"{name}_{k}"]), k
+    for k in ("q", "w_i", "w_second"):
+        assert np.array_equal(r[k].view(np.uint32), d[f"{name}_{k}"].view(np.uint32)), k
 
 
 def test_phi_from_voxels_matches_reference():
-    from fluxcore3d_gb300 import geometry as geo
+    from oracle import geometry as og
     d = load("ibb_links.npz")
     for name in ("cube", "heatsink"):
-        phi = geo.phi_from_voxels(d[f"{name}_solid"]).astype(np.float32)
-        assert np.array_equal(phi, d[f"{name}_phi"])
+        phi = og.signed_edt(d[f"{name}_solid"])
+        assert np.array_equal(phi.view(np.uint32), d[f"{name}_phi"].view(np.uint32))
+
+
+def test_signed_edt_oracle_matches_scipy():
+    """The separable restatement against scipy.ndimage.distance_transform_edt itself (the routine
+    build_phi_from_voxel_mask_mm calls), on seeded masks, two pitches and both degenerate masks."""
+    edt = pytest.importorskip("scipy.ndimage").distance_transform_edt
+    from oracle import geometry as og
+    rng = np.random.default_rng(5)
+    masks = [rng.random(tuple(rng.integers(1, 26, size=3))) < rng.uniform(0.005, 0.7) for _ in range(10)]
+    masks += [np.zeros((4, 5, 6), bool), np.ones((4, 5, 6), bool), np.zeros((1, 1, 7), bool)]
+    for s in masks:
+        for pitch in (1.0, 0.37):
+            ref = edt(~s) * pitch
+            ref[s] = -(edt(s) * pitch)[s]
+            got = og.signed_edt(s, pitch)
+            assert np.array_equal(got.view(np.uint32), ref.astype(np.float32).view(np.uint32)), (s.shape, pitch)
 
 
 def _golden_mg():
