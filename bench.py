@@ -7,7 +7,10 @@ populations with FP32 collision, velocity inlet u = 0.08, pressure outlet,
 walls at +-z, periodic in y, outlet sponge of 40 cells.  One step = one fused
 pass + the inlet/outlet plane kernels.  The same case with FP32 populations
 is timed as the plain-precision comparison, and the thermal MG-Krylov solve
-time to a 1e-8 FP64 residual is reported beside it when available.
+time to a 1e-8 FP64 residual is reported beside it when available.  The
+geometry set-up (voxel SDF, boundary links, Bouzidi fractions) is timed on the
+384x192x192 gyroid and the 768x384x384 pin + gyroid hybrid, with scipy's host
+distance transform on the gyroid as its CPU baseline.
 
 The populations (2 x 159 MB at FP16) exceed the 129 MB L2, so no L2 flush is
 inserted between steps.
@@ -252,6 +255,7 @@ def main():
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-thermal", action="store_true")
+    ap.add_argument("--no-geometry", action="store_true", help="skip the voxel SDF / link builder timings")
     ap.add_argument("--storages", default="fp16,fp32", help="population storages to time (first = headline)")
     ap.add_argument("--profile", action="store_true",
                     help="short run for ncu captures: headline storage only, no e2e / thermal / CPU legs")
@@ -259,7 +263,7 @@ def main():
     args.warmup = max(3, args.warmup)
     if args.profile:
         args.storages = args.storages.split(",")[0]
-        args.no_e2e = args.no_cpu = args.no_thermal = True
+        args.no_e2e = args.no_cpu = args.no_thermal = args.no_geometry = True
     if args.impl == "reference":
         run_reference(args)
         return
@@ -368,6 +372,9 @@ def main():
                 line["thermal"] = th
         except ImportError:
             pass
+    if not args.no_geometry:
+        from fluxcore3d_gb300 import geometry_bench
+        line["geometry"] = geometry_bench.run(dev, cpu_baseline=(rank == 0 and not args.no_cpu))
     if rank == 0 and not args.no_cpu:
         line["cpu_baseline"] = cpu_baseline_sample(args)
     if rank == 0:

@@ -34,9 +34,10 @@
 //
 // Link order.  A link is a fluid cell x whose neighbour x + c_q (q = 1..18,
 // no wrap) is solid.  The list is grouped by q and row-major inside each q.
-// Blocks of 1024 cells count their links per q, one block scans the counts
-// (q-major, so the offsets follow the list order), and the write pass places
-// every link at its block offset plus its rank inside the block (warp ballots).
+// Blocks of 1024 cells count their links per q, a two-level scan turns the
+// counts (q-major, so the offsets follow the list order) into offsets, and the
+// write pass places every link at its block offset plus its rank inside the
+// block (warp ballots).
 //
 // Fractions.  FP32, every operation rounded on its own as the reference's
 // elementwise tensor operations are (no contraction).  sdf_trilinear's
@@ -58,7 +59,7 @@ constexpr int ROW_WARPS = 8;
 constexpr int EDT_MAX_NZ = 4096;      // z pass: 128 chunks of ballots per warp in shared memory
 constexpr int LINE_THREADS = 256;
 constexpr int LINE_SMEM = 96 * 1024;  // y / x pass staging budget per block
-constexpr int EDT_MAX_LINE = LINE_SMEM / 16;  // KW = 4 at the longest line
+constexpr int EDT_MAX_LINE = 4096;    // y / x lines: KW = 4 columns of 4096 cells fit the budget
 
 // ---------------------------------------------------------------------------
 // pass z: 1-D squared distance to the nearest cell of the other kind in the row
@@ -119,14 +120,37 @@ k_edt_rows(const uint8_t* __restrict__ solid, int* __restrict__ g, long long nro
 
 // ---------------------------------------------------------------------------
 // passes y and x: min over the line of g(y) + (x - y)^2, in place; the x pass
-// (FINAL) writes the signed FP32 distance instead
+// (FINAL) writes the signed FP32 distance instead.
+//
+// A cell first checks the cells within EDT_NEAR of it one by one, then walks
+// outward block by block (EDT_BS cells): a block whose minimum value plus the
+// squared distance to its nearest cell is not below the best so far is
+// skipped whole, and the walk stops once that squared distance alone reaches
+// it.  Both bounds are exact, so the result is the exact minimum; in open
+// regions, where the values vary slowly along the line, a cell far from the
+// wall costs a few block tests instead of a scan out to its distance.
 // ---------------------------------------------------------------------------
+constexpr int EDT_BS = 16;
+constexpr int EDT_NEAR = 4;
+constexpr int SQRT_TAB = 1 << 18;   // FP32 phi magnitudes of d^2 < 2^18 (distances below 512 cells)
+
+__device__ __forceinline__ int g_of(unsigned w, unsigned kind) {
+    return (w >> 31) != kind ? 0 : (int)(w & 0x7fffffffu);
+}
+
+__host__ __device__ constexpr long long line_smem_bytes(int L, int kw) {
+    return 4LL * kw * ((long long)L + 2LL * ((L + EDT_BS - 1) / EDT_BS));
+}
+
 template <int KW, bool FINAL>
 __global__ void __launch_bounds__(LINE_THREADS)
-k_edt_lines(const uint8_t* __restrict__ solid, int* __restrict__ g, float* __restrict__ phi, int L,
-            long long lstride, long long ostride, int nz, double pitch) {
+k_edt_lines(const uint8_t* __restrict__ solid, int* __restrict__ g, float* __restrict__ phi,
+            const float* __restrict__ tab, int L, long long lstride, long long ostride, int nz, double pitch) {
     extern __shared__ unsigned edt_sh[];
     constexpr int RP = LINE_THREADS / KW;
+    const int NB = (L + EDT_BS - 1) / EDT_BS;
+    unsigned* sv = edt_sh;                          // [y][column]: value | kind << 31
+    int* bm = (int*)(edt_sh + (size_t)L * KW);      // [kind][block][column]: block minima
     const int c = threadIdx.x % KW, xr = threadIdx.x / KW;
     const int k = blockIdx.x * KW + c;
     const bool col = k < nz;
@@ -134,39 +158,85 @@ k_edt_lines(const uint8_t* __restrict__ solid, int* __restrict__ g, float* __res
     if (col) {
         for (int x = xr; x < L; x += RP) {
             const long long cell = base + x * lstride;
-            edt_sh[x * KW + c] = (unsigned)g[cell] | (solid[cell] ? 0x80000000u : 0u);
+            sv[x * KW + c] = (unsigned)g[cell] | (solid[cell] ? 0x80000000u : 0u);
         }
+    }
+    __syncthreads();
+    for (int p = threadIdx.x; p < NB * KW; p += LINE_THREADS) {
+        const int b = p / KW, cc = p % KW;
+        int m0 = EDT_INF, m1 = EDT_INF;
+        if ((int)blockIdx.x * KW + cc < nz) {
+            const int y1 = min(L, (b + 1) * EDT_BS);
+            for (int y = b * EDT_BS; y < y1; ++y) {
+                const unsigned w = sv[y * KW + cc];
+                const int v = (int)(w & 0x7fffffffu);
+                if (w >> 31) {
+                    m0 = 0;
+                    m1 = min(m1, v);
+                } else {
+                    m1 = 0;
+                    m0 = min(m0, v);
+                }
+            }
+        }
+        bm[b * KW + cc] = m0;
+        bm[(NB + b) * KW + cc] = m1;
     }
     __syncthreads();
     if (!col) return;
     for (int x = xr; x < L; x += RP) {
-        const unsigned own = edt_sh[x * KW + c];
+        const unsigned own = sv[x * KW + c];
         const unsigned kind = own >> 31;
+        const int* bmk = bm + (size_t)kind * NB * KW + c;
         int best = (int)(own & 0x7fffffffu);
-        for (int r = 1; r * r < best; ++r) {
-            const bool lo = x - r >= 0, hi = x + r < L;
-            if (!lo && !hi) break;
+        for (int r = 1; r <= EDT_NEAR; ++r) {
             const int rr = r * r;
-            if (lo) {
-                const unsigned w = edt_sh[(x - r) * KW + c];
-                best = min(best, ((w >> 31) != kind ? 0 : (int)(w & 0x7fffffffu)) + rr);
+            if (rr >= best) break;
+            if (x - r >= 0) best = min(best, g_of(sv[(x - r) * KW + c], kind) + rr);
+            if (x + r < L) best = min(best, g_of(sv[(x + r) * KW + c], kind) + rr);
+        }
+        for (int yl = x - EDT_NEAR - 1; yl >= 0;) {
+            const int d = x - yl;
+            if (d * d >= best) break;
+            const int y0 = (yl / EDT_BS) * EDT_BS;
+            if (bmk[(yl / EDT_BS) * KW] + d * d < best) {
+                for (int y = yl; y >= y0; --y) {
+                    const int dd = (x - y) * (x - y);
+                    if (dd >= best) break;
+                    best = min(best, g_of(sv[y * KW + c], kind) + dd);
+                }
             }
-            if (hi) {
-                const unsigned w = edt_sh[(x + r) * KW + c];
-                best = min(best, ((w >> 31) != kind ? 0 : (int)(w & 0x7fffffffu)) + rr);
+            yl = y0 - 1;
+        }
+        for (int yr = x + EDT_NEAR + 1; yr < L;) {
+            const int d = yr - x;
+            if (d * d >= best) break;
+            const int y1 = min(L, (yr / EDT_BS + 1) * EDT_BS);
+            if (bmk[(yr / EDT_BS) * KW] + d * d < best) {
+                for (int y = yr; y < y1; ++y) {
+                    const int dd = (y - x) * (y - x);
+                    if (dd >= best) break;
+                    best = min(best, g_of(sv[y * KW + c], kind) + dd);
+                }
             }
+            yr = y1;
         }
         const long long cell = base + x * lstride;
         if constexpr (FINAL) {
             // x pass: x is i, blockIdx.y is j
-            double d2;
-            if (best < EDT_INF) {
-                d2 = (double)best;
+            float v;
+            if (best < SQRT_TAB) {
+                v = __ldg(tab + best);
             } else {
-                const double a = (double)(x + 1), b = (double)blockIdx.y, e = (double)k;
-                d2 = __dadd_rn(__dadd_rn(__dmul_rn(a, a), __dmul_rn(b, b)), __dmul_rn(e, e));
+                double d2;
+                if (best < EDT_INF) {
+                    d2 = (double)best;
+                } else {
+                    const double a = (double)(x + 1), b = (double)blockIdx.y, e = (double)k;
+                    d2 = __dadd_rn(__dadd_rn(__dmul_rn(a, a), __dmul_rn(b, b)), __dmul_rn(e, e));
+                }
+                v = __double2float_rn(__dmul_rn(__dsqrt_rn(d2), pitch));
             }
-            const float v = __double2float_rn(__dmul_rn(__dsqrt_rn(d2), pitch));
             phi[cell] = kind ? -v : v;
         } else {
             g[cell] = best;
@@ -174,17 +244,23 @@ k_edt_lines(const uint8_t* __restrict__ solid, int* __restrict__ g, float* __res
     }
 }
 
+// tab[d2] = float(double(sqrt(d2)) * pitch): numpy's FP64 sqrt and product, then the cast
+__global__ void __launch_bounds__(256) k_edt_sqrt_table(float* __restrict__ tab, double pitch) {
+    const int d2 = blockIdx.x * blockDim.x + threadIdx.x;
+    if (d2 < SQRT_TAB) tab[d2] = __double2float_rn(__dmul_rn(__dsqrt_rn((double)d2), pitch));
+}
+
 template <bool FINAL>
-int launch_lines(const uint8_t* solid, int* g, float* phi, int L, long long lstride, long long ostride, int n_outer,
-                 int nz, double pitch, cudaStream_t st) {
+int launch_lines(const uint8_t* solid, int* g, float* phi, const float* tab, int L, long long lstride,
+                 long long ostride, int n_outer, int nz, double pitch, cudaStream_t st) {
     int kw = 32;
-    while (kw > 4 && (long long)L * kw * 4 > LINE_SMEM) kw >>= 1;
-    if ((long long)L * kw * 4 > LINE_SMEM) return FC_ERR_UNSUPPORTED;
-    const size_t smem = (size_t)L * kw * 4;
+    while (kw > 4 && line_smem_bytes(L, kw) > LINE_SMEM) kw >>= 1;
+    if (line_smem_bytes(L, kw) > LINE_SMEM) return FC_ERR_UNSUPPORTED;
+    const size_t smem = (size_t)line_smem_bytes(L, kw);
     const dim3 grid((unsigned)((nz + kw - 1) / kw), (unsigned)n_outer);
     auto run = [&](auto kern) {
         if (smem > 48 * 1024) cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-        kern<<<grid, LINE_THREADS, smem, st>>>(solid, g, phi, L, lstride, ostride, nz, pitch);
+        kern<<<grid, LINE_THREADS, smem, st>>>(solid, g, phi, tab, L, lstride, ostride, nz, pitch);
     };
     switch (kw) {
         case 32: run(k_edt_lines<32, FINAL>); break;
@@ -246,45 +322,77 @@ k_links_count(const uint8_t* __restrict__ solid, Dims d, unsigned* __restrict__ 
         counts[(long long)(threadIdx.x - 1) * nblocks + blockIdx.x] = cnt[threadIdx.x];
 }
 
-// exclusive scan of the M per-(q, block) counts by one block; off[M] = total
-__global__ void __launch_bounds__(1024)
-k_links_scan(const unsigned* __restrict__ counts, long long* __restrict__ off, long long M,
-             long long* __restrict__ total) {
-    __shared__ long long wsum[32];
-    const long long seg = (M + 1023) / 1024;
-    const long long b = (long long)threadIdx.x * seg, e = min(M, b + seg);
-    long long s = 0;
-    for (long long x = b; x < e; ++x) s += counts[x];
+// Exclusive scan of the M per-(q, block) counts, in two levels: every block of
+// 1024 threads scans a chunk of SCAN_CHUNK counts in place (local offsets), one
+// block scans the chunk sums.  The offset of entry e is then
+// counts[e] + chunk_off[e / SCAN_CHUNK].
+constexpr int SCAN_THREADS = 1024, SCAN_PER_THREAD = 4, SCAN_CHUNK = SCAN_THREADS * SCAN_PER_THREAD;
+
+template <class T>
+__device__ __forceinline__ T block_exclusive_scan(T v, T* wsum, T& total) {
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-    long long v = s;
+    T x = v;
     for (int o = 1; o < 32; o <<= 1) {
-        const long long y = __shfl_up_sync(FULL, v, o);
-        if (lane >= o) v += y;
+        const T y = __shfl_up_sync(FULL, x, o);
+        if (lane >= o) x += y;
     }
-    if (lane == 31) wsum[warp] = v;
+    if (lane == 31) wsum[warp] = x;
     __syncthreads();
     if (warp == 0) {
-        long long w = wsum[lane];
+        T w = wsum[lane];
         for (int o = 1; o < 32; o <<= 1) {
-            const long long y = __shfl_up_sync(FULL, w, o);
+            const T y = __shfl_up_sync(FULL, w, o);
             if (lane >= o) w += y;
         }
         wsum[lane] = w;
     }
     __syncthreads();
-    long long run = v - s + (warp ? wsum[warp - 1] : 0);
-    for (long long x = b; x < e; ++x) {
-        off[x] = run;
-        run += counts[x];
+    total = wsum[31];
+    const T r = x - v + (warp ? wsum[warp - 1] : T(0));
+    __syncthreads();
+    return r;
+}
+
+__global__ void __launch_bounds__(SCAN_THREADS)
+k_scan_chunks(unsigned* __restrict__ counts, long long M, long long* __restrict__ chunk_sum) {
+    __shared__ unsigned wsum[32];
+    const long long e0 = (long long)blockIdx.x * SCAN_CHUNK + (long long)threadIdx.x * SCAN_PER_THREAD;
+    unsigned v[SCAN_PER_THREAD];
+    unsigned s = 0;
+#pragma unroll
+    for (int t = 0; t < SCAN_PER_THREAD; ++t) {
+        v[t] = e0 + t < M ? counts[e0 + t] : 0u;
+        s += v[t];
     }
-    if (threadIdx.x == 1023) {
-        off[M] = run;
-        if (total) *total = run;
+    unsigned total;
+    unsigned run = block_exclusive_scan<unsigned>(s, wsum, total);
+#pragma unroll
+    for (int t = 0; t < SCAN_PER_THREAD; ++t) {
+        if (e0 + t < M) counts[e0 + t] = run;
+        run += v[t];
     }
+    if (threadIdx.x == 0) chunk_sum[blockIdx.x] = total;
+}
+
+__global__ void __launch_bounds__(SCAN_THREADS)
+k_scan_totals(const long long* __restrict__ chunk_sum, long long nch, long long* __restrict__ chunk_off,
+              long long* __restrict__ grand) {
+    __shared__ long long wsum[32];
+    long long carry = 0;
+    for (long long b = 0; b < nch; b += SCAN_THREADS) {
+        const long long e = b + threadIdx.x;
+        const long long v = e < nch ? chunk_sum[e] : 0;
+        long long total;
+        const long long r = block_exclusive_scan<long long>(v, wsum, total);
+        if (e < nch) chunk_off[e] = carry + r;
+        carry += total;
+    }
+    if (threadIdx.x == 0 && grand) *grand = carry;
 }
 
 __global__ void __launch_bounds__(LB_THREADS)
-k_links_write(const uint8_t* __restrict__ solid, Dims d, const long long* __restrict__ off, int nblocks,
+k_links_write(const uint8_t* __restrict__ solid, Dims d, const unsigned* __restrict__ loc,
+              const long long* __restrict__ chunk_off, int nblocks,
               long long n_links, long long* __restrict__ fluid_flat, long long* __restrict__ dir_i,
               long long* __restrict__ dir_opp, long long* __restrict__ ff_flat, uint8_t* __restrict__ ff_valid,
               unsigned* __restrict__ err) {
@@ -292,8 +400,10 @@ k_links_write(const uint8_t* __restrict__ solid, Dims d, const long long* __rest
     __shared__ long long base[19];
     __shared__ unsigned wc[19][NW];
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-    if (threadIdx.x >= 1 && threadIdx.x < 19)
-        base[threadIdx.x] = off[(long long)(threadIdx.x - 1) * nblocks + blockIdx.x];
+    if (threadIdx.x >= 1 && threadIdx.x < 19) {
+        const long long e = (long long)(threadIdx.x - 1) * nblocks + blockIdx.x;
+        base[threadIdx.x] = (long long)loc[e] + chunk_off[e / SCAN_CHUNK];
+    }
     const unsigned lt = (1u << lane) - 1u;
     for (int r = 0; r < LB_ROUNDS; ++r) {
         const long long cell = (long long)blockIdx.x * LB_CELLS + r * LB_THREADS + threadIdx.x;
@@ -493,7 +603,7 @@ extern "C" {
 
 long long fc_geom_edt_workspace_bytes(int nx, int ny, int nz) {
     if (!dims_ok(nx, ny, nz)) return -1;
-    return (long long)nx * ny * nz * (long long)sizeof(int);
+    return (long long)nx * ny * nz * (long long)sizeof(int) + (long long)SQRT_TAB * (long long)sizeof(float);
 }
 
 int fc_geom_signed_edt(const uint8_t* solid, int nx, int ny, int nz, double pitch, float* phi, void* workspace,
@@ -512,17 +622,22 @@ int fc_geom_signed_edt(const uint8_t* solid, int nx, int ny, int nz, double pitc
         solid, g, nrows, nz, nch);
     int rc = launch_status();
     if (rc) return rc;
+    float* tab = (float*)(g + (long long)nx * ny * nz);
+    k_edt_sqrt_table<<<SQRT_TAB / 256, 256, 0, st>>>(tab, pitch);
+    rc = launch_status();
+    if (rc) return rc;
     // y pass: lines along j (stride nz), one block row per i
-    rc = launch_lines<false>(solid, g, nullptr, ny, nz, (long long)ny * nz, nx, nz, pitch, st);
+    rc = launch_lines<false>(solid, g, nullptr, nullptr, ny, nz, (long long)ny * nz, nx, nz, pitch, st);
     if (rc) return rc;
     // x pass: lines along i (stride ny*nz), one block row per j; writes phi
-    return launch_lines<true>(solid, g, phi, nx, (long long)ny * nz, nz, ny, nz, pitch, st);
+    return launch_lines<true>(solid, g, phi, tab, nx, (long long)ny * nz, nz, ny, nz, pitch, st);
 }
 
 long long fc_ibb_links_workspace_bytes(int nx, int ny, int nz) {
     if (!dims_ok(nx, ny, nz)) return -1;
     const long long M = 18 * link_blocks(nx, ny, nz);
-    return align8(M * 4) + (M + 1) * 8 + 8;
+    const long long nch = (M + SCAN_CHUNK - 1) / SCAN_CHUNK;
+    return align8(M * 4) + 2 * nch * 8;
 }
 
 int fc_ibb_count_links(const uint8_t* solid, int nx, int ny, int nz, void* workspace, long long workspace_bytes,
@@ -532,14 +647,19 @@ int fc_ibb_count_links(const uint8_t* solid, int nx, int ny, int nz, void* works
     const long long nb = link_blocks(nx, ny, nz);
     if (nb > 0x7fffffffLL) return FC_ERR_UNSUPPORTED;
     const long long M = 18 * nb;
+    const long long nch = (M + SCAN_CHUNK - 1) / SCAN_CHUNK;
     unsigned* counts = (unsigned*)workspace;
-    long long* off = (long long*)((char*)workspace + align8(M * 4));
+    long long* chunk_sum = (long long*)((char*)workspace + align8(M * 4));
+    long long* chunk_off = chunk_sum + nch;
     Dims d{nx, ny, nz, (long long)ny * nz, (long long)nx * ny * nz};
     cudaStream_t st = (cudaStream_t)stream;
     k_links_count<<<(unsigned)nb, LB_THREADS, 0, st>>>(solid, d, counts, (int)nb);
     int rc = launch_status();
     if (rc) return rc;
-    k_links_scan<<<1, 1024, 0, st>>>(counts, off, M, n_links);
+    k_scan_chunks<<<(unsigned)nch, SCAN_THREADS, 0, st>>>(counts, M, chunk_sum);
+    rc = launch_status();
+    if (rc) return rc;
+    k_scan_totals<<<1, SCAN_THREADS, 0, st>>>(chunk_sum, nch, chunk_off, n_links);
     return launch_status();
 }
 
@@ -553,10 +673,13 @@ int fc_ibb_build_links(const uint8_t* solid, int nx, int ny, int nz, const void*
     const long long nb = link_blocks(nx, ny, nz);
     if (nb > 0x7fffffffLL) return FC_ERR_UNSUPPORTED;
     const long long M = 18 * nb;
-    const long long* off = (const long long*)((const char*)workspace + align8(M * 4));
+    const long long nch = (M + SCAN_CHUNK - 1) / SCAN_CHUNK;
+    const unsigned* loc = (const unsigned*)workspace;
+    const long long* chunk_off = (const long long*)((const char*)workspace + align8(M * 4)) + nch;
     Dims d{nx, ny, nz, (long long)ny * nz, (long long)nx * ny * nz};
-    k_links_write<<<(unsigned)nb, LB_THREADS, 0, (cudaStream_t)stream>>>(solid, d, off, (int)nb, n_links, fluid_flat,
-                                                                          dir_i, dir_opp, ff_flat, ff_valid, err);
+    k_links_write<<<(unsigned)nb, LB_THREADS, 0, (cudaStream_t)stream>>>(solid, d, loc, chunk_off, (int)nb, n_links,
+                                                                          fluid_flat, dir_i, dir_opp, ff_flat,
+                                                                          ff_valid, err);
     return launch_status();
 }
 

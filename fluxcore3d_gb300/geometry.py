@@ -225,6 +225,23 @@ def pin_fin_levelset(nx, ny, nz, n_pins=(16, 8), radius=3.5, height=80, base=8, 
     return G
 
 
+def pin_gyroid_levelset(nx, ny, nz, n_pins=(48, 24), radius=5.0, height=80, base=8, L=64.0, t=0.3, seed=2,
+                        device="cpu"):
+    """Pin-fin / TPMS hybrid: the base plate and jittered cylinders of pin_fin_levelset with gyroid
+    (level t, period L) infill between the pins, from the plate top to the pin tops."""
+    pins = pin_fin_levelset(nx, ny, nz, n_pins=n_pins, radius=radius, height=height, base=base, seed=seed,
+                            device=device)
+    gyr = gyroid_levelset(L, t)
+    top = float(base + height) - 0.5
+    zb = float(base) - 0.5
+
+    def G(x):
+        Z = x[..., 2]
+        band = torch.minimum(torch.minimum(gyr(x), top - Z), Z - zb)
+        return torch.maximum(pins(x), band)
+    return G
+
+
 def gyroid_levelset(L=48.0, t=0.3):
     w = 2 * math.pi / L
 

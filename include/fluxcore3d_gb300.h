@@ -374,7 +374,7 @@ int fc_nn_adam(float* w, const float* g, float* m, float* v, void* w_bf16, long 
  * replaces build_phi_from_voxel_mask_mm (pre_post/sdf_tracing.py:312-340), which
  * runs scipy.ndimage.distance_transform_edt on the host.  phi equals
  * float32(scipy distance * pitch) bit for bit.  Workspace: one int32 per cell.
- * Limits: nz <= 4096, nx, ny <= 6144 (status 3 beyond). */
+ * Limits: nx, ny, nz <= 4096 (status 3 beyond). */
 long long fc_geom_edt_workspace_bytes(int nx, int ny, int nz);
 int fc_geom_signed_edt(const uint8_t* solid, int nx, int ny, int nz, double pitch, float* phi, void* workspace,
                        long long workspace_bytes, void* stream);
