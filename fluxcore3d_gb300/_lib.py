@@ -163,6 +163,10 @@ SIGNATURES: dict[str, tuple] = {
     "fc_ibb_build_links": (i32, [vp, i32, i32, i32, vp, i64, i64, vp, vp, vp, vp, vp, vp, vp]),
     "fc_ibb_q_from_sdf": (i32, [vp, i32, i32, i32, f32, f32, f32, f64, i32, vp, vp, i64, vp, vp, vp, vp, vp, vp]),
     "fc_ibb_weights_from_q": (i32, [vp, i64, vp, vp, vp, vp]),
+    # snapshot / checkpoint I/O
+    "fc_snapshot_pack": (i32, [vp, vp, vp, vp, vp, i64, i32, vp, vp]),
+    "fc_columns_gather": (i32, [vp, i32, i64, vp, i64, vp, vp, vp]),
+    "fc_columns_scatter": (i32, [vp, i32, i64, vp, i64, vp, vp, vp]),
 }
 
 STATUS_TEXT = {1: "bad argument", 2: "CUDA launch failure", 3: "unsupported combination",

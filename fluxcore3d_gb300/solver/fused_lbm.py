@@ -476,5 +476,39 @@ class FusedLBM:
     def check_device_error(self) -> int:
         return int(self.dev_err.item())
 
+    # -- checkpoint support ----------------------------------------------------
+    def plane_cells(self) -> torch.Tensor:
+        """Cells whose sim.f populations carry state from one step to the next: the deferred
+        inlet/outlet plane cells and the cells exporting their post-stream values to them."""
+        return torch.nonzero((self.flags & (CF_DEFER | CF_WRITE_S)) != 0).flatten().to(torch.int64)
+
+    def export_state(self) -> dict:
+        """Device tensors that determine every later step exactly (no copies are made)."""
+        if not self.primed:
+            self._prime()
+        return {"k": self.k, "P": self.P[self.cur], "M0": torch.stack(self.M[0]), "M1": torch.stack(self.M[1])}
+
+    def import_state(self, k: int, P: torch.Tensor, M0: torch.Tensor, M1: torch.Tensor):
+        """Resume from export_state's tensors: the next step continues the saved run bit for bit.
+        sim.f must already hold the saved plane-cell populations."""
+        sim, a = self.sim, self.args
+        if P.shape != self.P[0].shape or P.dtype != self.P[0].dtype:
+            raise ValueError("checkpoint populations do not match this engine's storage or size")
+        self._prime()                       # static arguments, pinned solid cells in both buffers
+        self.P[0].copy_(P)
+        for b, Mb in enumerate((M0, M1)):
+            for q in range(4):
+                self.M[b][q].copy_(Mb[q])
+        self.cur = 0
+        self.k = int(k)
+        self._graphs.clear()
+        self._eager_steps = 0
+        if self.concurrent_gather:          # link values of the next step come from P_k
+            a.pop_in = ptr(self.P[0])
+            a.f32 = ptr(sim.f)
+            _lib.call("fc_lbm_link_gather", a, None, 0, 0, stream_ptr())
+        if self.k > 0:
+            self._expose(self.M[(self.k - 1) % 2])
+
 
 _W = torch.tensor([0.33333333] + [0.05555556] * 6 + [0.02777778] * 12, dtype=torch.float32)

@@ -401,6 +401,22 @@ int fc_ibb_q_from_sdf(const float* phi, int nx, int ny, int nz, float origin_x, 
 int fc_ibb_weights_from_q(const float* q, long long n_links, uint8_t* q_ge_half, float* w_i, float* w_second,
                           void* stream);
 
+/* ---------------------------------------------------------------------------
+ * Snapshot and checkpoint I/O (device side)
+ * ------------------------------------------------------------------------- */
+/* One frame of _save_snapshot (LBM_CHT.py:2749-2769) in one pass: the fields
+ * selected by `fields` (bit 0 u, 1 v, 2 w, 3 speed = sqrt(u*u + v*v + w*w) rounded
+ * as torch rounds it, 4 rho, 5 T) written to out in that order, n floats each. */
+int fc_snapshot_pack(const float* rho, const float* u, const float* v, const float* w, const float* T, long long n,
+                     int fields, float* out, void* stream);
+/* out[r*m + j] = src[r*ld + idx[j]] (no reference counterpart: the populations
+ * of the inlet/outlet plane cells a checkpoint carries); scatter is the inverse.
+ * err: device word, DEV_ERR_INDEX for an index outside [0, ld). */
+int fc_columns_gather(const float* src, int rows, long long ld, const long long* idx, long long m, float* out,
+                      unsigned* err, void* stream);
+int fc_columns_scatter(float* dst, int rows, long long ld, const long long* idx, long long m, const float* cols,
+                       unsigned* err, void* stream);
+
 #ifdef __cplusplus
 }
 #endif
