@@ -10,7 +10,8 @@ is timed as the plain-precision comparison, and the thermal MG-Krylov solve
 time to a 1e-8 FP64 residual is reported beside it when available.  The
 geometry set-up (voxel SDF, boundary links, Bouzidi fractions) is timed on the
 384x192x192 gyroid and the 768x384x384 pin + gyroid hybrid, with scipy's host
-distance transform on the gyroid as its CPU baseline.
+distance transform on the gyroid as its CPU baseline; snapshot and checkpoint
+I/O is timed on the pin-fin case.
 
 The populations (2 x 159 MB at FP16) exceed the 129 MB L2, so no L2 flush is
 inserted between steps.
@@ -126,6 +127,15 @@ def dist_env():
     return ws, rank, local
 
 
+def setup_device():
+    """Where the CPU legs build their inputs: the geometry set-up (links, fractions) runs on the GPU;
+    only the timed oracle steps run on the host cores."""
+    import torch
+    if not torch.cuda.is_available():
+        raise RuntimeError("the CPU baseline builds its case with the device geometry kernels: a GPU is required")
+    return "cuda"
+
+
 def make_case(device, storage, args):
     from fluxcore3d_gb300 import case as cases
     sim = cases.pin_fin(device=device, collision=args.collision, storage=storage, nx=args.nx, ny=args.ny,
@@ -184,15 +194,16 @@ def run_reference(args):
     import numpy as np
     import torch
     from oracle.lbm import OracleLBM
-    sim = make_case("cpu", "fp32", args)
+    sim = make_case(setup_device(), "fp32", args)
     d = sim.ibb_data
-    links = {k: getattr(d, k).numpy() for k in
+    links = {k: getattr(d, k).cpu().numpy() for k in
              ("fluid_flat", "dir_i", "dir_opp", "w_i", "w_second", "q_ge_half", "ff_flat", "ff_valid")}
     cores = os.cpu_count() or 1
     os.environ.setdefault("OMP_NUM_THREADS", str(cores))
-    orc = OracleLBM(sim.nx, sim.ny, sim.nz, sim.f.numpy(), sim.solid_flow.numpy(), collision=args.collision,
-                    omega=float(sim.omega_plus), S=sim._mrt_S.numpy() if hasattr(sim, "_mrt_S") else None,
-                    sigma=sim._sponge_sigma.numpy() if sim.cfg.sponge_length > 0 else None, links=links,
+    orc = OracleLBM(sim.nx, sim.ny, sim.nz, sim.f.cpu().numpy(), sim.solid_flow.cpu().numpy(),
+                    collision=args.collision, omega=float(sim.omega_plus),
+                    S=sim._mrt_S.cpu().numpy() if hasattr(sim, "_mrt_S") else None,
+                    sigma=sim._sponge_sigma.cpu().numpy() if sim.cfg.sponge_length > 0 else None, links=links,
                     domain_walls=sim.cfg.domain_walls, u_in_lat=sim.u_in_lat, real="f32")
     orc.step(args.warmup)
     t = time.perf_counter()
@@ -217,13 +228,14 @@ def cpu_baseline_sample(args):
     """A bounded sample of the same workload on the host cores (oracle, FP32)."""
     import numpy as np
     from oracle.lbm import OracleLBM
-    sim = make_case("cpu", "fp32", args)
+    sim = make_case(setup_device(), "fp32", args)
     d = sim.ibb_data
-    links = {k: getattr(d, k).numpy() for k in
+    links = {k: getattr(d, k).cpu().numpy() for k in
              ("fluid_flat", "dir_i", "dir_opp", "w_i", "w_second", "q_ge_half", "ff_flat", "ff_valid")}
-    orc = OracleLBM(sim.nx, sim.ny, sim.nz, sim.f.numpy(), sim.solid_flow.numpy(), collision=args.collision,
-                    omega=float(sim.omega_plus), S=sim._mrt_S.numpy() if hasattr(sim, "_mrt_S") else None,
-                    sigma=sim._sponge_sigma.numpy() if sim.cfg.sponge_length > 0 else None, links=links,
+    orc = OracleLBM(sim.nx, sim.ny, sim.nz, sim.f.cpu().numpy(), sim.solid_flow.cpu().numpy(),
+                    collision=args.collision, omega=float(sim.omega_plus),
+                    S=sim._mrt_S.cpu().numpy() if hasattr(sim, "_mrt_S") else None,
+                    sigma=sim._sponge_sigma.cpu().numpy() if sim.cfg.sponge_length > 0 else None, links=links,
                     domain_walls=sim.cfg.domain_walls, u_in_lat=sim.u_in_lat, real="f32")
     orc.step(1)
     n = args.cpu_steps
@@ -256,6 +268,7 @@ def main():
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-thermal", action="store_true")
     ap.add_argument("--no-geometry", action="store_true", help="skip the voxel SDF / link builder timings")
+    ap.add_argument("--no-io", action="store_true", help="skip the snapshot / checkpoint timings")
     ap.add_argument("--storages", default="fp16,fp32", help="population storages to time (first = headline)")
     ap.add_argument("--profile", action="store_true",
                     help="short run for ncu captures: headline storage only, no e2e / thermal / CPU legs")
@@ -263,7 +276,7 @@ def main():
     args.warmup = max(3, args.warmup)
     if args.profile:
         args.storages = args.storages.split(",")[0]
-        args.no_e2e = args.no_cpu = args.no_thermal = args.no_geometry = True
+        args.no_e2e = args.no_cpu = args.no_thermal = args.no_geometry = args.no_io = True
     if args.impl == "reference":
         run_reference(args)
         return
@@ -375,6 +388,9 @@ def main():
     if not args.no_geometry:
         from fluxcore3d_gb300 import geometry_bench
         line["geometry"] = geometry_bench.run(dev, cpu_baseline=(rank == 0 and not args.no_cpu))
+    if not args.no_io:
+        from fluxcore3d_gb300 import io_bench
+        line["io"] = io_bench.run(dev)
     if rank == 0 and not args.no_cpu:
         line["cpu_baseline"] = cpu_baseline_sample(args)
     if rank == 0:
