@@ -167,6 +167,12 @@ SIGNATURES: dict[str, tuple] = {
     "fc_snapshot_pack": (i32, [vp, vp, vp, vp, vp, i64, i32, vp, vp]),
     "fc_columns_gather": (i32, [vp, i32, i64, vp, i64, vp, vp, vp]),
     "fc_columns_scatter": (i32, [vp, i32, i64, vp, i64, vp, vp, vp]),
+    # STL voxelization, body stamping
+    "fc_vox_prepared_floats": (i64, [i64]),
+    "fc_vox_prepare_triangles": (i32, [vp, i64, f32, vp, vp]),
+    "fc_vox_parity_z": (i32, [vp, i64, i32, i32, i32, f64, f64, f64, f64, f64, f64, vp, vp]),
+    "fc_geom_stamp_body": (i32, [vp, i32, i32, i32, i32, i32, i32, i32, i32, i32, vp, vp, vp, f32, f32, vp, vp,
+                                 vp]),
 }
 
 STATUS_TEXT = {1: "bad argument", 2: "CUDA launch failure", 3: "unsupported combination",

@@ -417,6 +417,30 @@ int fc_columns_gather(const float* src, int rows, long long ld, const long long*
 int fc_columns_scatter(float* dst, int rows, long long ld, const long long* idx, long long m, const float* cols,
                        unsigned* err, void* stream);
 
+/* ---------------------------------------------------------------------------
+ * STL voxelization and body stamping (device side)
+ * ------------------------------------------------------------------------- */
+/* gpu_voxelize_mesh (pre_post/gpu_voxelizer.py:81-170), in two calls.
+ * prepare: tri = n_tri x 3 vertices x (x,y,z) FP32; prep = fc_vox_prepared_floats(n_tri)
+ * floats (16-byte aligned); z0 = FP32 grid origin z.
+ * parity: +z rays from (origin_x + i*pitch + perturb_x, origin_y + j*pitch + perturb_y)
+ * (FP64, then FP32), cell centres origin_z + (k + 0.5)*pitch; voxels[(i*ny + j)*nz + k]
+ * = 1 where an odd number of triangles is pierced below the centre.  nz <= 4096. */
+long long fc_vox_prepared_floats(long long n_tri);
+int fc_vox_prepare_triangles(const float* tri, long long n_tri, float z0, float* prep, void* stream);
+int fc_vox_parity_z(const float* prep, long long n_tri, int nx, int ny, int nz, double origin_x, double origin_y,
+                    double origin_z, double pitch, double perturb_x, double perturb_y, uint8_t* voxels,
+                    void* stream);
+/* LBMCHT3D_Torch.add_solid_body's stamp (LBM_CHT.py:959-1023): voxels (gx,gy,gz) placed
+ * with voxel (0,0,0) at domain cell (i0,j0,k0), clamped to the domain; solid |= voxel,
+ * k_field / rho_cp_field (may be NULL) set where the voxel is solid; body_mask (may be
+ * NULL, caller-zeroed) = cells this body added (SolidAssembly.stamp's per-body mask,
+ * pre_post/solid_assembly.py:164-184); *stamped (device, may be NULL) += solid voxels
+ * placed. */
+int fc_geom_stamp_body(const uint8_t* vox, int gx, int gy, int gz, int i0, int j0, int k0, int nx, int ny, int nz,
+                       uint8_t* solid, float* k_field, float* rho_cp_field, float k_val, float rho_cp_val,
+                       uint8_t* body_mask, unsigned long long* stamped, void* stream);
+
 #ifdef __cplusplus
 }
 #endif

@@ -15,6 +15,10 @@ use them).  Fixtures written (all small .npz files):
   ibb_pitch.npz       the same with a non-unit pitch, a shifted voxel origin and a
                       non-zero offset_ijk, and the fractions q themselves (captured
                       from bfl_q_from_sdf); written alone by `--only ibb_pitch`
+  voxels.npz          gpu_voxelize_mesh (pre_post/gpu_voxelizer.py, torch CPU path)
+                      on three closed meshes built by fluxcore3d_gb300.pre_post.stl
+                      (box, icosphere, finned heat sink): triangles, grid and the
+                      packed voxel grids; written alone by `--only voxels`
   mg_solve.npz        NLevelGeometricMGSolver (torch fallback, float64): coefficients,
                       L_apply_fine, V-cycle solve, pcg_mg and bicgstab_mg results
 """
@@ -209,11 +213,43 @@ def ibb_pitch(ref_root: str):
     print("ibb_pitch.npz written to", HERE)
 
 
+def voxels(ref_root: str):
+    """Reference voxel grids of three procedural meshes (triangles stored, so no mesh file travels)."""
+    os.environ["PYTHONDONTWRITEBYTECODE"] = "1"
+    sys.dont_write_bytecode = True
+    _stub_modules()
+    sys.path.insert(0, ref_root)
+    sys.path.insert(0, os.path.dirname(os.path.dirname(HERE)))
+    from pre_post import gpu_voxelizer as GV
+    from fluxcore3d_gb300.pre_post import stl
+    meshes = {
+        "box": (stl.box_mesh((0.0, 0.0, 0.0), (10.0, 20.0, 5.0)), 0.5),
+        "sphere": (stl.icosphere_mesh(5.0, 3, center=(1.3, -0.7, 2.1)), 0.45),
+        "finsink": (stl.fin_heatsink_mesh(base=(24.0, 16.0, 2.0), n_fins=6, fin_t=1.2, fin_h=9.0,
+                                          origin=(-3.1, 2.2, 0.4)), 0.37),
+    }
+    out = {}
+    for name, (mesh, pitch) in meshes.items():
+        v, o = GV.gpu_voxelize_mesh(mesh, pitch, device="cpu")
+        out[f"{name}_tri"] = mesh.triangles.astype(np.float32)
+        out[f"{name}_pitch"] = np.float64(pitch)
+        out[f"{name}_origin"] = o
+        out[f"{name}_dims"] = np.array(v.shape, np.int64)
+        out[f"{name}_bits"] = np.packbits(v.astype(bool).ravel())
+        out[f"{name}_count"] = np.int64(v.sum())
+    np.savez_compressed(os.path.join(HERE, "voxels.npz"), **out)
+    print("voxels.npz written to", HERE)
+
+
 if __name__ == "__main__":
     args = [a for a in sys.argv[1:] if not a.startswith("--")]
     root = args[0] if args else "/root/reference"
-    if "--only" in sys.argv and sys.argv[sys.argv.index("--only") + 1] == "ibb_pitch":
+    only = sys.argv[sys.argv.index("--only") + 1] if "--only" in sys.argv else None
+    if only == "ibb_pitch":
         ibb_pitch(root)
+    elif only == "voxels":
+        voxels(root)
     else:
         main(root)
         ibb_pitch(root)
+        voxels(root)

@@ -153,3 +153,35 @@ def test_mg_apply_and_solves_match_reference():
     xb, ib = omg.bicgstab(mg, d["b"], None, tol=1e-9, max_it=8)
     assert ib["it"] == int(d["bicgstab_it"])
     assert np.linalg.norm(xb - d["bicgstab_x"]) / np.linalg.norm(d["bicgstab_x"]) < 1e-5
+
+
+def test_voxelizer_oracle_matches_reference_grids():
+    """The restated ray-parity voxelizer reproduces gpu_voxelize_mesh's grids, origins and sizes."""
+    from oracle import voxelizer as ov
+    d = load("voxels.npz")
+    for name in ("box", "sphere", "finsink"):
+        tri, pitch = d[f"{name}_tri"], float(d[f"{name}_pitch"])
+        origin, dims = ov.grid(tri.reshape(-1, 3), pitch)
+        assert dims == tuple(int(x) for x in d[f"{name}_dims"])
+        assert np.array_equal(origin.astype(np.float64), d[f"{name}_origin"])
+        want = np.unpackbits(d[f"{name}_bits"])[:np.prod(dims)].reshape(dims)
+        assert np.array_equal(ov.voxelize(tri, origin, dims, pitch), want), name
+
+
+def test_stl_round_trip_and_grid_helper(tmp_path):
+    from fluxcore3d_gb300.pre_post import gpu_voxelizer as gv
+    from fluxcore3d_gb300.pre_post import stl
+    from oracle import voxelizer as ov
+    m = stl.fin_heatsink_mesh()
+    p = str(tmp_path / "sink.stl")
+    stl.write_stl(p, m)
+    r = stl.read_stl(p)
+    assert np.array_equal(r.triangles, m.triangles.astype(np.float32))
+    ascii_path = str(tmp_path / "tri.stl")
+    with open(ascii_path, "w") as fh:
+        fh.write("solid t\nfacet normal 0 0 1\nouter loop\nvertex 0 0 0\nvertex 1 0 0\nvertex 0 1 0\n"
+                 "endloop\nendfacet\nendsolid t\n")
+    assert stl.read_stl(ascii_path).triangles.shape == (1, 3, 3)
+    o1, *d1 = gv.voxel_grid(m.vertices.astype(np.float32), 0.37)
+    o2, d2 = ov.grid(m.vertices, 0.37)
+    assert tuple(d1) == d2 and np.array_equal(o1, o2)
