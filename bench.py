@@ -387,7 +387,14 @@ def main():
             pass
     if not args.no_geometry:
         from fluxcore3d_gb300 import geometry_bench
-        line["geometry"] = geometry_bench.run(dev, cpu_baseline=(rank == 0 and not args.no_cpu))
+        cpu_vox = None
+        if rank == 0 and not args.no_cpu:
+            from oracle import voxelizer as ov
+
+            def cpu_vox(tri, origin, dims, pitch, ids):
+                return ov.voxelize(tri, origin, dims, pitch, ray_ids=ids)
+        line["geometry"] = geometry_bench.run(dev, cpu_baseline=(rank == 0 and not args.no_cpu),
+                                              cpu_voxelize=cpu_vox)
     if not args.no_io:
         from fluxcore3d_gb300 import io_bench
         line["io"] = io_bench.run(dev)

@@ -12,7 +12,8 @@
 //    once by the prepare kernel.  A block stages 512 prepared triangles at a
 //    time in shared memory; each thread walks them for its ray and, for every
 //    hit, toggles a bit at the first cell centre above the hit (binary search in
-//    the centre table); a prefix XOR over the bits gives the parity column.
+//    the centre table); a prefix XOR over the bits gives the parity column, and
+//    the block writes its columns (one contiguous byte range) with 16-byte stores.
 //    Every triangle is tested against every ray, as in the reference: a bounding
 //    box cull would be exact only with an error bound that sliver triangles
 //    (tiny determinant, huge reciprocal) do not have.
@@ -102,21 +103,46 @@ k_vox_parity(const float4* __restrict__ prep, long long T, int nx, int ny, int n
             if (lo < nz) bits[(lo >> 5) * VOX_RAYS + threadIdx.x] ^= 1u << (lo & 31);
         }
     }
-    if (!active) return;
-    uint8_t* col = out + r * nz;
-    unsigned carry = 0u;
-    for (int w = 0; w < nw; ++w) {
-        unsigned p = bits[w * VOX_RAYS + threadIdx.x];
-        p ^= p << 1;
-        p ^= p << 2;
-        p ^= p << 4;
-        p ^= p << 8;
-        p ^= p << 16;
-        if (carry) p = ~p;
-        carry = p >> 31;
-        const int k0 = w * 32;
-        const int kn = min(32, nz - k0);
-        for (int b = 0; b < kn; ++b) col[k0 + b] = (uint8_t)((p >> b) & 1u);
+    // flip bits -> parity bits (prefix XOR along the column), in place
+    if (active) {
+        unsigned carry = 0u;
+        for (int w = 0; w < nw; ++w) {
+            unsigned p = bits[w * VOX_RAYS + threadIdx.x];
+            p ^= p << 1;
+            p ^= p << 2;
+            p ^= p << 4;
+            p ^= p << 8;
+            p ^= p << 16;
+            if (carry) p = ~p;
+            carry = p >> 31;
+            bits[w * VOX_RAYS + threadIdx.x] = p;
+        }
+    }
+    __syncthreads();
+    // the block's columns are one contiguous byte range: write it with 16-byte stores
+    const long long r0 = (long long)blockIdx.x * VOX_RAYS;
+    const long long nr = min((long long)VOX_RAYS, nrays - r0);
+    const long long nbytes = nr * nz;
+    uint8_t* dst = out + r0 * nz;       // r0 * nz is a multiple of 128
+    const long long nchunk = nbytes >> 4;
+    for (long long c = threadIdx.x; c < nchunk; c += VOX_RAYS) {
+        const long long b0 = c << 4;
+        int ray = (int)(b0 / nz), k = (int)(b0 - (long long)ray * nz);
+        unsigned wd[4] = {0u, 0u, 0u, 0u};
+#pragma unroll
+        for (int i = 0; i < 16; ++i) {
+            const unsigned bit = (bits[(k >> 5) * VOX_RAYS + ray] >> (k & 31)) & 1u;
+            wd[i >> 2] |= bit << ((i & 3) * 8);
+            if (++k == nz) {
+                k = 0;
+                ++ray;
+            }
+        }
+        *reinterpret_cast<uint4*>(dst + b0) = make_uint4(wd[0], wd[1], wd[2], wd[3]);
+    }
+    for (long long b = (nchunk << 4) + threadIdx.x; b < nbytes; b += VOX_RAYS) {
+        const int ray = (int)(b / nz), k = (int)(b - (long long)ray * nz);
+        dst[b] = (uint8_t)((bits[(k >> 5) * VOX_RAYS + ray] >> (k & 31)) & 1u);
     }
 }
 
