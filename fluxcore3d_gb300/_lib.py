@@ -173,6 +173,9 @@ SIGNATURES: dict[str, tuple] = {
     "fc_vox_parity_z": (i32, [vp, i64, i32, i32, i32, f64, f64, f64, f64, f64, f64, vp, vp]),
     "fc_geom_stamp_body": (i32, [vp, i32, i32, i32, i32, i32, i32, i32, i32, i32, vp, vp, vp, f32, f32, vp, vp,
                                  vp]),
+    # passive tracer
+    "fc_tracer_step": (i32, [vp, vp, vp, vp, vp, vp, i32, i32, i32, f32, vp]),
+    "fc_tracer_inject": (i32, [vp, vp, i64, vp]),
 }
 
 STATUS_TEXT = {1: "bad argument", 2: "CUDA launch failure", 3: "unsupported combination",

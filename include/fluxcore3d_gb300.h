@@ -441,6 +441,17 @@ int fc_geom_stamp_body(const uint8_t* vox, int gx, int gy, int gz, int i0, int j
                        uint8_t* solid, float* k_field, float* rho_cp_field, float k_val, float rho_cp_val,
                        uint8_t* body_mask, unsigned long long* stamped, void* stream);
 
+/* ---------------------------------------------------------------------------
+ * Passive tracer (device side)
+ * ------------------------------------------------------------------------- */
+/* One TracerField.step (pre_post/tracer_patch.py:55-82): upwind advection of phi by
+ * (u, v, w) with periodic neighbours, clamp to [0, 1], times dissipation, 0 where
+ * solid_flow != 0; phi_out must not alias phi.  nx, ny <= 65535. */
+int fc_tracer_step(const float* phi, float* phi_out, const float* u, const float* v, const float* w,
+                   const uint8_t* solid_flow, int nx, int ny, int nz, float dissipation, void* stream);
+/* TracerField.inject (:51-53): phi = 1 where mask != 0 */
+int fc_tracer_inject(float* phi, const uint8_t* mask, long long n, void* stream);
+
 #ifdef __cplusplus
 }
 #endif

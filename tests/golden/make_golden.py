@@ -15,6 +15,9 @@ use them).  Fixtures written (all small .npz files):
   ibb_pitch.npz       the same with a non-unit pitch, a shifted voxel origin and a
                       non-zero offset_ijk, and the fractions q themselves (captured
                       from bfl_q_from_sdf); written alone by `--only ibb_pitch`
+  tracer.npz          TracerField (pre_post/tracer_patch.py) on seeded velocity and
+                      solid fields: the field after 1 and after 25 steps with
+                      injections; written alone by `--only tracer`
   voxels.npz          gpu_voxelize_mesh (pre_post/gpu_voxelizer.py, torch CPU path)
                       on three closed meshes built by fluxcore3d_gb300.pre_post.stl
                       (box, icosphere, finned heat sink): triangles, grid and the
@@ -241,6 +244,39 @@ def voxels(ref_root: str):
     print("voxels.npz written to", HERE)
 
 
+def tracer(ref_root: str):
+    os.environ["PYTHONDONTWRITEBYTECODE"] = "1"
+    sys.dont_write_bytecode = True
+    _stub_modules()
+    sys.path.insert(0, ref_root)
+    import torch
+    from pre_post import tracer_patch as TP
+    g = torch.Generator().manual_seed(21)
+    nx, ny, nz = 20, 14, 11
+    solid = torch.rand((nx, ny, nz), generator=g) < 0.15
+    out = {"solid_flow": solid.numpy()}
+    sim = types.SimpleNamespace(nx=nx, ny=ny, nz=nz, device=torch.device("cpu"), solid_flow=solid)
+    vel = []
+    for s in range(5):
+        f = [(torch.rand((nx, ny, nz), generator=g) - 0.45) * 0.3 for _ in range(3)]
+        vel.append(f)
+        for a, name in enumerate(("u", "v", "w")):
+            out[f"{name}{s}"] = f[a].numpy()
+    tr = TP.TracerField(sim, flow_dir="+X", inject_depth=3, dissipation=0.9995)
+    tr.inject()
+    out["inlet"] = tr._inlet.numpy()
+    for it in range(25):
+        sim.u, sim.v, sim.wv = vel[it // 5]
+        if it % 7 == 6:
+            tr.inject()
+        tr.step()
+        if it == 0:
+            out["field1"] = tr.field.numpy().copy()
+    out["field25"] = tr.field.numpy().copy()
+    np.savez_compressed(os.path.join(HERE, "tracer.npz"), **out)
+    print("tracer.npz written to", HERE)
+
+
 if __name__ == "__main__":
     args = [a for a in sys.argv[1:] if not a.startswith("--")]
     root = args[0] if args else "/root/reference"
@@ -249,7 +285,10 @@ if __name__ == "__main__":
         ibb_pitch(root)
     elif only == "voxels":
         voxels(root)
+    elif only == "tracer":
+        tracer(root)
     else:
         main(root)
         ibb_pitch(root)
         voxels(root)
+        tracer(root)

@@ -185,3 +185,17 @@ def test_stl_round_trip_and_grid_helper(tmp_path):
     o1, *d1 = gv.voxel_grid(m.vertices.astype(np.float32), 0.37)
     o2, d2 = ov.grid(m.vertices, 0.37)
     assert tuple(d1) == d2 and np.array_equal(o1, o2)
+
+
+def test_tracer_oracle_matches_reference():
+    from oracle import tracer as ot
+    d = load("tracer.npz")
+    phi = ot.inject(np.zeros(d["solid_flow"].shape, np.float32), d["inlet"])
+    for it in range(25):
+        s = it // 5
+        if it % 7 == 6:
+            phi = ot.inject(phi, d["inlet"])
+        phi = ot.step(phi, d[f"u{s}"], d[f"v{s}"], d[f"w{s}"], d["solid_flow"])
+        if it == 0:
+            assert np.array_equal(phi.view(np.uint32), d["field1"].view(np.uint32))
+    assert np.array_equal(phi.view(np.uint32), d["field25"].view(np.uint32))
