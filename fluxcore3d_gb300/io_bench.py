@@ -9,6 +9,8 @@
   six blocking .cpu() copies into numpy frames) on the same fields.
 * steps_with_snapshots: the time loop with a snapshot every 10 steps against the
   same loop without snapshots (device time per step).
+* tracer: device time of one fc_tracer_step (21 B/cell algorithmic) and of the
+  reference's tensor sequence for TracerField.step on the same fields.
 * checkpoint: save_checkpoint / load_checkpoint wall time and size, file in /tmp.
 """
 from __future__ import annotations
@@ -108,6 +110,41 @@ def run(dev, steps=200):
     snap = statistics.median([loop(True) for _ in range(3)])
     out["step_ms_without_snapshots"] = round(base, 5)
     out["step_ms_with_snapshot_every_10"] = round(snap, 5)
+    # passive tracer: one fused kernel per step against the reference's tensor sequence
+    from .pre_post.tracer_patch import TracerField
+    sim._fc.macro_stride = 1
+    sim.step(do_thermal=False)
+    tr = TracerField(sim, flow_dir="+X", inject_depth=6)
+    tr.inject()
+
+    def ref_step(phi):
+        u, v, w = sim.u, sim.v, sim.wv
+        ax = torch.where(u >= 0, phi - torch.roll(phi, 1, 0), torch.roll(phi, -1, 0) - phi)
+        ay = torch.where(v >= 0, phi - torch.roll(phi, 1, 1), torch.roll(phi, -1, 1) - phi)
+        az = torch.where(w >= 0, phi - torch.roll(phi, 1, 2), torch.roll(phi, -1, 2) - phi)
+        phi = torch.clamp(phi - (u * ax + v * ay + w * az), 0.0, 1.0)
+        phi *= 0.9995
+        phi[~tr.fluid] = 0.0
+        return phi
+
+    def timed(fn, n=50):
+        for _ in range(5):
+            fn()
+        torch.cuda.synchronize()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record()
+        for _ in range(n):
+            fn()
+        e1.record()
+        torch.cuda.synchronize()
+        return e0.elapsed_time(e1) / n
+    out["tracer_step_ms"] = round(timed(tr.step), 4)
+    out["tracer_achieved_gbs"] = round(21 * n / (out["tracer_step_ms"] / 1e3) / 1e9, 1)
+    holder = [tr.field.clone()]
+
+    def ref():
+        holder[0] = ref_step(holder[0])
+    out["tracer_reference_sequence_ms"] = round(timed(ref), 4)
     # checkpoint
     path = os.path.join(tmp, "ck.npz")
     ts, tl = [], []
