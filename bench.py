@@ -11,7 +11,9 @@ time to a 1e-8 FP64 residual is reported beside it when available.  The
 geometry set-up (voxel SDF, boundary links, Bouzidi fractions) is timed on the
 384x192x192 gyroid and the 768x384x384 pin + gyroid hybrid, with scipy's host
 distance transform on the gyroid as its CPU baseline; snapshot and checkpoint
-I/O is timed on the pin-fin case.
+I/O is timed on the pin-fin case.  The accuracy report compares FP16 and FP32
+storage runs with an FP64 run of the plain method (velocity, temperature, wall
+heat flow, Nusselt number) on a reduced pin fin.
 
 The populations (2 x 159 MB at FP16) exceed the 129 MB L2, so no L2 flush is
 inserted between steps.
@@ -31,6 +33,7 @@ import threading
 import time
 
 ROOT = os.path.dirname(os.path.abspath(__file__))
+RESULT_OUT = sys.stdout
 sys.path.insert(0, ROOT)
 
 METRIC = "D3Q19 CHT MLUPS + thermal ms to 1e-8 residual, mixed/learned vs plain, 1 GB300"
@@ -221,7 +224,108 @@ def run_reference(args):
                          "sample": f"{args.steps} full steps of the 256x128x128 workload (oracle C, OpenMP)"},
         "e2e": {"value": round(v, 3), "unit": "MLUPS", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
-    print(json.dumps(line), flush=True)
+    print(json.dumps(line), file=RESULT_OUT, flush=True)
+
+
+ACC_CASE = dict(nx=128, ny=64, nz=64, n_pins=(8, 4), height=40, base=4, sponge_length=20)
+
+
+def _velocity_from_f(f, shape):
+    """(u, v, w) in FP64 from populations [19, N] (post-stream state)."""
+    import numpy as np
+    from fluxcore3d_gb300.geometry import C_NP
+    f = np.asarray(f, dtype=np.float64).reshape(19, -1)
+    rho = f.sum(0)
+    return [(C_NP[:, a].astype(np.float64) @ f / rho).reshape(shape) for a in range(3)]
+
+
+def _wall_heat(T, k, solid, D):
+    """Heat flow through the solid/fluid faces (harmonic-mean conductance times the temperature
+    jump, summed over the 6-neighbour faces), the face count, and the Nusselt number
+    Nu = (Q / A) * D / (k_f * mean wall temperature rise over the inlet)."""
+    import numpy as np
+    q, n, tw = 0.0, 0, 0.0
+    for ax in range(3):
+        a = [slice(None)] * 3
+        b = [slice(None)] * 3
+        a[ax] = slice(0, -1)
+        b[ax] = slice(1, None)
+        sa, sb = solid[tuple(a)], solid[tuple(b)]
+        face = sa != sb
+        ka, kb = k[tuple(a)], k[tuple(b)]
+        kh = 2.0 * ka * kb / (ka + kb)
+        Ta, Tb = T[tuple(a)], T[tuple(b)]
+        ts = np.where(sa, Ta, Tb)
+        tf = np.where(sa, Tb, Ta)
+        q += float((kh * (ts - tf))[face].sum())
+        n += int(face.sum())
+        tw += float((0.5 * (ts + tf))[face].sum())
+    k_f = float(k[~solid].min())
+    tw /= max(n, 1)
+    return q, n, (q / n) * D / (k_f * tw)
+
+
+def accuracy_run(args, dev):
+    """FP16- and FP32-storage GPU runs against an FP64 run of the plain method (the CPU oracle in
+    double precision) from the same initial state on a reduced pin fin (128x64x64, 8x4 pins of
+    radius 3.5 and height 40, MRT, analytic link fractions): velocity error after `accuracy_steps`
+    steps, then the thermal system of each velocity field solved to a 1e-10 FP64 residual, and the
+    temperature, wall heat flow and Nusselt number of each against the FP64 run's."""
+    import numpy as np
+    import torch
+    from fluxcore3d_gb300 import case as cases
+    from fluxcore3d_gb300 import thermal_bench
+    from fluxcore3d_gb300.solver import mg_pcg
+    from fluxcore3d_gb300.solver.lbm_cuda_ext import LBMCUDAUpgrade
+    from oracle.lbm import OracleLBM
+    steps = args.accuracy_steps
+    ref = cases.pin_fin(device=dev, storage="fp32", **ACC_CASE)
+    shape = (ref.nx, ref.ny, ref.nz)
+    d = ref.ibb_data
+    links = {k: getattr(d, k).cpu().numpy() for k in
+             ("fluid_flat", "dir_i", "dir_opp", "w_i", "w_second", "q_ge_half", "ff_flat", "ff_valid")}
+    t = time.perf_counter()
+    orc = OracleLBM(ref.nx, ref.ny, ref.nz, ref.f.cpu().numpy(), ref.solid_flow.cpu().numpy(), collision="mrt",
+                    omega=float(ref.omega_plus), S=ref._mrt_S.cpu().numpy(), sigma=ref._sponge_sigma.cpu().numpy(),
+                    links=links, domain_walls=ref.cfg.domain_walls, u_in_lat=ref.u_in_lat, real="f64")
+    orc.step(steps)
+    fp64_s = time.perf_counter() - t
+    vel = {"fp64": _velocity_from_f(orc.f, shape)}
+    for storage in ("fp32", "fp16"):
+        sim = cases.pin_fin(device=dev, storage=storage, **ACC_CASE)
+        sim.cfg.macro_stride = 1
+        LBMCUDAUpgrade.patch(sim)
+        for _ in range(steps):
+            sim.step(do_thermal=False)
+        sim.sync_f()
+        vel[storage] = _velocity_from_f(sim.f.cpu().numpy(), shape)
+    fluid = ~ref.solid_flow.cpu().numpy()
+    U64 = np.stack(vel["fp64"])[:, fluid]
+    out = {"workload": "pin fin 128x64x64 (8x4 pins r=3.5, h=40), MRT + Bouzidi IBB, u=0.08, Re=200",
+           "steps": steps, "fp64_run": f"CPU oracle in FP64, {os.cpu_count()} threads, {fp64_s:.1f} s",
+           "velocity_rel_l2": {}, "temperature_rel_max": {}, "temperature_rel_l2": {}, "wall_heat_flow_rel": {},
+           "nusselt": {}, "nusselt_rel": {}}
+    k = ref.k.cpu().numpy().astype(np.float64)
+    solid = ref.solid.cpu().numpy()
+    T, heat = {}, {}
+    for name in ("fp64", "fp32", "fp16"):
+        if name != "fp64":
+            U = np.stack(vel[name])[:, fluid]
+            out["velocity_rel_l2"][name] = float(np.linalg.norm(U - U64) / np.linalg.norm(U64))
+        u, v, w = (torch.from_numpy(a.astype(np.float32)).to(dev) for a in vel[name])
+        mg, b = thermal_bench.thermal_system(ref, u, v, w)
+        x, info = mg_pcg.bicgstab_mg_f64(mg, b, tol=1e-10, max_it=400)
+        T[name] = x.reshape(shape).cpu().numpy().astype(np.float64)
+        heat[name] = _wall_heat(T[name], k, solid, 2 * 3.5)
+        out["nusselt"][name] = round(heat[name][2], 6)
+    for name in ("fp32", "fp16"):
+        dT = T[name] - T["fp64"]
+        out["temperature_rel_max"][name] = float(np.abs(dT).max() / np.abs(T["fp64"]).max())
+        out["temperature_rel_l2"][name] = float(np.linalg.norm(dT) / np.linalg.norm(T["fp64"]))
+        out["wall_heat_flow_rel"][name] = float(abs(heat[name][0] - heat["fp64"][0]) / abs(heat["fp64"][0]))
+        out["nusselt_rel"][name] = float(abs(heat[name][2] - heat["fp64"][2]) / abs(heat["fp64"][2]))
+    out["wall_faces"] = heat["fp64"][1]
+    return out
 
 
 def cpu_baseline_sample(args):
@@ -269,6 +373,8 @@ def main():
     ap.add_argument("--no-thermal", action="store_true")
     ap.add_argument("--no-geometry", action="store_true", help="skip the voxel SDF / link builder timings")
     ap.add_argument("--no-io", action="store_true", help="skip the snapshot / checkpoint timings")
+    ap.add_argument("--no-accuracy", action="store_true", help="skip the FP16/FP32 vs FP64 accuracy report")
+    ap.add_argument("--accuracy-steps", type=int, default=600)
     ap.add_argument("--storages", default="fp16,fp32", help="population storages to time (first = headline)")
     ap.add_argument("--profile", action="store_true",
                     help="short run for ncu captures: headline storage only, no e2e / thermal / CPU legs")
@@ -276,7 +382,7 @@ def main():
     args.warmup = max(3, args.warmup)
     if args.profile:
         args.storages = args.storages.split(",")[0]
-        args.no_e2e = args.no_cpu = args.no_thermal = args.no_geometry = args.no_io = True
+        args.no_e2e = args.no_cpu = args.no_thermal = args.no_geometry = args.no_io = args.no_accuracy = True
     if args.impl == "reference":
         run_reference(args)
         return
@@ -398,10 +504,12 @@ def main():
     if not args.no_io:
         from fluxcore3d_gb300 import io_bench
         line["io"] = io_bench.run(dev)
+    if rank == 0 and not args.no_accuracy:
+        line["accuracy"] = accuracy_run(args, dev)
     if rank == 0 and not args.no_cpu:
         line["cpu_baseline"] = cpu_baseline_sample(args)
     if rank == 0:
-        print(json.dumps(line), flush=True)
+        print(json.dumps(line), file=RESULT_OUT, flush=True)
     if ws > 1:
         torch.distributed.destroy_process_group()
 
@@ -441,4 +549,7 @@ def thermal_run(args, dev):
 
 
 if __name__ == "__main__":
+    # stdout carries only the result line; progress lines of the solvers go to stderr
+    RESULT_OUT = sys.stdout
+    sys.stdout = sys.stderr
     main()

@@ -16,15 +16,13 @@ import time
 import torch
 
 
-def build_system(dev, nx=256, ny=128, nz=128, lbm_steps=3000, dt=1000.0, flux=5e-3, k_ratio=200.0):
-    from . import case as cases
-    from .solver.lbm_cuda_ext import LBMCUDAUpgrade
+def thermal_system(sim, u, v, w, dt=1000.0, flux=5e-3):
+    """A = I + dt L for the velocity (u, v, w) on sim's geometry (zero velocity in flow-solid
+    cells), inlet plane (x = 0) Dirichlet, a uniform heat flux into the bottom layer of the solid;
+    returns (mg, b)."""
     from .solver.nlevel_mg_cuda import NLevelGeometricMGSolver
-    sim = cases.pin_fin(device=dev, nx=nx, ny=ny, nz=nz, storage="fp16", k_ratio=k_ratio)
-    LBMCUDAUpgrade.patch(sim)
-    for _ in range(lbm_steps):
-        sim.step(do_thermal=False)
-    torch.cuda.synchronize()
+    dev = sim.device
+    nx, ny, nz = sim.nx, sim.ny, sim.nz
     mask = torch.ones((nx, ny, nz), dtype=torch.bool, device=dev)
     mask[0] = False                                   # inlet plane (flow +X) is Dirichlet
     src = torch.zeros((nx, ny, nz), device=dev)
@@ -32,12 +30,24 @@ def build_system(dev, nx=256, ny=128, nz=128, lbm_steps=3000, dt=1000.0, flux=5e
     src[~sim.solid] = 0.0
     b = (mask.float() * dt * src).contiguous()
     mg = NLevelGeometricMGSolver(dev, torch.float32, 0, +1, 1.0, omega=0.6, n_pre=2, n_post=2, n_coarse=20)
-    u = sim.u.clone()
-    v = sim.v.clone()
-    w = sim.wv.clone()
+    vel = []
     for t in (u, v, w):
+        t = t.to(device=dev, dtype=torch.float32).clone()
         t[sim.solid_flow] = 0.0
-    mg.build_if_needed(sim.k, sim.rho_cp, u, v, w, mask, dt)
+        vel.append(t)
+    mg.build_if_needed(sim.k, sim.rho_cp, *vel, mask, dt)
+    return mg, b
+
+
+def build_system(dev, nx=256, ny=128, nz=128, lbm_steps=3000, dt=1000.0, flux=5e-3, k_ratio=200.0):
+    from . import case as cases
+    from .solver.lbm_cuda_ext import LBMCUDAUpgrade
+    sim = cases.pin_fin(device=dev, nx=nx, ny=ny, nz=nz, storage="fp16", k_ratio=k_ratio)
+    LBMCUDAUpgrade.patch(sim)
+    for _ in range(lbm_steps):
+        sim.step(do_thermal=False)
+    torch.cuda.synchronize()
+    mg, b = thermal_system(sim, sim.u, sim.v, sim.wv, dt, flux)
     return sim, mg, b
 
 
