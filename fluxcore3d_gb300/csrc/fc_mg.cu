@@ -13,6 +13,8 @@
 // the first sweep from a zero guess (x = invD b), residual + 2x mean
 // restriction, trilinear prolongation + damped correction + mask, and the
 // operator / hierarchy builders.  Reductions are FP64 with a fixed tree order.
+#include <initializer_list>
+
 #include "fc_common.cuh"
 #include "../../include/fluxcore3d_gb300.h"
 
@@ -59,12 +61,32 @@ struct Coef {
     const float *aE, *aW, *aN, *aS, *aU, *aD, *diagL;
 };
 
-template <typename T>
-__device__ __forceinline__ T apply_L(const Coef& a, const T* __restrict__ x, const Nb7& n, T xc) {
-    return (T)__ldg(a.diagL + n.c) * xc - (T)__ldg(a.aE + n.c) * x[n.e] - (T)__ldg(a.aW + n.c) * x[n.w] -
-           (T)__ldg(a.aN + n.c) * x[n.n] - (T)__ldg(a.aS + n.c) * x[n.s] - (T)__ldg(a.aU + n.c) * x[n.u] -
-           (T)__ldg(a.aD + n.c) * x[n.d];
+// The 7-point operator and the damped-Jacobi update with every rounding
+// explicit (no compiler contraction), so the one-cell, two-cell and
+// single-CTA smoothers give the same bits:
+//   L  = dg*xc - aE*xe - aW*xw - aN*xn - aS*xs - aU*xu - aD*xd  (left to right)
+//   lo = xc + dt*L,  x' = xc + inv*(b - lo),  r = b - lo.
+__device__ __forceinline__ float stencil_L(float dg, float xc, float ae, float xe, float aw, float xw, float an,
+                                           float xn, float as, float xs, float au, float xu, float ad, float xd) {
+    float s = __fmul_rn(dg, xc);
+    s = __fmaf_rn(-ae, xe, s);
+    s = __fmaf_rn(-aw, xw, s);
+    s = __fmaf_rn(-an, xn, s);
+    s = __fmaf_rn(-as, xs, s);
+    s = __fmaf_rn(-au, xu, s);
+    return __fmaf_rn(-ad, xd, s);
 }
+__device__ __forceinline__ float m_apply(float xc, float dt, float L) { return __fmaf_rn(dt, L, xc); }
+__device__ __forceinline__ float jacobi(float xc, float iv, float bc, float lo) {
+    return __fmaf_rn(iv, __fsub_rn(bc, lo), xc);
+}
+
+__device__ __forceinline__ float apply_Lf(const Coef& a, const float* __restrict__ x, const Nb7& n, float xc) {
+    return stencil_L(__ldg(a.diagL + n.c), xc, __ldg(a.aE + n.c), x[n.e], __ldg(a.aW + n.c), x[n.w],
+                     __ldg(a.aN + n.c), x[n.n], __ldg(a.aS + n.c), x[n.s], __ldg(a.aU + n.c), x[n.u],
+                     __ldg(a.aD + n.c), x[n.d]);
+}
+
 
 // (levels hold fewer than 2^31 cells: 32-bit index arithmetic)
 __device__ __forceinline__ void coords(const Lvl& g, long long idx, int& i, int& j, int& k) {
@@ -85,7 +107,7 @@ __global__ void __launch_bounds__(BLOCK) k_mop(const float* __restrict__ T, Coef
     coords(g, idx, i, j, k);
     const Nb7 n = nb7(g, i, j, k);
     const float tc = T[idx];
-    Lo[idx] = tc + dt * apply_L<float>(a, T, n, tc);
+    Lo[idx] = m_apply(tc, dt, apply_Lf(a, T, n, tc));
 }
 
 __global__ void __launch_bounds__(BLOCK) k_jacobi(float* __restrict__ x, const float* __restrict__ b,
@@ -105,7 +127,7 @@ __global__ void __launch_bounds__(BLOCK) k_apply_L(const float* __restrict__ T, 
     coords(g, idx, i, j, k);
     const Nb7 n = nb7(g, i, j, k);
     const float tc = T[idx];
-    const float lo = tc + dt * apply_L<float>(a, T, n, tc);
+    const float lo = m_apply(tc, dt, apply_Lf(a, T, n, tc));
     out[idx] = (lo - tc) / dt;
 }
 
@@ -119,15 +141,14 @@ __global__ void __launch_bounds__(BLOCK) k_smooth(const float* __restrict__ x, f
     coords(g, idx, i, j, k);
     const Nb7 n = nb7(g, i, j, k);
     const float tc = x[idx];
-    const float lo = tc + dt * apply_L<float>(a, x, n, tc);
-    xo[idx] = tc + __ldg(inv + idx) * (__ldg(b + idx) - lo);
+    xo[idx] = jacobi(tc, __ldg(inv + idx), __ldg(b + idx), m_apply(tc, dt, apply_Lf(a, x, n, tc)));
 }
 
 __global__ void __launch_bounds__(BLOCK) k_smooth_zero(float* __restrict__ xo, const float* __restrict__ b,
                                                        const float* __restrict__ inv, long long n) {
     const long long idx = (long long)blockIdx.x * blockDim.x + threadIdx.x;
     if (idx >= n) return;
-    xo[idx] = 0.f + inv[idx] * (b[idx] - 0.f);
+    xo[idx] = jacobi(0.f, inv[idx], b[idx], 0.f);
 }
 
 // The first two sweeps from a zero guess in one pass: x1 = invD b is formed on
@@ -139,13 +160,74 @@ __global__ void __launch_bounds__(BLOCK) k_smooth_first2(float* __restrict__ xo,
     int i, j, k;
     coords(g, idx, i, j, k);
     const Nb7 nb = nb7(g, i, j, k);
-    auto x1 = [&](long long q) { return 0.f + __ldg(inv + q) * (__ldg(b + q) - 0.f); };
+    auto x1 = [&](long long q) { return jacobi(0.f, __ldg(inv + q), __ldg(b + q), 0.f); };
     const float tc = x1(nb.c);
-    const float L = __ldg(a.diagL + nb.c) * tc - __ldg(a.aE + nb.c) * x1(nb.e) - __ldg(a.aW + nb.c) * x1(nb.w) -
-                    __ldg(a.aN + nb.c) * x1(nb.n) - __ldg(a.aS + nb.c) * x1(nb.s) - __ldg(a.aU + nb.c) * x1(nb.u) -
-                    __ldg(a.aD + nb.c) * x1(nb.d);
-    const float lo = tc + dt * L;
-    xo[idx] = tc + __ldg(inv + idx) * (__ldg(b + idx) - lo);
+    const float L = stencil_L(__ldg(a.diagL + nb.c), tc, __ldg(a.aE + nb.c), x1(nb.e), __ldg(a.aW + nb.c), x1(nb.w),
+                              __ldg(a.aN + nb.c), x1(nb.n), __ldg(a.aS + nb.c), x1(nb.s), __ldg(a.aU + nb.c),
+                              x1(nb.u), __ldg(a.aD + nb.c), x1(nb.d));
+    xo[idx] = jacobi(tc, __ldg(inv + idx), __ldg(b + idx), m_apply(tc, dt, L));
+}
+
+// ---- two cells per thread along k ------------------------------------------
+// Levels with an even nz: a thread owns cells (k, k+1) of one row, loads every
+// field as float2 and reuses the pair for each other's z neighbour.  Block =
+// 32 pairs x 4 rows; grid (nz/64, ny/4, nx) -- no index division.  Same
+// arithmetic per cell as k_smooth / k_smooth_first2.
+constexpr int PAIR_X = 32, PAIR_Y = 4;
+
+struct PairNb {
+    int c, e, w, n, s, d0, u1;   // row-major offsets: centre pair, lateral pairs, z neighbours outside the pair
+};
+__device__ __forceinline__ PairNb pair_nb(const Lvl& g, int i, int j, int k) {
+    const int iE = i < g.nx - 1 ? i + 1 : i - 1, iW = i > 0 ? i - 1 : low_ghost(g, 0);
+    const int jN = j < g.ny - 1 ? j + 1 : j - 1, jS = j > 0 ? j - 1 : low_ghost(g, 1);
+    const int kD = k > 0 ? k - 1 : low_ghost(g, 2);
+    const int kU = k + 2 < g.nz ? k + 2 : k;     // cell k+1's upper neighbour (mirror at the top)
+    const int nyz = g.ny * g.nz;
+    PairNb p;
+    p.c = i * nyz + j * g.nz + k;
+    p.e = iE * nyz + j * g.nz + k;
+    p.w = iW * nyz + j * g.nz + k;
+    p.n = i * nyz + jN * g.nz + k;
+    p.s = i * nyz + jS * g.nz + k;
+    p.d0 = i * nyz + j * g.nz + kD;
+    p.u1 = i * nyz + j * g.nz + kU;
+    return p;
+}
+__device__ __forceinline__ float2 ld2(const float* __restrict__ p, int o) {
+    return __ldg(reinterpret_cast<const float2*>(p + o));
+}
+
+template <bool FROM_ZERO>
+__global__ void __launch_bounds__(PAIR_X * PAIR_Y) k_smooth2(const float* __restrict__ x, float* __restrict__ xo,
+                                                             const float* __restrict__ b,
+                                                             const float* __restrict__ inv, Coef a, float dt, Lvl g) {
+    const int k = 2 * (blockIdx.x * PAIR_X + threadIdx.x);
+    const int j = blockIdx.y * PAIR_Y + threadIdx.y;
+    const int i = blockIdx.z;
+    if (k >= g.nz || j >= g.ny) return;
+    const PairNb p = pair_nb(g, i, j, k);
+    // the iterate at a pair position (or, from zero, the first sweep's value there)
+    auto X2 = [&](int o) -> float2 {
+        if (FROM_ZERO) {
+            const float2 iv = ld2(inv, o), bb = ld2(b, o);
+            return make_float2(jacobi(0.f, iv.x, bb.x, 0.f), jacobi(0.f, iv.y, bb.y, 0.f));
+        }
+        return *reinterpret_cast<const float2*>(x + o);
+    };
+    auto X1 = [&](int o) -> float {
+        if (FROM_ZERO) return jacobi(0.f, __ldg(inv + o), __ldg(b + o), 0.f);
+        return x[o];
+    };
+    const float2 xc = X2(p.c), xe = X2(p.e), xw = X2(p.w), xn = X2(p.n), xs = X2(p.s);
+    const float xd0 = X1(p.d0), xu1 = X1(p.u1);
+    const float2 dg = ld2(a.diagL, p.c), ae = ld2(a.aE, p.c), aw = ld2(a.aW, p.c), an = ld2(a.aN, p.c);
+    const float2 as = ld2(a.aS, p.c), au = ld2(a.aU, p.c), ad = ld2(a.aD, p.c);
+    const float2 iv = ld2(inv, p.c), bc = ld2(b, p.c);
+    const float L0 = stencil_L(dg.x, xc.x, ae.x, xe.x, aw.x, xw.x, an.x, xn.x, as.x, xs.x, au.x, xc.y, ad.x, xd0);
+    const float L1 = stencil_L(dg.y, xc.y, ae.y, xe.y, aw.y, xw.y, an.y, xn.y, as.y, xs.y, au.y, xu1, ad.y, xc.x);
+    *reinterpret_cast<float2*>(xo + p.c) = make_float2(jacobi(xc.x, iv.x, bc.x, m_apply(xc.x, dt, L0)),
+                                                       jacobi(xc.y, iv.y, bc.y, m_apply(xc.y, dt, L1)));
 }
 
 // All sweeps of a level small enough for one CTA (the coarsest level): the
@@ -163,7 +245,7 @@ __global__ void __launch_bounds__(SMALL_THREADS) k_smooth_small(float* __restric
     float* nxt = xs + n;
     int s0 = 0;
     for (int c = threadIdx.x; c < n; c += blockDim.x) {
-        if (from_zero) cur[c] = 0.f + inv[c] * (b[c] - 0.f);
+        if (from_zero) cur[c] = jacobi(0.f, inv[c], b[c], 0.f);
         else cur[c] = x[c];
     }
     if (from_zero) s0 = 1;
@@ -185,10 +267,9 @@ __global__ void __launch_bounds__(SMALL_THREADS) k_smooth_small(float* __restric
         for (int sw = s0; sw < n_sweeps; ++sw) {
             if (act) {
                 const float tc = cur[c];
-                const float L = dg * tc - ae * cur[nb.e] - aw * cur[nb.w] - an * cur[nb.n] - as * cur[nb.s] -
-                                au * cur[nb.u] - ad * cur[nb.d];
-                const float lo = tc + dt * L;
-                nxt[c] = tc + iv * (bc - lo);
+                const float L = stencil_L(dg, tc, ae, cur[nb.e], aw, cur[nb.w], an, cur[nb.n], as, cur[nb.s], au,
+                                          cur[nb.u], ad, cur[nb.d]);
+                nxt[c] = jacobi(tc, iv, bc, m_apply(tc, dt, L));
             }
             __syncthreads();
             float* t = cur;
@@ -202,8 +283,7 @@ __global__ void __launch_bounds__(SMALL_THREADS) k_smooth_small(float* __restric
                 coords(g, c, i, j, k);
                 const Nb7 nb = nb7(g, i, j, k);
                 const float tc = cur[c];
-                const float lo = tc + dt * apply_L<float>(a, cur, nb, tc);
-                nxt[c] = tc + __ldg(inv + c) * (__ldg(b + c) - lo);
+                nxt[c] = jacobi(tc, __ldg(inv + c), __ldg(b + c), m_apply(tc, dt, apply_Lf(a, cur, nb, tc)));
             }
             __syncthreads();
             float* t = cur;
@@ -235,10 +315,44 @@ __global__ void __launch_bounds__(BLOCK) k_residual_restrict(const float* __rest
                 const int i = 2 * ic + di, j = 2 * jc + dj, k = 2 * kc + dk;
                 const Nb7 n = nb7(g, i, j, k);
                 const float tc = x[n.c];
-                const float lo = tc + dt * apply_L<float>(a, x, n, tc);
-                s += (__ldg(b + n.c) - lo) * __ldg(mask + n.c);
+                const float lo = m_apply(tc, dt, apply_Lf(a, x, n, tc));
+                s += __fmul_rn(__fsub_rn(__ldg(b + n.c), lo), __ldg(mask + n.c));
             }
     bc[t] = s * 0.125f;
+}
+
+// The same restriction with one thread per fine cell: a block covers 64 fine k
+// x 2 fine j x 2 fine i of one coarse (jc, ic) column; k pairs are summed by a
+// shuffle, the four (j, i) partials in shared memory.  Full parallelism on the
+// coarse levels, where one thread per coarse cell leaves too few threads to
+// hide the latency of its eight stencils.  Sum order per coarse cell:
+// ((s00 + s01) + s10) + s11 with s_ji = r(k) + r(k+1).
+__global__ void __launch_bounds__(256) k_residual_restrict2(const float* __restrict__ x, const float* __restrict__ b,
+                                                            const float* __restrict__ mask, Coef a, float dt, Lvl g,
+                                                            float* __restrict__ bc, int cx, int cy, int cz) {
+    __shared__ float part[4][32];
+    const int t = threadIdx.x;
+    const int kk = t & 63, dj = (t >> 6) & 1, di = t >> 7;
+    const int k = blockIdx.x * 64 + kk;
+    const int jc = blockIdx.y, ic = blockIdx.z;
+    const int j = 2 * jc + dj, i = 2 * ic + di;
+    float r = 0.f;
+    if (k < 2 * cz) {
+        const Nb7 n = nb7(g, i, j, k);
+        const float tc = x[n.c];
+        const float lo = m_apply(tc, dt, apply_Lf(a, x, n, tc));
+        r = __fmul_rn(__fsub_rn(__ldg(b + n.c), lo), __ldg(mask + n.c));
+    }
+    r = __fadd_rn(r, __shfl_xor_sync(0xffffffffu, r, 1));
+    if ((kk & 1) == 0) part[(di << 1) | dj][kk >> 1] = r;
+    __syncthreads();
+    if (t < 32) {
+        const int kc = blockIdx.x * 32 + t;
+        if (kc < cz) {
+            const float s = __fadd_rn(__fadd_rn(__fadd_rn(part[0][t], part[1][t]), part[2][t]), part[3][t]);
+            bc[((long long)ic * cy + jc) * cz + kc] = __fmul_rn(s, 0.125f);
+        }
+    }
 }
 
 // trilinear (align_corners = False) source coordinate of fine index i
@@ -295,14 +409,10 @@ __device__ __forceinline__ void src_2to1(int i, int nc, int& i0, int& i1, float&
     }
 }
 
-__global__ void __launch_bounds__(BLOCK) k_prolong_2to1(float* __restrict__ x, const float* __restrict__ xc,
-                                                        const float* __restrict__ mask, int nx, int ny, int nz,
-                                                        int cx, int cy, int cz, float alpha) {
-    const int k = blockIdx.x * 64 + (threadIdx.x & 63);
-    const int j = blockIdx.y * 4 + (threadIdx.x >> 6);
-    const int i = blockIdx.z;
-    if (k >= nz || j >= ny) return;
-    const int idx = (i * ny + j) * nz + k;
+// trilinear interpolation of the coarse correction at one fine cell of an exact
+// 2:1 coarsening, then x = (x + alpha e) mask, every rounding explicit
+__device__ __forceinline__ float prolong_cell(const float* __restrict__ xc, int cy, int cz, int i, int j, int k, int cx,
+                                              float xv, float m, float alpha) {
     int i0, i1, j0, j1, k0, k1;
     float li, lj, lk;
     src_2to1(i, cx, i0, i1, li);
@@ -311,9 +421,38 @@ __global__ void __launch_bounds__(BLOCK) k_prolong_2to1(float* __restrict__ x, c
     const float hi = 1.f - li, hj = 1.f - lj, hk = 1.f - lk;
     const int p0 = i0 * cy * cz, p1 = i1 * cy * cz, r0 = j0 * cz, r1 = j1 * cz;
     auto X = [&](int p, int r, int c) { return __ldg(xc + p + r + c); };
-    const float e = hi * (hj * (hk * X(p0, r0, k0) + lk * X(p0, r0, k1)) + lj * (hk * X(p0, r1, k0) + lk * X(p0, r1, k1))) +
-                    li * (hj * (hk * X(p1, r0, k0) + lk * X(p1, r0, k1)) + lj * (hk * X(p1, r1, k0) + lk * X(p1, r1, k1)));
-    x[idx] = (x[idx] + alpha * e) * __ldg(mask + idx);
+    auto zl = [&](int p, int r) { return __fmaf_rn(lk, X(p, r, k1), __fmul_rn(hk, X(p, r, k0))); };
+    const float y0 = __fmaf_rn(lj, zl(p0, r1), __fmul_rn(hj, zl(p0, r0)));
+    const float y1 = __fmaf_rn(lj, zl(p1, r1), __fmul_rn(hj, zl(p1, r0)));
+    const float e = __fmaf_rn(li, y1, __fmul_rn(hi, y0));
+    return __fmul_rn(__fmaf_rn(alpha, e, xv), m);
+}
+
+__global__ void __launch_bounds__(BLOCK) k_prolong_2to1(float* __restrict__ x, const float* __restrict__ xc,
+                                                        const float* __restrict__ mask, int nx, int ny, int nz,
+                                                        int cx, int cy, int cz, float alpha) {
+    const int k = blockIdx.x * 64 + (threadIdx.x & 63);
+    const int j = blockIdx.y * 4 + (threadIdx.x >> 6);
+    const int i = blockIdx.z;
+    if (k >= nz || j >= ny) return;
+    const int idx = (i * ny + j) * nz + k;
+    x[idx] = prolong_cell(xc, cy, cz, i, j, k, cx, x[idx], __ldg(mask + idx), alpha);
+}
+
+// k_prolong_2to1 on two cells (k, k+1) per thread (nz even): float2 update of
+// x and float2 mask; the same interpolation per cell.
+__global__ void __launch_bounds__(PAIR_X * PAIR_Y) k_prolong2(float* __restrict__ x, const float* __restrict__ xc,
+                                                              const float* __restrict__ mask, int nx, int ny, int nz,
+                                                              int cx, int cy, int cz, float alpha) {
+    const int k = 2 * (blockIdx.x * PAIR_X + threadIdx.x);
+    const int j = blockIdx.y * PAIR_Y + threadIdx.y;
+    const int i = blockIdx.z;
+    if (k >= nz || j >= ny) return;
+    const int idx = (i * ny + j) * nz + k;
+    float2* xp = reinterpret_cast<float2*>(x + idx);
+    const float2 xv = *xp, m = __ldg(reinterpret_cast<const float2*>(mask + idx));
+    *xp = make_float2(prolong_cell(xc, cy, cz, i, j, k, cx, xv.x, m.x, alpha),
+                      prolong_cell(xc, cy, cz, i, j, k + 1, cx, xv.y, m.y, alpha));
 }
 
 // per-block partial sums of (w * (b - M x))^2 in FP64, w = mask or 1
@@ -328,9 +467,9 @@ __global__ void __launch_bounds__(BLOCK) k_residual_sq(const float* __restrict__
         coords(g, idx, i, j, k);
         const Nb7 n = nb7(g, i, j, k);
         const float tc = x[idx];
-        const float lo = tc + dt * apply_L<float>(a, x, n, tc);
-        float r = __ldg(b + idx) - lo;
-        if (mask) r *= __ldg(mask + idx);
+        const float lo = m_apply(tc, dt, apply_Lf(a, x, n, tc));
+        float r = __fsub_rn(__ldg(b + idx), lo);
+        if (mask) r = __fmul_rn(r, __ldg(mask + idx));
         if (r_out) r_out[idx] = r;
         v = (double)r * (double)r;
     }
@@ -427,6 +566,18 @@ int level_ok(const Lvl& g) {
 
 }  // namespace
 
+// two-cells-per-thread path: even nz, 8-byte aligned fields, grid within limits
+static bool pair_ok(const Lvl& g, std::initializer_list<const float*> ptrs) {
+    if (g.nz < 2 || (g.nz & 1) || g.nx > 65535 || (g.ny + PAIR_Y - 1) / PAIR_Y > 65535) return false;
+    for (const float* p : ptrs)
+        if (reinterpret_cast<uintptr_t>(p) & 7) return false;
+    return true;
+}
+static dim3 pair_grid(const Lvl& g) {
+    return dim3((unsigned)((g.nz + 2 * PAIR_X - 1) / (2 * PAIR_X)), (unsigned)((g.ny + PAIR_Y - 1) / PAIR_Y),
+                (unsigned)g.nx);
+}
+
 extern "C" {
 
 int fc_mg_mop(const float* T, const float* aE, const float* aW, const float* aN, const float* aS, const float* aU,
@@ -462,7 +613,12 @@ int fc_mg_smooth(const float* x_in, float* x_out, const float* b, const float* i
     Lvl g{nx, ny, nz, ax, out_idx};
     if (level_ok(g) || !x_in || !x_out || x_in == x_out || !b || !inv_diagM) return FC_ERR_ARG;
     Coef a{aE, aW, aN, aS, aU, aD, diagL};
-    k_smooth<<<grid_for((long long)nx * ny * nz), BLOCK, 0, (cudaStream_t)stream>>>(x_in, x_out, b, inv_diagM, a, dt, g);
+    if (pair_ok(g, {x_in, x_out, b, inv_diagM, aE, aW, aN, aS, aU, aD, diagL}))
+        k_smooth2<false><<<pair_grid(g), dim3(PAIR_X, PAIR_Y), 0, (cudaStream_t)stream>>>(x_in, x_out, b, inv_diagM,
+                                                                                         a, dt, g);
+    else
+        k_smooth<<<grid_for((long long)nx * ny * nz), BLOCK, 0, (cudaStream_t)stream>>>(x_in, x_out, b, inv_diagM, a,
+                                                                                      dt, g);
     return launch_status();
 }
 
@@ -486,8 +642,12 @@ int fc_mg_smooth_first2(float* x_out, const float* b, const float* inv_diagM, co
     Lvl g{nx, ny, nz, ax, out_idx};
     if (level_ok(g) || !x_out || !b || !inv_diagM || x_out == b) return FC_ERR_ARG;
     Coef a{aE, aW, aN, aS, aU, aD, diagL};
-    k_smooth_first2<<<grid_for((long long)nx * ny * nz), BLOCK, 0, (cudaStream_t)stream>>>(x_out, b, inv_diagM, a,
-                                                                                         dt, g);
+    if (pair_ok(g, {x_out, b, inv_diagM, aE, aW, aN, aS, aU, aD, diagL}))
+        k_smooth2<true><<<pair_grid(g), dim3(PAIR_X, PAIR_Y), 0, (cudaStream_t)stream>>>(nullptr, x_out, b, inv_diagM,
+                                                                                        a, dt, g);
+    else
+        k_smooth_first2<<<grid_for((long long)nx * ny * nz), BLOCK, 0, (cudaStream_t)stream>>>(x_out, b, inv_diagM,
+                                                                                             a, dt, g);
     return launch_status();
 }
 
@@ -506,8 +666,13 @@ int fc_mg_residual_restrict(const float* x, const float* b, const float* mask, c
     if (level_ok(g) || !x || !b || !mask || !b_coarse) return FC_ERR_ARG;
     if (cx != nx / 2 || cy != ny / 2 || cz != nz / 2 || cx < 1 || cy < 1 || cz < 1) return FC_ERR_ARG;
     Coef a{aE, aW, aN, aS, aU, aD, diagL};
-    k_residual_restrict<<<grid_for((long long)cx * cy * cz), BLOCK, 0, (cudaStream_t)stream>>>(
-        x, b, mask, a, dt, g, b_coarse, cx, cy, cz);
+    if (cy <= 65535 && cx <= 65535) {
+        const dim3 grid((unsigned)((2 * cz + 63) / 64), (unsigned)cy, (unsigned)cx);
+        k_residual_restrict2<<<grid, 256, 0, (cudaStream_t)stream>>>(x, b, mask, a, dt, g, b_coarse, cx, cy, cz);
+    } else {
+        k_residual_restrict<<<grid_for((long long)cx * cy * cz), BLOCK, 0, (cudaStream_t)stream>>>(
+            x, b, mask, a, dt, g, b_coarse, cx, cy, cz);
+    }
     return launch_status();
 }
 
@@ -516,8 +681,15 @@ int fc_mg_prolong_correct(float* x, const float* x_coarse, const float* mask, in
     if (!x || !x_coarse || !mask || nx < 1 || ny < 1 || nz < 1 || cx < 1 || cy < 1 || cz < 1) return FC_ERR_ARG;
     if ((long long)nx * ny * nz >= (1LL << 31)) return FC_ERR_ARG;
     if (nx == 2 * cx && ny == 2 * cy && nz == 2 * cz) {
-        const dim3 grid((unsigned)((nz + 63) / 64), (unsigned)((ny + 3) / 4), (unsigned)nx);
-        k_prolong_2to1<<<grid, BLOCK, 0, (cudaStream_t)stream>>>(x, x_coarse, mask, nx, ny, nz, cx, cy, cz, alpha);
+        const Lvl g{nx, ny, nz, 0, 0};
+        if (pair_ok(g, {x, mask})) {
+            k_prolong2<<<pair_grid(g), dim3(PAIR_X, PAIR_Y), 0, (cudaStream_t)stream>>>(x, x_coarse, mask, nx, ny, nz,
+                                                                                       cx, cy, cz, alpha);
+        } else {
+            const dim3 grid((unsigned)((nz + 63) / 64), (unsigned)((ny + 3) / 4), (unsigned)nx);
+            k_prolong_2to1<<<grid, BLOCK, 0, (cudaStream_t)stream>>>(x, x_coarse, mask, nx, ny, nz, cx, cy, cz,
+                                                                      alpha);
+        }
     } else {
         k_prolong_correct<<<grid_for((long long)nx * ny * nz), BLOCK, 0, (cudaStream_t)stream>>>(
             x, x_coarse, mask, nx, ny, nz, cx, cy, cz, alpha);

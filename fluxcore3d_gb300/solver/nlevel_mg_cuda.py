@@ -202,14 +202,12 @@ class NLevelGeometricMGSolver:
         cur, alt = lv["x"], lv["Lo"]
         start = 0
         if from_zero and n_sweeps >= 2:
-            # sweeps 1 and 2 from the zero guess in one pass
-            _lib.call("fc_mg_smooth_first2", ptr(alt), ptr(lv["b_buf"]), ptr(lv["inv_diagM"]), *cp, dt, nx, ny, nz,
+            # sweeps 1 and 2 from the zero guess in one pass, straight into x (x is not read)
+            _lib.call("fc_mg_smooth_first2", ptr(cur), ptr(lv["b_buf"]), ptr(lv["inv_diagM"]), *cp, dt, nx, ny, nz,
                       self.ax, lv["out_idx"], st)
-            cur, alt = alt, cur
             start = 2
         elif from_zero:
-            _lib.call("fc_mg_smooth_from_zero", ptr(alt), ptr(lv["b_buf"]), ptr(lv["inv_diagM"]), cur.numel(), st)
-            cur, alt = alt, cur
+            _lib.call("fc_mg_smooth_from_zero", ptr(cur), ptr(lv["b_buf"]), ptr(lv["inv_diagM"]), cur.numel(), st)
             start = 1
         for _ in range(start, n_sweeps):
             _lib.call("fc_mg_smooth", ptr(cur), ptr(alt), ptr(lv["b_buf"]), ptr(lv["inv_diagM"]), *cp, dt, nx, ny,

@@ -248,3 +248,4 @@ def test_thermal_pseudo_time_steps_match_oracle(cuda):
         assert rise > 1e-2
         assert float(np.abs(got - T).max()) <= 8 * float(np.spacing(np.float32(32.0))) + 1e-5 * rise, it
     assert np.isfinite(info["r_rel"])
+
