@@ -329,6 +329,18 @@ def _bicg_solve(mg, V: _Vec, b: Tensor, x: Tensor, bnorm: float, tol: float, max
     ws = W["ws"]
     pc = _graph_pc(mg).eager
     lv0 = mg._levels[0]
+    if not f64:
+        # FP32 vectors: the V-cycle reads its right-hand side from the Krylov vector and leaves its
+        # result in the destination vector (no masked copies in or out).  Every vector of this
+        # recurrence is zero on the Dirichlet rows (the operator apply masks them, and the
+        # smoother's inverse diagonal is zero there), so the copies would change nothing.
+        def pc(src, dst):
+            saved = (lv0["b_buf"], lv0["x"])
+            lv0["b_buf"], lv0["x"] = src, dst
+            try:
+                mg._vcycle(0, zero_guess=True)
+            finally:
+                lv0["b_buf"], lv0["x"] = saved
     nx, ny, nz = lv0["shape"]
     mop_name = "fc_mg_mop_f64" if f64 else "fc_mg_mop_f32"
     dt = float(mg._dt_cache)
