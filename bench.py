@@ -374,6 +374,7 @@ def main():
     ap.add_argument("--no-geometry", action="store_true", help="skip the voxel SDF / link builder timings")
     ap.add_argument("--no-io", action="store_true", help="skip the snapshot / checkpoint timings")
     ap.add_argument("--no-accuracy", action="store_true", help="skip the FP16/FP32 vs FP64 accuracy report")
+    ap.add_argument("--no-learned", action="store_true", help="skip the learned-preconditioner training / A-B")
     ap.add_argument("--accuracy-steps", type=int, default=600)
     ap.add_argument("--storages", default="fp16,fp32", help="population storages to time (first = headline)")
     ap.add_argument("--profile", action="store_true",
@@ -383,6 +384,7 @@ def main():
     if args.profile:
         args.storages = args.storages.split(",")[0]
         args.no_e2e = args.no_cpu = args.no_thermal = args.no_geometry = args.no_io = args.no_accuracy = True
+        args.no_learned = True
     if args.impl == "reference":
         run_reference(args)
         return
@@ -504,6 +506,9 @@ def main():
     if not args.no_io:
         from fluxcore3d_gb300 import io_bench
         line["io"] = io_bench.run(dev)
+    if rank == 0 and not args.no_learned:
+        from fluxcore3d_gb300 import learned_bench
+        line["learned"] = learned_bench.run(dev, eval_seeds=(1001, 1002))
     if rank == 0 and not args.no_accuracy:
         line["accuracy"] = accuracy_run(args, dev)
     if rank == 0 and not args.no_cpu:

@@ -142,10 +142,10 @@ __global__ void k_mse_grad(const float* __restrict__ y, int C, const float* __re
     const long long v = (long long)blockIdx.x * BLOCK + threadIdx.x;
     double l = 0.0;
     if (v < nvox) {
-        const float m = mask ? mask[v] : 1.f;
+        const float m = mask ? mask[v] : 1.f;   // per-voxel weight (0/1 mask or a relative-error scale)
         const float d = (y[v * C] - target[v]) * m;
         l = (double)d * d;
-        for (int c = 0; c < C; ++c) grad[v * C + c] = c == 0 ? 2.f * d / (float)nvox : 0.f;
+        for (int c = 0; c < C; ++c) grad[v * C + c] = c == 0 ? 2.f * d * m / (float)nvox : 0.f;
     }
     sh[threadIdx.x] = l;
     __syncthreads();

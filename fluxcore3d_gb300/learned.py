@@ -161,8 +161,11 @@ class UNetPreconditioner:
         _lib.call("fc_nn_act_bwd", ptr(g), ptr(add), ptr(y), int(relu), n, ptr(gf), ptr(gb), stream_ptr())
         return gf, gb
 
-    def loss_and_grad(self, r, k, target):
+    def loss_and_grad(self, r, k, target, relative: bool = False):
         """MSE between the network output and target / rms(r) (the normalised error); fills layer.g.
+        With `relative`, each sample's squared error is divided by the mean square of its
+        normalised target, so a sample whose error is small next to its residual weighs as much
+        as any other (otherwise predicting zero is already a low loss for it).
         Returns (loss, [grad per layer as [C_out, 27, C_in] FP32])."""
         self.forward(r, k, keep=True)
         S = self._saved
@@ -170,11 +173,16 @@ class UNetPreconditioner:
         s0, s1, s2 = (B, D, H, W), (B, D // 2, H // 2, W // 2), (B, D // 4, H // 4, W // 4)
         st = stream_ptr()
         nvox = B * D * H * W
-        tn = (target.reshape(B, -1) * S["inv"][:, None]).reshape(-1).contiguous()
+        tn2 = target.reshape(B, -1) * S["inv"][:, None]
+        tn = tn2.reshape(-1).contiguous()
+        wv = None
+        if relative:
+            trms = torch.sqrt(torch.mean(tn2.double() ** 2, dim=1)).float() + 1e-30
+            wv = (1.0 / trms)[:, None].expand(B, D * H * W).reshape(-1).contiguous()
         gj = torch.empty((B, D, H, W, 16), dtype=torch.float32, device=self.device)
         nb = int(_lib.call("fc_nn_mse_workspace_bytes", nvox))
         ws = self._buf(("mse", nb), (nb,), torch.uint8)
-        _lib.call("fc_nn_mse_grad", ptr(S["yj"]), 16, ptr(tn), None, nvox, ptr(gj), ptr(ws), nb, st)
+        _lib.call("fc_nn_mse_grad", ptr(S["yj"]), 16, ptr(tn), ptr(wv), nvox, ptr(gj), ptr(ws), nb, st)
         nblk = (nvox + 255) // 256
         loss = float(ws[: nblk * 8].view(torch.float64).sum().item()) / nvox
         L = self.L
@@ -256,4 +264,49 @@ class LearnedPreconditioner:
         _lib.call("fc_vec_convert", 1, ptr(self.r32), ptr(r64), n, ptr(self.mask), 1.0, st)
         z = self.net.forward(self.r32, self.k)
         _lib.call("fc_vec_convert", 0, ptr(z64), ptr(z), n, ptr(self.mask), 1.0, st)
+        self.calls += 1
+
+
+class LearnedCorrection:
+    """Preconditioner callable (r64, z64) for fgmres_mg_f64: one plain V-cycle, then the network
+    applied to what it leaves behind,  z = v + N(r - A v)  with v = V(r).
+
+    The V-cycle removes the oscillatory error; the network is trained (learned_bench,
+    `correction=True` pairs) on the residual a V-cycle leaves and the exact error that goes with
+    it, i.e. on the smooth, long-range part that geometric coarsening handles poorly across the
+    conductivity jumps and along the flow.  Every vector is zero on the Dirichlet rows."""
+
+    def __init__(self, net: UNetPreconditioner, mg_solver, k_field: torch.Tensor):
+        self.net = net
+        self.mg = mg_solver
+        lv0 = mg_solver._levels[0]
+        self.lv0 = lv0
+        self.shape = lv0["shape"]
+        self.mask = lv0["mask_f"]
+        self.k = k_field.reshape((1,) + tuple(self.shape)).float().contiguous()
+        self.r1 = torch.empty((1,) + tuple(self.shape), dtype=torch.float32, device=net.device)
+        self.calls = 0
+
+    def residual_after_vcycle(self, b32: torch.Tensor) -> torch.Tensor:
+        """v = V(b) in lv0['x'] and r1 = b - A v (masked) in self.r1; b32 FP32 masked."""
+        mg, lv0 = self.mg, self.lv0
+        nx, ny, nz = self.shape
+        st = stream_ptr()
+        if b32.data_ptr() != lv0["b_buf"].data_ptr():
+            lv0["b_buf"].copy_(b32.reshape(self.shape))
+        mg._vcycle(0, zero_guess=True)
+        _lib.call("fc_mg_mop_f32", ptr(lv0["x"]), *mg._cptrs(lv0), float(mg._dt_cache), nx, ny, nz, mg.ax,
+                  lv0["out_idx"], ptr(lv0["b_buf"]), ptr(self.mask), ptr(self.r1), st)
+        return self.r1
+
+    def __call__(self, r64: torch.Tensor, z64: torch.Tensor) -> None:
+        lv0 = self.lv0
+        n = self.r1.numel()
+        st = stream_ptr()
+        _lib.call("fc_vec_convert", 1, ptr(lv0["b_buf"]), ptr(r64), n, ptr(self.mask), 1.0, st)
+        r1 = self.residual_after_vcycle(lv0["b_buf"])
+        y = self.net.forward(r1, self.k)
+        # x += y (masked), then z = x in FP64
+        _lib.call("fc_vec_axpby", 0, ptr(lv0["x"]), ptr(y), n, 1.0, None, None, 1.0, ptr(self.mask), st)
+        _lib.call("fc_vec_convert", 0, ptr(z64), ptr(lv0["x"]), n, ptr(self.mask), 1.0, st)
         self.calls += 1

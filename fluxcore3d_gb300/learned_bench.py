@@ -8,7 +8,11 @@ Training pairs (r, e) are generated by the plain solver itself: e = A^-1 r to
 an FP64 relative residual of 1e-9 for right-hand sides that mix point sources,
 smooth fields and noise.  Evaluation: flexible GMRES to a 1e-8 FP64 residual
 with the network as preconditioner (plain V-cycle fallback on stall) against
-the same FGMRES with one V-cycle, on held-out seeds.
+the same FGMRES with one V-cycle, on held-out seeds, and the device-resident
+plain BiCGSTAB beside them.  The default mode uses the network as a correction
+after one V-cycle (LearnedCorrection), trained with a relative loss on the
+residual a V-cycle leaves; `correction_quality` measures what one application
+gains over the V-cycle alone.
 """
 from __future__ import annotations
 
@@ -19,7 +23,7 @@ import numpy as np
 import torch
 
 from .geometry import random_spheres_mask
-from .learned import LearnedPreconditioner, UNetPreconditioner
+from .learned import LearnedCorrection, LearnedPreconditioner, UNetPreconditioner
 from .solver import mg_pcg
 from .solver.nlevel_mg_cuda import NLevelGeometricMGSolver
 
@@ -63,19 +67,38 @@ def random_rhs(n: int, rng: np.random.Generator, dev, solid):
     return b.contiguous()
 
 
-def generate_pairs(n: int, n_geom: int, per_geom: int, seed0: int, dev):
+def residual_after_vcycle(mg, b: torch.Tensor) -> torch.Tensor:
+    """b - A V(b) (FP32, masked): what one plain V-cycle leaves of the right-hand side b."""
+    from . import _lib
+    from ._torch import ptr, stream_ptr
+    lv0 = mg._levels[0]
+    nx, ny, nz = lv0["shape"]
+    lv0["b_buf"].copy_(b.reshape(lv0["shape"]))
+    mg._vcycle(0, zero_guess=True)
+    r1 = torch.empty(lv0["shape"], dtype=torch.float32, device=b.device)
+    _lib.call("fc_mg_mop_f32", ptr(lv0["x"]), *mg._cptrs(lv0), float(mg._dt_cache), nx, ny, nz, mg.ax,
+              lv0["out_idx"], ptr(lv0["b_buf"]), ptr(lv0["mask_f"]), ptr(r1), stream_ptr())
+    return r1
+
+
+def generate_pairs(n: int, n_geom: int, per_geom: int, seed0: int, dev, correction: bool = False):
+    """(r, e = A^-1 r, k) triples solved by the plain solver; with `correction`, r is the residual
+    one V-cycle leaves of a random right-hand side (the network's input inside LearnedCorrection)."""
     rng = np.random.default_rng(seed0)
     data = []
     for g in range(n_geom):
         mg, k, solid = make_problem(n, seed0 + g, dev)
         for _ in range(per_geom):
             b = random_rhs(n, rng, dev, solid)
+            if correction:
+                b = residual_after_vcycle(mg, b).contiguous()
             x, info = mg_pcg.bicgstab_mg_f64(mg, b, tol=1e-9, max_it=400)
             data.append((b, x.float().contiguous(), k))
     return data
 
 
-def train(net: UNetPreconditioner, data, steps: int, batch: int = 2, lr: float = 2e-3, seed: int = 0):
+def train(net: UNetPreconditioner, data, steps: int, batch: int = 2, lr: float = 2e-3, seed: int = 0,
+          relative: bool = True):
     rng = np.random.default_rng(seed)
     losses = []
     t0 = time.perf_counter()
@@ -84,7 +107,7 @@ def train(net: UNetPreconditioner, data, steps: int, batch: int = 2, lr: float =
         r = torch.stack([data[i][0] for i in idx])
         e = torch.stack([data[i][1] for i in idx])
         k = torch.stack([data[i][2] for i in idx])
-        loss, _ = net.loss_and_grad(r, k, e)
+        loss, _ = net.loss_and_grad(r, k, e, relative=relative)
         lr_t = lr * 0.5 * (1 + math.cos(math.pi * it / max(1, steps)))
         net.adam_step(lr=lr_t)
         losses.append(loss)
@@ -92,13 +115,13 @@ def train(net: UNetPreconditioner, data, steps: int, batch: int = 2, lr: float =
     return losses, time.perf_counter() - t0
 
 
-def evaluate(net: UNetPreconditioner, n: int, seeds, dev, tol=1e-8, repeats=3):
+def evaluate(net: UNetPreconditioner, n: int, seeds, dev, tol=1e-8, repeats=3, correction: bool = False):
     rows = []
     rng = np.random.default_rng(12345)
     for s in seeds:
         mg, k, solid = make_problem(n, s, dev)
         b = random_rhs(n, rng, dev, solid)
-        pc = LearnedPreconditioner(net, mg, k)
+        pc = LearnedCorrection(net, mg, k) if correction else LearnedPreconditioner(net, mg, k)
 
         def timed(fn):
             best, info = None, None
@@ -113,22 +136,53 @@ def evaluate(net: UNetPreconditioner, n: int, seeds, dev, tol=1e-8, repeats=3):
         plain_ms, plain = timed(lambda: mg_pcg.fgmres_mg_f64(mg, b, tol=tol, max_it=300, restart=30))
         learn_ms, learn = timed(lambda: mg_pcg.fgmres_mg_f64(mg, b, tol=tol, max_it=300, restart=30, precond=pc,
                                                               stall_fallback=mg_pcg._vcycle_pc(mg)))
+        bicg_ms, bicg = timed(lambda: mg_pcg.bicgstab_mg_f64(mg, b, tol=tol, max_it=300))
         rows.append({"seed": int(s), "plain_ms": round(plain_ms, 3), "plain_it": plain["it"],
                      "plain_res": plain["res_rel"], "learned_ms": round(learn_ms, 3), "learned_it": learn["it"],
-                     "learned_res": learn["res_rel"], "learned_fell_back": learn["fell_back"]})
+                     "learned_res": learn["res_rel"], "learned_fell_back": learn["fell_back"],
+                     "plain_bicgstab_ms": round(bicg_ms, 3), "plain_bicgstab_it": bicg["it"],
+                     "plain_bicgstab_res": bicg["res_rel"]})
     return rows
 
 
-def run(dev, n_train=32, n_eval=64, n_geom=12, per_geom=4, steps=300, eval_seeds=(1001, 1002, 1003)):
+def correction_quality(net: UNetPreconditioner, n: int, seeds, dev) -> list:
+    """Relative error after one plain V-cycle and after the V-cycle plus the network correction,
+    against the exact solution (FP64 solve to 1e-10), on held-out problems."""
+    rows = []
+    rng = np.random.default_rng(7)
+    for s in seeds:
+        mg, k, solid = make_problem(n, s, dev)
+        b = random_rhs(n, rng, dev, solid)
+        e, _ = mg_pcg.bicgstab_mg_f64(mg, b, tol=1e-10, max_it=500)
+        e = e.float()
+        pc = LearnedCorrection(net, mg, k)
+        r1 = pc.residual_after_vcycle(b.contiguous())
+        v = mg._levels[0]["x"].clone()
+        y = net.forward(r1.reshape((1,) + tuple(r1.shape[-3:])), pc.k).reshape(v.shape)
+        nrm = float(torch.linalg.norm(e))
+        rows.append({"seed": int(s), "vcycle_rel_err": float(torch.linalg.norm(e - v)) / nrm,
+                     "vcycle_plus_net_rel_err": float(torch.linalg.norm(e - v - y)) / nrm})
+    return rows
+
+
+def run(dev, n_train=32, n_eval=64, n_geom=12, per_geom=4, steps=300, eval_seeds=(1001, 1002, 1003),
+        correction: bool = True):
     t = time.perf_counter()
-    data = generate_pairs(n_train, n_geom, per_geom, 100, dev)
+    data = generate_pairs(n_train, n_geom, per_geom, 100, dev, correction=correction)
     gen_s = time.perf_counter() - t
     net = UNetPreconditioner(device=dev, seed=0)
     losses, train_s = train(net, data, steps)
-    rows = evaluate(net, n_eval, eval_seeds, dev)
-    out = {"train_volume": n_train, "pairs": len(data), "pair_generation_s": round(gen_s, 2), "train_steps": steps,
+    rows = evaluate(net, n_eval, eval_seeds, dev, correction=correction)
+    quality = correction_quality(net, n_eval, eval_seeds[:2], dev) if correction else []
+    out = {"mode": "V-cycle + network correction" if correction else "network alone",
+           "train_volume": n_train, "pairs": len(data), "pair_generation_s": round(gen_s, 2), "train_steps": steps,
            "train_s": round(train_s, 2), "loss_first": float(np.mean(losses[:10])),
            "loss_last": float(np.mean(losses[-10:])), "eval_volume": n_eval, "eval": rows,
            "speedup_plain_over_learned": round(float(np.median([r["plain_ms"] / r["learned_ms"] for r in rows])), 3),
+           "iteration_ratio_plain_over_learned": round(float(np.median([r["plain_it"] / max(1, r["learned_it"])
+                                                                        for r in rows])), 3),
+           "speedup_plain_bicgstab_over_learned": round(float(np.median([r["plain_bicgstab_ms"] / r["learned_ms"]
+                                                                         for r in rows])), 3),
+           "correction_quality": quality,
            "device_error": net.check_device_error()}
     return out
