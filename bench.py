@@ -275,6 +275,7 @@ def accuracy_run(args, dev):
     import torch
     from fluxcore3d_gb300 import case as cases
     from fluxcore3d_gb300 import thermal_bench
+    from fluxcore3d_gb300.diagnostics import heat_balance, lbm_mass
     from fluxcore3d_gb300.solver import mg_pcg
     from fluxcore3d_gb300.solver.lbm_cuda_ext import LBMCUDAUpgrade
     from oracle.lbm import OracleLBM
@@ -291,12 +292,15 @@ def accuracy_run(args, dev):
     orc.step(steps)
     fp64_s = time.perf_counter() - t
     vel = {"fp64": _velocity_from_f(orc.f, shape)}
+    mass = {}
     for storage in ("fp32", "fp16"):
         sim = cases.pin_fin(device=dev, storage=storage, **ACC_CASE)
         sim.cfg.macro_stride = 1
         LBMCUDAUpgrade.patch(sim)
+        m0 = lbm_mass(sim)
         for _ in range(steps):
             sim.step(do_thermal=False)
+        mass[storage] = (lbm_mass(sim) - m0) / m0
         sim.sync_f()
         vel[storage] = _velocity_from_f(sim.f.cpu().numpy(), shape)
     fluid = ~ref.solid_flow.cpu().numpy()
@@ -304,7 +308,7 @@ def accuracy_run(args, dev):
     out = {"workload": "pin fin 128x64x64 (8x4 pins r=3.5, h=40), MRT + Bouzidi IBB, u=0.08, Re=200",
            "steps": steps, "fp64_run": f"CPU oracle in FP64, {os.cpu_count()} threads, {fp64_s:.1f} s",
            "velocity_rel_l2": {}, "temperature_rel_max": {}, "temperature_rel_l2": {}, "wall_heat_flow_rel": {},
-           "nusselt": {}, "nusselt_rel": {}}
+           "nusselt": {}, "nusselt_rel": {}, "heat_balance": {}, "mass_rel_change": {}}
     k = ref.k.cpu().numpy().astype(np.float64)
     solid = ref.solid.cpu().numpy()
     T, heat = {}, {}
@@ -316,6 +320,8 @@ def accuracy_run(args, dev):
         mg, b = thermal_bench.thermal_system(ref, u, v, w)
         x, info = mg_pcg.bicgstab_mg_f64(mg, b, tol=1e-10, max_it=400)
         T[name] = x.reshape(shape).cpu().numpy().astype(np.float64)
+        hb = heat_balance(mg, x, b / 1000.0, 1000.0)
+        out["heat_balance"][name] = {k: (float(f"{v:.6g}")) for k, v in hb.items()}
         heat[name] = _wall_heat(T[name], k, solid, 2 * 3.5)
         out["nusselt"][name] = round(heat[name][2], 6)
     for name in ("fp32", "fp16"):
@@ -325,6 +331,7 @@ def accuracy_run(args, dev):
         out["wall_heat_flow_rel"][name] = float(abs(heat[name][0] - heat["fp64"][0]) / abs(heat["fp64"][0]))
         out["nusselt_rel"][name] = float(abs(heat[name][2] - heat["fp64"][2]) / abs(heat["fp64"][2]))
     out["wall_faces"] = heat["fp64"][1]
+    out["mass_rel_change"] = {k: float(f"{v:.6g}") for k, v in mass.items()}
     return out
 
 

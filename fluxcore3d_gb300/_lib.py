@@ -173,6 +173,11 @@ SIGNATURES: dict[str, tuple] = {
     "fc_vox_parity_z": (i32, [vp, i64, i32, i32, i32, f64, f64, f64, f64, f64, f64, vp, vp]),
     "fc_geom_stamp_body": (i32, [vp, i32, i32, i32, i32, i32, i32, i32, i32, i32, vp, vp, vp, f32, f32, vp, vp,
                                  vp]),
+    # FP64 conservation integrals
+    "fc_lbm_mass_workspace_bytes": (i64, []),
+    "fc_lbm_mass": (i32, [vp, i32, vp, i64, vp, i64, vp, vp]),
+    "fc_mg_heat_balance_workspace_bytes": (i64, [i64]),
+    "fc_mg_heat_balance": (i32, [vp, vp, vp, vp, vp, vp, vp, vp, vp, vp, i32, i32, i32, i32, i32, vp, i64, vp, vp]),
     # passive tracer
     "fc_tracer_step": (i32, [vp, vp, vp, vp, vp, vp, i32, i32, i32, f32, vp]),
     "fc_tracer_inject": (i32, [vp, vp, i64, vp]),

@@ -482,6 +482,58 @@ __global__ void __launch_bounds__(BLOCK) k_residual_sq(const float* __restrict__
     if (threadIdx.x == 0) part[blockIdx.x] = sh[0];
 }
 
+// Heat-balance integrals in FP64 over the non-Dirichlet cells (mask != 0):
+// part[3 b + 0] = sum src, [3 b + 1] = sum L(T) (the operator's net outflow of
+// heat, boundary fluxes included), [3 b + 2] = sum T.  L in FP64 from the FP32
+// coefficients and temperatures.
+__global__ void __launch_bounds__(BLOCK) k_heat_balance(const float* __restrict__ T, const float* __restrict__ src,
+                                                        const float* __restrict__ mask, Coef a, Lvl g,
+                                                        double* __restrict__ part) {
+    __shared__ double sh[3][BLOCK];
+    const long long idx = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    double vs = 0.0, vl = 0.0, vt = 0.0;
+    if (idx < (long long)g.nx * g.ny * g.nz && __ldg(mask + idx) != 0.f) {
+        int i, j, k;
+        coords(g, idx, i, j, k);
+        const Nb7 n = nb7(g, i, j, k);
+        const double tc = T[idx];
+        vl = (double)__ldg(a.diagL + idx) * tc - (double)__ldg(a.aE + idx) * (double)T[n.e] -
+             (double)__ldg(a.aW + idx) * (double)T[n.w] - (double)__ldg(a.aN + idx) * (double)T[n.n] -
+             (double)__ldg(a.aS + idx) * (double)T[n.s] - (double)__ldg(a.aU + idx) * (double)T[n.u] -
+             (double)__ldg(a.aD + idx) * (double)T[n.d];
+        vs = src ? (double)__ldg(src + idx) : 0.0;
+        vt = tc;
+    }
+    sh[0][threadIdx.x] = vs;
+    sh[1][threadIdx.x] = vl;
+    sh[2][threadIdx.x] = vt;
+    __syncthreads();
+    for (int st = BLOCK / 2; st > 0; st >>= 1) {
+        if ((int)threadIdx.x < st)
+            for (int c = 0; c < 3; ++c) sh[c][threadIdx.x] += sh[c][threadIdx.x + st];
+        __syncthreads();
+    }
+    if (threadIdx.x < 3) part[3 * (long long)blockIdx.x + threadIdx.x] = sh[threadIdx.x][0];
+}
+
+// column c of an [n][3] partial array summed in fixed order by one block
+__global__ void __launch_bounds__(BLOCK) k_sum_partials3(const double* __restrict__ part, int n,
+                                                         double* __restrict__ out) {
+    __shared__ double sh[BLOCK];
+    for (int c = 0; c < 3; ++c) {
+        double v = 0.0;
+        for (int p = threadIdx.x; p < n; p += BLOCK) v += part[3 * p + c];
+        sh[threadIdx.x] = v;
+        __syncthreads();
+        for (int s = BLOCK / 2; s > 0; s >>= 1) {
+            if ((int)threadIdx.x < s) sh[threadIdx.x] += sh[threadIdx.x + s];
+            __syncthreads();
+        }
+        if (threadIdx.x == 0) out[c] = sh[0];
+        __syncthreads();
+    }
+}
+
 // sum of partials in fixed order by one block
 __global__ void __launch_bounds__(BLOCK) k_sum_partials(const double* __restrict__ part, int n, double* __restrict__ out) {
     __shared__ double sh[BLOCK];
@@ -718,6 +770,31 @@ int fc_mg_residual_norm2(const float* x, const float* b, const float* mask, cons
     int rc = launch_status();
     if (rc) return rc;
     k_sum_partials<<<1, BLOCK, 0, st>>>(part, (int)nb, result);
+    return launch_status();
+}
+
+long long fc_mg_heat_balance_workspace_bytes(long long n) {
+    if (n < 0) return -1;
+    return (long long)(grid_for(n) + 1) * 3 * (long long)sizeof(double);
+}
+
+int fc_mg_heat_balance(const float* T, const float* src, const float* mask, const float* aE, const float* aW,
+                       const float* aN, const float* aS, const float* aU, const float* aD, const float* diagL, int nx,
+                       int ny, int nz, int ax, int out_idx, void* workspace, long long workspace_bytes,
+                       double* result3, void* stream) {
+    Lvl g{nx, ny, nz, ax, out_idx};
+    const long long n = (long long)nx * ny * nz;
+    if (level_ok(g) || !T || !mask || !workspace || !result3 || !aE || !aW || !aN || !aS || !aU || !aD || !diagL)
+        return FC_ERR_ARG;
+    if (workspace_bytes < fc_mg_heat_balance_workspace_bytes(n)) return FC_ERR_ARG;
+    Coef a{aE, aW, aN, aS, aU, aD, diagL};
+    double* part = reinterpret_cast<double*>(workspace);
+    const unsigned nb = grid_for(n);
+    cudaStream_t st = (cudaStream_t)stream;
+    k_heat_balance<<<nb, BLOCK, 0, st>>>(T, src, mask, a, g, part);
+    int rc = launch_status();
+    if (rc) return rc;
+    k_sum_partials3<<<1, BLOCK, 0, st>>>(part, (int)nb, result3);
     return launch_status();
 }
 

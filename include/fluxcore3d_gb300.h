@@ -452,6 +452,26 @@ int fc_tracer_step(const float* phi, float* phi_out, const float* u, const float
 /* TracerField.inject (:51-53): phi = 1 where mask != 0 */
 int fc_tracer_inject(float* phi, const uint8_t* mask, long long n, void* stream);
 
+/* ---------------------------------------------------------------------------
+ * FP64 conservation integrals (no reference counterpart: the reference tracks
+ * mass change and heat in FP32 torch reductions or not at all)
+ * ------------------------------------------------------------------------- */
+/* mass = sum over cells with flag bit CF_SOLID clear (flags may be NULL: all
+ * cells) of sum_q f_q, populations [19][n] in storage `storage` (0 FP32, 1 FP16
+ * shifted, 2 BF16 shifted), decoded and summed in FP64; *result is device memory. */
+long long fc_lbm_mass_workspace_bytes(void);
+int fc_lbm_mass(const void* pop, int storage, const uint8_t* flags, long long n_cells, void* workspace,
+                long long workspace_bytes, double* result, void* stream);
+/* Heat balance of the thermal operator over the cells with mask != 0, in FP64:
+ * result3 = { sum src, sum L(T), sum T } with L the operator of the multigrid
+ * level's coefficients (L(T) summed is the net heat leaving through the
+ * boundaries, Dirichlet planes included); src may be NULL (0). */
+long long fc_mg_heat_balance_workspace_bytes(long long n);
+int fc_mg_heat_balance(const float* T, const float* src, const float* mask, const float* aE, const float* aW,
+                       const float* aN, const float* aS, const float* aU, const float* aD, const float* diagL, int nx,
+                       int ny, int nz, int ax, int out_idx, void* workspace, long long workspace_bytes,
+                       double* result3, void* stream);
+
 #ifdef __cplusplus
 }
 #endif
