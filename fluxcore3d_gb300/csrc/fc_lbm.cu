@@ -155,13 +155,13 @@ __device__ __forceinline__ long long plane_flat(int axis, int p, int a, int b, i
 // Second-order Hermite tensors Q = c c - I/3 use the reference's 8-digit literals.
 __device__ __forceinline__ float q_diag(int c) { return c != 0 ? 0.66666667f : -0.33333333f; }
 
-// Writes the node's new populations to f and, when out is given, to out too.
-__device__ void zou_he_node(float* __restrict__ f, long long N, long long flat_bc, long long flat_in,
-                            int axis, int plane_idx, int bc_type, float u_in, float rho_out, int sign,
-                            float* out = nullptr) {
-    float fi[19];
-#pragma unroll
-    for (int q = 0; q < 19; ++q) fi[q] = f[q * N + flat_bc];
+// The node's post-stream populations fi and, for a pressure outlet (bc_type 1,
+// whose both branches read it), those of its interior neighbour fin, loaded
+// by the caller so that every load of the node is in flight at once.  Writes
+// the node's new populations to f and, when out is given, to out too.
+__device__ __forceinline__ void zou_he_core(const float fi[19], const float fin[19], float* __restrict__ f,
+                                            long long N, long long flat_bc, int axis, int plane_idx, int bc_type,
+                                            float u_in, float rho_out, int sign, float* out) {
     const int unknown = (plane_idx == 0) ? 1 : -1;
     const int known = -unknown;
     float s0 = 0.f, sk = 0.f;
@@ -183,15 +183,11 @@ __device__ void zou_he_node(float* __restrict__ f, long long N, long long flat_b
         if (uax * (float)sign < 0.f) {
 #pragma unroll
             for (int q = 0; q < 19; ++q) {
-                const float v = f[q * N + flat_in];
-                f[q * N + flat_bc] = v;
-                if (out) out[q] = v;
+                f[q * N + flat_bc] = fin[q];
+                if (out) out[q] = fin[q];
             }
             return;
         }
-        float fin[19];
-#pragma unroll
-        for (int q = 0; q < 19; ++q) fin[q] = f[q * N + flat_in];
         const Macro mi = macros_of(fin);
         if (axis == 0) { ub = uax; vb = mi.uy; wb = mi.uz; }
         else if (axis == 1) { ub = mi.ux; vb = uax; wb = mi.uz; }
@@ -225,6 +221,24 @@ __device__ void zou_he_node(float* __restrict__ f, long long N, long long flat_b
         f[q * N + flat_bc] = v;
         if (out) out[q] = v;
     }
+}
+
+__device__ __forceinline__ void load_zou_he(const float* __restrict__ f, long long N, long long flat_bc,
+                                            long long flat_in, int bc_type, float fi[19], float fin[19]) {
+#pragma unroll
+    for (int q = 0; q < 19; ++q) fi[q] = f[q * N + flat_bc];
+    if (bc_type != 0) {
+#pragma unroll
+        for (int q = 0; q < 19; ++q) fin[q] = f[q * N + flat_in];
+    }
+}
+
+__device__ void zou_he_node(float* __restrict__ f, long long N, long long flat_bc, long long flat_in,
+                            int axis, int plane_idx, int bc_type, float u_in, float rho_out, int sign,
+                            float* out = nullptr) {
+    float fi[19], fin[19];
+    load_zou_he(f, N, flat_bc, flat_in, bc_type, fi, fin);
+    zou_he_core(fi, fin, f, N, flat_bc, axis, plane_idx, bc_type, u_in, rho_out, sign, out);
 }
 
 __global__ void __launch_bounds__(BLOCK) k_zou_he(
@@ -531,8 +545,10 @@ struct PlaneSet {
     int start[FC_MAX_PLANES + 1];
 };
 
+constexpr int PLANE_BLOCK = 128;     // plane work is a few thousand warps: spread it over every SM
+
 template <int KIND, int MODE>
-__global__ void __launch_bounds__(BLOCK) k_planes_zou_he_collide(const FusedArgs a, const PlaneSet ps) {
+__global__ void __launch_bounds__(PLANE_BLOCK) k_planes_zou_he_collide(const FusedArgs a, const PlaneSet ps) {
     const int t = blockIdx.x * blockDim.x + threadIdx.x;
     if (t >= ps.start[ps.n]) return;
     int p = 0;
@@ -542,9 +558,13 @@ __global__ void __launch_bounds__(BLOCK) k_planes_zou_he_collide(const FusedArgs
     const int pa = u / ps.n2[p], pb = u - (u / ps.n2[p]) * ps.n2[p];
     const int idx = (int)plane_flat(pl.axis, pl.plane_idx, pa, pb, a.g.ny, a.g.nz);
     const long long fi = plane_flat(pl.axis, pl.interior_idx, pa, pb, a.g.ny, a.g.nz);
-    if (a.flags[idx] & CF_SOLID) return;
+    // the flag byte and every population the node reads are requested together
+    const uint8_t fl = a.flags[idx];
+    float fb[19], fn[19];
+    load_zou_he(a.f32, a.g.N, idx, fi, pl.bc_type, fb, fn);
+    if (fl & CF_SOLID) return;
     float fv[19];
-    zou_he_node(a.f32, a.g.N, idx, fi, pl.axis, pl.plane_idx, pl.bc_type, pl.u_in_lat, pl.rho_out_lat, pl.sign,
+    zou_he_core(fb, fn, a.f32, a.g.N, idx, pl.axis, pl.plane_idx, pl.bc_type, pl.u_in_lat, pl.rho_out_lat, pl.sign,
                 fv);
     const int i = idx / a.g.nynz;
     const int rem = idx - i * a.g.nynz;
@@ -558,7 +578,8 @@ __global__ void __launch_bounds__(BLOCK) k_planes_zou_he_collide(const FusedArgs
 template <int S, int M>
 struct PlanesLauncher {
     static int go(const FusedArgs& a, cudaStream_t st, const PlaneSet& ps) {
-        k_planes_zou_he_collide<S, M><<<grid_for(ps.start[ps.n]), BLOCK, 0, st>>>(a, ps);
+        const unsigned nb = (unsigned)((ps.start[ps.n] + PLANE_BLOCK - 1) / PLANE_BLOCK);
+        k_planes_zou_he_collide<S, M><<<nb, PLANE_BLOCK, 0, st>>>(a, ps);
         return launch_status();
     }
 };
