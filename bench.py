@@ -514,8 +514,10 @@ def main():
         from fluxcore3d_gb300 import io_bench
         line["io"] = io_bench.run(dev)
     if rank == 0 and not args.no_learned:
-        from fluxcore3d_gb300 import learned_bench
+        from fluxcore3d_gb300 import conv_bench, learned_bench
         line["learned"] = learned_bench.run(dev, eval_seeds=(1001, 1002))
+        # the network's tcgen05 convolution alone: FLOP/s against the measured bf16 peak
+        line["learned"]["conv_fwd"] = conv_bench.run(dev, bf16_peak_tflops=peaks()[1])
     if rank == 0 and not args.no_accuracy:
         line["accuracy"] = accuracy_run(args, dev)
     if rank == 0 and not args.no_cpu:

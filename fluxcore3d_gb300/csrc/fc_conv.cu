@@ -26,6 +26,7 @@ namespace {
 constexpr int TM = 128;       // rows per CTA tile
 constexpr int KC = 64;        // K per chunk (4 MMAs of K = 16)
 constexpr int NTHR = 128;
+constexpr int STAGES = 2;     // shared-memory stages of the K loop (3 measured slower: fewer CTAs per SM)
 constexpr unsigned SPIN_LIMIT = 1u << 26;
 
 struct ConvGeom {
@@ -88,33 +89,58 @@ __device__ __forceinline__ void mma_commit(uint64_t* bar) {
 }
 
 // --------------------------------------------------------------------------
-// operand loaders: return 8 consecutive K elements (one 16-byte core-matrix row)
+// operand loaders.  Each returns 8 consecutive K elements (one 16-byte row of
+// a core matrix).  A loaders fill one tile row per thread (NTHR == TM): row()
+// decodes the row once per tile and chunk() fills the row's 8 vectors of one
+// 64-wide K chunk, so no chunk repeats the voxel decomposition.
 // --------------------------------------------------------------------------
-__device__ __forceinline__ bool nb_voxel(const ConvGeom& g, int v, int tap, int sgn, int& nv) {
-    const int dz = tap / 9 - 1, dy = (tap / 3) % 3 - 1, dx = tap % 3 - 1;
-    const int w = v % g.W;
-    const int h = (v / g.W) % g.H;
-    const int d = (v / (g.W * g.H)) % g.D;
-    const int d2 = d + sgn * dz, h2 = h + sgn * dy, w2 = w + sgn * dx;
-    if (d2 < 0 || d2 >= g.D || h2 < 0 || h2 >= g.H || w2 < 0 || w2 >= g.W) return false;
-    nv = v + sgn * ((dz * g.H + dy) * g.W + dx);
-    return true;
+__device__ __forceinline__ void tap_offsets(int tap, int& dz, int& dy, int& dx) {
+    dz = tap / 9 - 1;
+    dy = (tap / 3) % 3 - 1;
+    dx = tap % 3 - 1;
 }
 
-// forward / data-grad A: activations of the neighbour voxel (sgn = +1 forward)
+// forward / data-grad A: activations of the neighbour voxel v + o(tap), K = (tap, channel block)
 struct LoadActA {
     const __nv_bfloat16* X;
     ConvGeom g;
     int cin;
     int nvox;
-    __device__ uint4 operator()(int m, int k8) const {
-        uint4 z = make_uint4(0, 0, 0, 0);
+    struct Row {
+        int v, d, h, w;
+        bool ok;
+    };
+    __device__ Row row(int m) const {
+        Row r;
+        r.v = m;
+        r.ok = m < nvox;
+        r.w = m % g.W;
+        r.h = (m / g.W) % g.H;
+        r.d = (m / (g.W * g.H)) % g.D;
+        return r;
+    }
+    __device__ void chunk(const Row& r, int k8_0, uint4 out[KC / 8]) const {
+        const uint4 z = make_uint4(0, 0, 0, 0);
         const int cb = cin >> 3;
-        const int tap = k8 / cb;
-        if (m >= nvox || tap >= 27) return z;
-        int nv;
-        if (!nb_voxel(g, m, tap, 1, nv)) return z;
-        return __ldg(reinterpret_cast<const uint4*>(X + (long long)nv * cin + (k8 - tap * cb) * 8));
+        int tap = k8_0 / cb;
+        int cc = k8_0 - tap * cb;
+        int dz, dy, dx;
+        tap_offsets(tap, dz, dy, dx);
+        bool in = r.ok && tap < 27 && (unsigned)(r.d + dz) < (unsigned)g.D && (unsigned)(r.h + dy) < (unsigned)g.H &&
+                  (unsigned)(r.w + dx) < (unsigned)g.W;
+        long long base = (long long)(r.v + (dz * g.H + dy) * g.W + dx) * cin;
+#pragma unroll
+        for (int kb = 0; kb < KC / 8; ++kb) {
+            out[kb] = in ? __ldg(reinterpret_cast<const uint4*>(X + base + cc * 8)) : z;
+            if (++cc == cb) {
+                cc = 0;
+                ++tap;
+                tap_offsets(tap, dz, dy, dx);
+                in = r.ok && tap < 27 && (unsigned)(r.d + dz) < (unsigned)g.D &&
+                     (unsigned)(r.h + dy) < (unsigned)g.H && (unsigned)(r.w + dx) < (unsigned)g.W;
+                base = (long long)(r.v + (dz * g.H + dy) * g.W + dx) * cin;
+            }
+        }
     }
 };
 // weights [rows][kpad]
@@ -131,17 +157,42 @@ struct LoadWgradA {
     const __nv_bfloat16* X;
     ConvGeom g;
     int nvox;
-    __device__ uint4 operator()(int m, int k8) const {
-        __align__(16) __nv_bfloat16 e[8];
-        const int tap = m / g.cin, c = m - tap * g.cin;
+    struct Row {
+        int c, dz, dy, dx;
+        bool ok;
+    };
+    __device__ Row row(int m) const {
+        Row r;
+        const int tap = m / g.cin;
+        r.c = m - tap * g.cin;
+        r.ok = tap < 27;
+        tap_offsets(tap < 27 ? tap : 0, r.dz, r.dy, r.dx);
+        return r;
+    }
+    // the 64 voxels k8_0*8 .. k8_0*8+63 in order: decode the first, then step w with carries
+    __device__ void chunk(const Row& r, int k8_0, uint4 out[KC / 8]) const {
+        int v = k8_0 * 8;
+        int w = v % g.W, h = (v / g.W) % g.H, d = (v / (g.W * g.H)) % g.D;
+        const int off = (r.dz * g.H + r.dy) * g.W + r.dx;
 #pragma unroll
-        for (int t = 0; t < 8; ++t) {
-            const int v = k8 * 8 + t;
-            int nv;
-            e[t] = (tap < 27 && v < nvox && nb_voxel(g, v, tap, 1, nv)) ? X[(long long)nv * g.cin + c]
-                                                                         : __float2bfloat16(0.f);
+        for (int kb = 0; kb < KC / 8; ++kb) {
+            __align__(16) __nv_bfloat16 e[8];
+#pragma unroll
+            for (int t = 0; t < 8; ++t) {
+                const bool in = r.ok && v < nvox && (unsigned)(d + r.dz) < (unsigned)g.D &&
+                                (unsigned)(h + r.dy) < (unsigned)g.H && (unsigned)(w + r.dx) < (unsigned)g.W;
+                e[t] = in ? X[(long long)(v + off) * g.cin + r.c] : __float2bfloat16(0.f);
+                ++v;
+                if (++w == g.W) {
+                    w = 0;
+                    if (++h == g.H) {
+                        h = 0;
+                        if (++d == g.D) d = 0;
+                    }
+                }
+            }
+            out[kb] = *reinterpret_cast<uint4*>(e);
         }
-        return *reinterpret_cast<uint4*>(e);
     }
 };
 // weight-grad B: rows n, K = voxels: dY[v][n]
@@ -177,12 +228,12 @@ template <class LA, class LB>
 __device__ void gemm_tile(const LA& la, const LB& lb, int m0, int N, int k8_begin, int nchunks, const Epi& ep,
                           unsigned* err) {
     extern __shared__ __align__(1024) unsigned char smem[];
-    // layout: [stage 0 A | stage 0 B | stage 1 A | stage 1 B] then mbarriers + tmem slot
+    // layout: STAGES x [A | B] then STAGES mbarriers + tmem slot
     const int a_bytes = TM * KC * 2;
     const int b_bytes = N * KC * 2;
     const int stage_bytes = a_bytes + b_bytes;
-    uint64_t* bars = reinterpret_cast<uint64_t*>(smem + 2 * stage_bytes);
-    uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(bars + 2);
+    uint64_t* bars = reinterpret_cast<uint64_t*>(smem + STAGES * stage_bytes);
+    uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(bars + STAGES);
     __shared__ int s_abort;
     const int tid = threadIdx.x;
     const int warp = tid >> 5;
@@ -190,8 +241,7 @@ __device__ void gemm_tile(const LA& la, const LB& lb, int m0, int N, int k8_begi
     while (ncols < N) ncols <<= 1;
 
     if (tid == 0) {
-        mbar_init(&bars[0], 1);
-        mbar_init(&bars[1], 1);
+        for (int b = 0; b < STAGES; ++b) mbar_init(&bars[b], 1);
         s_abort = 0;
         asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
     }
@@ -205,24 +255,29 @@ __device__ void gemm_tile(const LA& la, const LB& lb, int m0, int N, int k8_begi
     asm volatile("tcgen05.fence::after_thread_sync;");
     const uint32_t tmem = *tmem_slot;
     const uint32_t idesc = make_idesc(TM, N);
+    static_assert(NTHR == TM, "one A row per thread");
+    const typename LA::Row ra = la.row(m0 + tid);
 
     for (int c = 0; c < nchunks; ++c) {
-        const int s = c & 1;
+        const int s = c % STAGES;
         unsigned char* As = smem + s * stage_bytes;
         unsigned char* Bs = As + a_bytes;
-        if (c >= 2) {
-            if (!mbar_wait(&bars[s], ((c - 2) >> 1) & 1)) {
+        if (c >= STAGES) {
+            if (!mbar_wait(&bars[s], ((c - STAGES) / STAGES) & 1)) {
                 if (err) atomicOr(err, 4u);
                 s_abort = 1;
             }
         }
         __syncthreads();
         if (s_abort) break;
-        // gather: A rows [TM] x 8 core columns; core (mb, kb) at kb*(TM/8)*128 + mb*128 + (row%8)*16
-        for (int t = tid; t < TM * (KC / 8); t += NTHR) {
-            const int row = t % TM, kb = t / TM;
-            const uint4 v = la(m0 + row, k8_begin + c * (KC / 8) + kb);
-            *reinterpret_cast<uint4*>(As + kb * (TM / 8) * 128 + (row >> 3) * 128 + (row & 7) * 16) = v;
+        // gather: A rows [TM] x 8 core columns; core (mb, kb) at kb*(TM/8)*128 + mb*128 + (row%8)*16;
+        // thread tid fills row tid
+        {
+            uint4 v[KC / 8];
+            la.chunk(ra, k8_begin + c * (KC / 8), v);
+#pragma unroll
+            for (int kb = 0; kb < KC / 8; ++kb)
+                *reinterpret_cast<uint4*>(As + kb * (TM / 8) * 128 + (tid >> 3) * 128 + (tid & 7) * 16) = v[kb];
         }
         for (int t = tid; t < N * (KC / 8); t += NTHR) {
             const int row = t % N, kb = t / N;
@@ -247,7 +302,7 @@ __device__ void gemm_tile(const LA& la, const LB& lb, int m0, int N, int k8_begi
     // wait for the last chunk's MMAs (commit covers all earlier ones)
     if (!s_abort && nchunks > 0) {
         const int c = nchunks - 1;
-        if (!mbar_wait(&bars[c & 1], (c >> 1) & 1)) {
+        if (!mbar_wait(&bars[c % STAGES], (c / STAGES) & 1)) {
             if (err) atomicOr(err, 4u);
             s_abort = 1;
         }
@@ -266,16 +321,33 @@ __device__ void gemm_tile(const LA& la, const LB& lb, int m0, int N, int k8_begi
                          : "r"(taddr));
             asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
             if (row < ep.rows) {
+                float v[8];
 #pragma unroll
                 for (int t = 0; t < 8; ++t) {
-                    const int n = n0 + t;
-                    if (n >= ep.nvalid) continue;
-                    float v = __uint_as_float(r[t]);
-                    if (ep.bias) v += ep.bias[n];
-                    if (ep.relu) v = fmaxf(v, 0.f);
-                    const long long o = (ep.row_offset + row) * (long long)ep.ldo + n;
-                    if (ep.out_f32) ep.out_f32[o] = v;
-                    if (ep.out_bf16) ep.out_bf16[o] = __float2bfloat16_rn(v);
+                    v[t] = __uint_as_float(r[t]);
+                    if (ep.bias && n0 + t < ep.nvalid) v[t] += ep.bias[n0 + t];
+                    if (ep.relu) v[t] = fmaxf(v[t], 0.f);
+                }
+                const long long o = (ep.row_offset + row) * (long long)ep.ldo + n0;
+                if (n0 + 8 <= ep.nvalid && (ep.ldo & 7) == 0) {
+                    // 16-byte stores of whole 8-column groups (rows are 16-byte aligned)
+                    if (ep.out_f32) {
+                        *reinterpret_cast<float4*>(ep.out_f32 + o) = make_float4(v[0], v[1], v[2], v[3]);
+                        *reinterpret_cast<float4*>(ep.out_f32 + o + 4) = make_float4(v[4], v[5], v[6], v[7]);
+                    }
+                    if (ep.out_bf16) {
+                        __align__(16) __nv_bfloat162 b[4];
+#pragma unroll
+                        for (int t = 0; t < 4; ++t) b[t] = __floats2bfloat162_rn(v[2 * t], v[2 * t + 1]);
+                        *reinterpret_cast<uint4*>(ep.out_bf16 + o) = *reinterpret_cast<const uint4*>(b);
+                    }
+                } else {
+#pragma unroll
+                    for (int t = 0; t < 8; ++t) {
+                        if (n0 + t >= ep.nvalid) continue;
+                        if (ep.out_f32) ep.out_f32[o + t] = v[t];
+                        if (ep.out_bf16) ep.out_bf16[o + t] = __float2bfloat16_rn(v[t]);
+                    }
                 }
             }
         }
@@ -325,9 +397,9 @@ __global__ void k_flip_weights(const __nv_bfloat16* __restrict__ W, __nv_bfloat1
 }
 
 inline size_t smem_bytes(int N) {
-    // two stages + barriers, plus 32 KB of slack past the last operand byte so that no
+    // the stages + barriers, plus 32 KB of slack past the last operand byte so that no
     // descriptor stride read can leave the allocation
-    size_t b = 2 * (size_t)(TM * KC * 2 + N * KC * 2) + 64 + 32768;
+    size_t b = STAGES * (size_t)(TM * KC * 2 + N * KC * 2) + 8 * (STAGES + 1) + 32768;
     int ncols = 32;
     while (ncols < N) ncols <<= 1;
     // keep (CTAs per SM) x ncols <= 512 TMEM columns: make the smem footprint cap residency
