@@ -101,6 +101,7 @@ SIGNATURES: dict[str, tuple] = {
     "fc_lbm_fused_step": (i32, [C.POINTER(StepArgs), vp]),
     "fc_lbm_link_gather": (i32, [C.POINTER(StepArgs), vp, C.c_int64, i32, vp]),
     "fc_lbm_planes_zou_he_collide": (i32, [C.POINTER(StepArgs), C.POINTER(PlaneBC), i32, vp]),
+    "fc_lbm_wait_selftest": (i32, [C.c_uint, i32, vp, vp]),
     "fc_lbm_tile_links": (C.c_int64, [C.POINTER(StepArgs), vp, C.c_int64, vp, C.c_int64, vp, C.c_int64, vp]),
     "fc_lbm_collide_from_f32": (i32, [C.POINTER(StepArgs), i32, i32, vp]),
     "fc_lbm_materialize": (i32, [C.POINTER(StepArgs), vp]),

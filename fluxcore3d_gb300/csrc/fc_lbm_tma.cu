@@ -110,8 +110,8 @@ __device__ __forceinline__ void bar_expect_tx(uint32_t bar, uint32_t bytes) {
     asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(bar), "r"(bytes) : "memory");
 }
 
-__device__ __forceinline__ bool bar_wait(uint32_t bar, unsigned parity) {
-    for (unsigned it = 0; it < TS_SPIN; ++it) {
+__device__ __forceinline__ bool bar_wait(uint32_t bar, unsigned parity, unsigned limit = TS_SPIN) {
+    for (unsigned it = 0; it < limit; ++it) {
         uint32_t done;
         asm volatile(
             "{\n\t.reg .pred p;\n\t"
@@ -647,6 +647,24 @@ int launch_typed(const FusedArgs& a, const CUtensorMap& tp, const CUtensorMap& t
     return launch_status();
 }
 
+// The pass's bounded mbarrier wait on its own: one warp waits on a barrier of
+// arrival count 1.  With arrive == 0 nothing arrives, so the wait gives up after
+// `polls` polls and the kernel records DEV_ERR_TIMEOUT and returns; with
+// arrive == 1 lane 0 arrives first and the wait completes.
+__global__ void k_wait_selftest(unsigned polls, int arrive, unsigned* status) {
+    __shared__ __align__(8) uint64_t bar;
+    const uint32_t b = su32(&bar);
+    if (threadIdx.x == 0) {
+        bar_init(b, 1);
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    }
+    __syncwarp();
+    if (arrive && threadIdx.x == 0) asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(b) : "memory");
+    __syncwarp();
+    const bool ok = __all_sync(0xffffffffu, bar_wait(b, 0u, polls));
+    if (!ok && threadIdx.x == 0) atomicOr(status, DEV_ERR_TIMEOUT);
+}
+
 }  // namespace
 
 bool fused_tma_eligible(const FusedArgs& a, int storage) {
@@ -735,3 +753,9 @@ int launch_fused_tma(const FusedArgs& a, int storage, int collision, cudaStream_
 }
 
 }  // namespace fc
+
+extern "C" int fc_lbm_wait_selftest(unsigned polls, int arrive, unsigned* status, void* stream) {
+    if (!status || polls < 1) return fc::FC_ERR_ARG;
+    fc::k_wait_selftest<<<1, 32, 0, (cudaStream_t)stream>>>(polls, arrive, status);
+    return fc::launch_status();
+}

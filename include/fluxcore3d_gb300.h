@@ -170,6 +170,14 @@ long long fc_lbm_tile_links(const fc_lbm_step_args* args, int32_t* records, long
 int fc_lbm_link_gather(const fc_lbm_step_args* args, const int32_t* subset, long long n_subset, int skip_marked,
                        void* stream);
 
+/* Failure-detection check of the staged pass's bounded mbarrier wait (the
+ * helper every wait of k_fused_tma uses), in a one-warp kernel: with arrive == 0
+ * nothing arrives on the barrier, the wait gives up after `polls` polls, and the
+ * kernel sets bit 4 (timeout) in *status and returns, leaving the context
+ * usable; with arrive == 1 the phase completes and *status is not touched.
+ * No reference counterpart (the reference has no bounded device waits). */
+int fc_lbm_wait_selftest(unsigned polls, int arrive, unsigned* status, void* stream);
+
 /* One inlet/outlet plane with a node-local (Zou/He) boundary condition. */
 typedef struct {
     int32_t axis, plane_idx, interior_idx, bc_type;   /* bc_type 0 velocity, 1 pressure (as fc_lbm_zou_he_bc) */

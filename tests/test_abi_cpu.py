@@ -47,6 +47,7 @@ def test_argument_checks_return_status_without_gpu(native_lib):
     args = _lib.StepArgs()
     args.storage = 7
     assert native_lib.fc_lbm_fused_step(args, None) == 1
+    assert native_lib.fc_lbm_wait_selftest(16, 0, None, None) == 1
 
 
 def test_face_roles_table():

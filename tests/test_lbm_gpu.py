@@ -158,6 +158,27 @@ def test_fused_planes_and_concurrent_gather_bit_identical(cuda, monkeypatch):
         assert np.array_equal(a, b)
 
 
+def test_bounded_mbarrier_wait_times_out_and_context_survives(cuda):
+    """Failure detection without a GPU fault: the staged pass's bounded mbarrier wait gives up
+    when nothing arrives and reports the timeout bit (4) to the host; with an arrival it completes;
+    the context stays usable (a lattice step runs and matches the oracle afterwards)."""
+    from fluxcore3d_gb300 import _lib
+    from fluxcore3d_gb300._torch import ptr, stream_ptr
+    status = torch.zeros(1, dtype=torch.int32, device=cuda)
+    _lib.call("fc_lbm_wait_selftest", 1024, 0, ptr(status), stream_ptr())
+    torch.cuda.synchronize()
+    assert int(status.item()) == 4
+    status.zero_()
+    _lib.call("fc_lbm_wait_selftest", 1024, 1, ptr(status), stream_ptr())
+    torch.cuda.synchronize()
+    assert int(status.item()) == 0
+    sim = cases.channel_cube(device=cuda, collision="bgk", nx=24, ny=12, nz=10, cube=4, cube_x=8,
+                             outlet="pressure")
+    orc = run_pair(sim, 20)
+    N = sim.nx * sim.ny * sim.nz
+    assert rel_l2(sim.f.reshape(19, N).cpu().numpy(), orc.f) < 1e-5
+
+
 def test_fused_step_c1_channel_1000_steps(cuda):
     """Plain method, small channel (64x32x32, BGK FP32, convective outlet, cube IBB): 1000 steps."""
     sim = cases.channel_cube(device=cuda, collision="bgk")
