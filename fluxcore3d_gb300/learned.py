@@ -11,7 +11,7 @@ the output rescaled, so z(a r) = a z(r) for a > 0.  Conductivity enters as
 (log k - k_shift) * k_scale.
 
 The reference solver has no learned component; the plain geometric multigrid
-remains the fallback inside fgmres_mg_f64 (`stall_fallback`) and the judge of
+remains the fallback inside fgmres_mg_f64 (`stall_fallback`) and the arbiter of
 convergence (the FP64 true residual).
 """
 from __future__ import annotations

@@ -1,4 +1,4 @@
-"""Build the oracle's C restatement (TEST INFRASTRUCTURE: checker and CPU baseline only).
+"""Build the oracle's C restatement (TEST INFRASTRUCTURE: parity oracle and CPU baseline only).
 
 Produces oracle/_build/liboracle_lbm_f32.so and liboracle_lbm_f64.so from
 oracle/lbm_oracle.c with gcc.  -ffp-contract=off keeps the arithmetic

@@ -1,6 +1,6 @@
 """CPU restatement of the geometry set-up for interpolated bounce-back.
 
-TEST INFRASTRUCTURE ONLY: the checker that the device kernels are compared
+TEST INFRASTRUCTURE ONLY: the oracle that the device kernels are compared
 with.  Nothing on the product path imports it.
 
   signed_edt        build_phi_from_voxel_mask_mm (pre_post/sdf_tracing.py:312-340):

@@ -1,7 +1,7 @@
 /*
  * lbm_oracle.c -- TEST INFRASTRUCTURE ONLY.  A plain-C restatement of the
  * reference's CUDA-path lattice kernels (fluxcore3D solver/lbm_kernels.cu),
- * used by the tests as the parity checker and by bench.py as the timed CPU
+ * used by the tests as the parity oracle and by bench.py as the timed CPU
  * baseline.  The product library never links or calls this code.
  *
  * Compiled twice by oracle/build_oracle.py: REAL=float (FP32 parity oracle)

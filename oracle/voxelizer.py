@@ -1,6 +1,6 @@
 """CPU restatement of the reference's ray-parity STL voxelizer and body stamp.
 
-TEST INFRASTRUCTURE ONLY: the checker the device kernels are compared with.
+TEST INFRASTRUCTURE ONLY: the oracle the device kernels are compared with.
 
   grid                gpu_voxelize_mesh's grid (pre_post/gpu_voxelizer.py:103-110):
                       origin = min corner - pitch/2 (FP32), n = ceil(extent/pitch) + 2
