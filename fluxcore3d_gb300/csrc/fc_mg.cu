@@ -455,6 +455,26 @@ __global__ void __launch_bounds__(PAIR_X * PAIR_Y) k_prolong2(float* __restrict_
                       prolong_cell(xc, cy, cz, i, j, k + 1, cx, xv.y, m.y, alpha));
 }
 
+// k_prolong_2to1 on four cells (k .. k+3) per thread (nz a multiple of 4):
+// float4 update of x and float4 mask, the same interpolation per cell; the four
+// cells read coarse columns m-1 .. m+2 of their two planes and two rows, which
+// the compiler loads once for all four.
+__global__ void __launch_bounds__(PAIR_X * PAIR_Y) k_prolong4(float* __restrict__ x, const float* __restrict__ xc,
+                                                              const float* __restrict__ mask, int nx, int ny, int nz,
+                                                              int cx, int cy, int cz, float alpha) {
+    const int k = 4 * (blockIdx.x * PAIR_X + threadIdx.x);
+    const int j = blockIdx.y * PAIR_Y + threadIdx.y;
+    const int i = blockIdx.z;
+    if (k >= nz || j >= ny) return;
+    const int idx = (i * ny + j) * nz + k;
+    float4* xp = reinterpret_cast<float4*>(x + idx);
+    const float4 xv = *xp, m = __ldg(reinterpret_cast<const float4*>(mask + idx));
+    *xp = make_float4(prolong_cell(xc, cy, cz, i, j, k, cx, xv.x, m.x, alpha),
+                      prolong_cell(xc, cy, cz, i, j, k + 1, cx, xv.y, m.y, alpha),
+                      prolong_cell(xc, cy, cz, i, j, k + 2, cx, xv.z, m.z, alpha),
+                      prolong_cell(xc, cy, cz, i, j, k + 3, cx, xv.w, m.w, alpha));
+}
+
 // per-block partial sums of (w * (b - M x))^2 in FP64, w = mask or 1
 __global__ void __launch_bounds__(BLOCK) k_residual_sq(const float* __restrict__ x, const float* __restrict__ b,
                                                        const float* __restrict__ mask, Coef a, float dt, Lvl g,
@@ -734,7 +754,14 @@ int fc_mg_prolong_correct(float* x, const float* x_coarse, const float* mask, in
     if ((long long)nx * ny * nz >= (1LL << 31)) return FC_ERR_ARG;
     if (nx == 2 * cx && ny == 2 * cy && nz == 2 * cz) {
         const Lvl g{nx, ny, nz, 0, 0};
-        if (pair_ok(g, {x, mask})) {
+        if (nz >= 4 * PAIR_X && nz % 4 == 0 && pair_ok(g, {x, mask}) &&
+            !((reinterpret_cast<uintptr_t>(x) | reinterpret_cast<uintptr_t>(mask)) & 15)) {
+            // whole warps of four cells per thread on the wide levels
+            const dim3 grid((unsigned)((nz + 4 * PAIR_X - 1) / (4 * PAIR_X)), (unsigned)((ny + PAIR_Y - 1) / PAIR_Y),
+                            (unsigned)nx);
+            k_prolong4<<<grid, dim3(PAIR_X, PAIR_Y), 0, (cudaStream_t)stream>>>(x, x_coarse, mask, nx, ny, nz, cx, cy,
+                                                                              cz, alpha);
+        } else if (pair_ok(g, {x, mask})) {
             k_prolong2<<<pair_grid(g), dim3(PAIR_X, PAIR_Y), 0, (cudaStream_t)stream>>>(x, x_coarse, mask, nx, ny, nz,
                                                                                        cx, cy, cz, alpha);
         } else {
