@@ -249,3 +249,29 @@ def test_thermal_pseudo_time_steps_match_oracle(cuda):
         assert float(np.abs(got - T).max()) <= 8 * float(np.spacing(np.float32(32.0))) + 1e-5 * rise, it
     assert np.isfinite(info["r_rel"])
 
+
+
+def test_prolongation_four_and_two_cells_per_thread_bit_identical(cuda):
+    """fc_mg_prolong_correct takes four cells per thread on 16-byte aligned levels with nz >= 128
+    and two cells per thread on 8-byte aligned ones: the same interpolation, the same bits."""
+    from fluxcore3d_gb300 import _lib
+    from fluxcore3d_gb300._torch import ptr, stream_ptr
+    nx, ny, nz = 16, 12, 128
+    N = nx * ny * nz
+    g = torch.Generator(device="cpu").manual_seed(3)
+    xc = torch.randn((nx // 2) * (ny // 2) * (nz // 2), generator=g).to(cuda)
+    x0 = torch.randn(N, generator=g).to(cuda)
+    m0 = (torch.rand(N, generator=g) > 0.2).float().to(cuda)
+    out = []
+    for off in (0, 2):   # float offset 0: 16-byte aligned; 2: 8-byte aligned only
+        bx = torch.zeros(N + 4, device=cuda)
+        bm = torch.zeros(N + 4, device=cuda)
+        x, m = bx[off:off + N], bm[off:off + N]
+        x.copy_(x0)
+        m.copy_(m0)
+        _lib.call("fc_mg_prolong_correct", ptr(x), ptr(xc), ptr(m), nx, ny, nz, nx // 2, ny // 2, nz // 2, 0.6,
+                  stream_ptr())
+        torch.cuda.synchronize()
+        out.append(x.clone())
+    assert torch.equal(out[0].view(torch.int32), out[1].view(torch.int32))
+    assert not torch.equal(out[0], x0)
