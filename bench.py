@@ -37,7 +37,7 @@ RESULT_OUT = sys.stdout
 sys.path.insert(0, ROOT)
 
 METRIC = "D3Q19 CHT MLUPS + thermal ms to 1e-8 residual, mixed/learned vs plain, 1 GB300"
-WORKLOAD = "pin-fin heat sink 256x128x128, MRT + Bouzidi IBB, FP16 shifted populations"
+WORKLOAD = "pin-fin heat sink 256x128x128 (16x8 pins r=3.5 h=80, seed 1), MRT + Bouzidi IBB, u=0.08, Re=200"
 
 
 def peaks():
@@ -130,13 +130,48 @@ def dist_env():
     return ws, rank, local
 
 
-def setup_device():
-    """Where the CPU legs build their inputs: the geometry set-up (links, fractions) runs on the GPU;
-    only the timed oracle steps run on the host cores."""
+def host_case(args):
+    """The workload's lattice state built on the host cores alone, for the CPU legs: the same level
+    set, mask and initial state as the device case, links from the oracle's link builder, fractions
+    by the same FP64 bisection of the analytic level set on the CPU, Bouzidi weights from the oracle.
+    No device library is loaded on this path."""
     import torch
-    if not torch.cuda.is_available():
-        raise RuntimeError("the CPU baseline builds its case with the device geometry kernels: a GPU is required")
-    return "cuda"
+    from fluxcore3d_gb300 import case as cases
+    from fluxcore3d_gb300 import geometry as geo
+    from oracle import geometry as og
+
+    def host_ibb(solid, G):
+        s = solid.cpu().numpy()
+        ff, di, do, fff, fv = og.links_from_mask(s)
+        q = geo.level_set_fractions(G, torch.from_numpy(ff), torch.from_numpy(di), s.shape).numpy()
+        ge, w1, w2 = og.weights_from_q(q)
+        t = torch.from_numpy
+        return geo.IBBData(int(ff.size), t(ff), t(di), t(do), t(ge), t(w1), t(w2), t(fff), t(fv))
+
+    sim = cases.pin_fin(device="cpu", collision=args.collision, storage="fp32", nx=args.nx, ny=args.ny, nz=args.nz,
+                        ibb_builder=host_ibb)
+    return sim
+
+
+def oracle_of(sim, real="f32"):
+    """The oracle lattice started from the case's state."""
+    from oracle.lbm import OracleLBM
+    d = sim.ibb_data
+    links = {k: getattr(d, k).cpu().numpy() for k in
+             ("fluid_flat", "dir_i", "dir_opp", "w_i", "w_second", "q_ge_half", "ff_flat", "ff_valid")}
+    return OracleLBM(sim.nx, sim.ny, sim.nz, sim.f.cpu().numpy(), sim.solid_flow.cpu().numpy(),
+                     collision=sim.cfg.collision, omega=float(sim.omega_plus),
+                     S=sim._mrt_S.cpu().numpy() if hasattr(sim, "_mrt_S") else None,
+                     sigma=sim._sponge_sigma.cpu().numpy() if sim.cfg.sponge_length > 0 else None, links=links,
+                     domain_walls=sim.cfg.domain_walls, u_in_lat=sim.u_in_lat, real=real)
+
+
+def bench_config(args):
+    """The `config` object both arms print (one workload, whatever the storage precision)."""
+    return {"workload": WORKLOAD, "cells": args.nx * args.ny * args.nz, "collision": args.collision,
+            "macro_stride": args.macro_stride,
+            "l2_flush": "inputs larger than L2 (2 x 159 MB FP16 / 2 x 319 MB FP32 populations)",
+            "parallelism": "replicas"}
 
 
 def make_case(device, storage, args):
@@ -174,40 +209,77 @@ def lbm_traffic(sim, fc, storage_bytes):
             "n_fluid": int(fluid.sum())}
 
 
-def time_steps(sim, steps):
-    """Total device time (ms) of `steps` solver steps, CUDA events on the current stream."""
+class Restarter:
+    """Keeps a timed lattice run inside its physically valid start-up window: plain MRT on the
+    pin fin at Re = 200 diverges after about 600 steps (FP32 and FP64 alike), so before a block of
+    steps would take the run past `max_age` steps since its start, the state is reset to the
+    initial populations (outside the timed region; the engine is re-primed there too).  The cost
+    of a step does not depend on the state, only on the geometry."""
+
+    def __init__(self, sim, max_age):
+        self.sim = sim
+        self.max_age = int(max_age)
+        self.f0 = sim.f.detach().clone()
+        self.age = 0
+        self.restarts = 0
+
+    def before(self, steps):
+        if self.max_age <= 0 or self.age + steps <= self.max_age:
+            self.age += steps
+            return
+        self.sim.f.copy_(self.f0)
+        self.sim._fc.invalidate()
+        self.sim._fc._prime()
+        self.age = steps
+        self.restarts += 1
+
+
+def time_steps(sim, steps, dev, min_seconds=1.0, ws=1, restarter=None):
+    """Device time (ms) of `steps` solver steps, CUDA events on the current stream.  One untimed
+    block of `steps` steps sizes the count R of timed blocks so that they add up to at least
+    `min_seconds` (long enough for the clock sampler); every rank then times the same R blocks,
+    each bracketed by a barrier and a synchronize.  Returns the median block time and R."""
     import torch
     st = torch.cuda.current_stream()
-    t0 = torch.cuda.Event(enable_timing=True)
-    t1 = torch.cuda.Event(enable_timing=True)
+    if restarter:
+        restarter.before(steps)
     torch.cuda.synchronize()
-    t0.record(st)
+    t = time.perf_counter()
     for _ in range(steps):
         sim.step(do_thermal=False)
-    t1.record(st)
     torch.cuda.synchronize()
-    return t0.elapsed_time(t1)
+    est = max(time.perf_counter() - t, 1e-6)
+    reps = torch.tensor([max(1, min(20000, int(min_seconds / est) + 1))], device=dev)
+    if ws > 1:
+        torch.distributed.all_reduce(reps, op=torch.distributed.ReduceOp.MAX)
+    blocks = []
+    for _ in range(int(reps)):
+        if restarter:
+            restarter.before(steps)
+        t0 = torch.cuda.Event(enable_timing=True)
+        t1 = torch.cuda.Event(enable_timing=True)
+        if ws > 1:
+            torch.distributed.barrier()
+        torch.cuda.synchronize()
+        t0.record(st)
+        for _ in range(steps):
+            sim.step(do_thermal=False)
+        t1.record(st)
+        torch.cuda.synchronize()
+        blocks.append(t0.elapsed_time(t1))
+    return statistics.median(blocks), len(blocks)
 
 
 def run_reference(args):
-    """CPU baseline: the oracle's C restatement of the reference step on all host cores."""
+    """CPU baseline: the oracle's C restatement of the reference step on all host cores, with the
+    case built on the host (nothing of the device library is loaded)."""
     ws, rank, _ = dist_env()
     if rank != 0:
         return
-    import numpy as np
-    import torch
-    from oracle.lbm import OracleLBM
-    sim = make_case(setup_device(), "fp32", args)
-    d = sim.ibb_data
-    links = {k: getattr(d, k).cpu().numpy() for k in
-             ("fluid_flat", "dir_i", "dir_opp", "w_i", "w_second", "q_ge_half", "ff_flat", "ff_valid")}
     cores = os.cpu_count() or 1
     os.environ.setdefault("OMP_NUM_THREADS", str(cores))
-    orc = OracleLBM(sim.nx, sim.ny, sim.nz, sim.f.cpu().numpy(), sim.solid_flow.cpu().numpy(),
-                    collision=args.collision, omega=float(sim.omega_plus),
-                    S=sim._mrt_S.cpu().numpy() if hasattr(sim, "_mrt_S") else None,
-                    sigma=sim._sponge_sigma.cpu().numpy() if sim.cfg.sponge_length > 0 else None, links=links,
-                    domain_walls=sim.cfg.domain_walls, u_in_lat=sim.u_in_lat, real="f32")
+    sim = host_case(args)
+    orc = oracle_of(sim)
     orc.step(args.warmup)
     t = time.perf_counter()
     orc.step(args.steps)
@@ -218,25 +290,23 @@ def run_reference(args):
         "impl": "reference", "metric": METRIC, "value": round(v, 3), "unit": "MLUPS", "n_gpus": ws,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(dt * 1e3 / args.steps, 3),
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
-        "data": "synthetic", "config": {"workload": WORKLOAD.replace("FP16 shifted", "FP32"),
-                                        "cells": N, "l2_flush": "inputs larger than L2"},
+        "data": "synthetic", "config": bench_config(args),
         "cpu_baseline": {"value": round(v, 3), "unit": "MLUPS", "cores": cores, "kind": "port",
-                         "sample": f"{args.steps} full steps of the 256x128x128 workload (oracle C, OpenMP)"},
+                         "sample": f"{args.steps} full steps of the 256x128x128 workload with FP32 populations "
+                                   f"(oracle C restatement of the reference's CUDA-path step, OpenMP)"},
         "e2e": {"value": round(v, 3), "unit": "MLUPS", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
     print(json.dumps(line), file=RESULT_OUT, flush=True)
 
 
-ACC_CASE = dict(nx=128, ny=64, nz=64, n_pins=(8, 4), height=40, base=4, sponge_length=20)
-
-
-def _velocity_from_f(f, shape):
-    """(u, v, w) in FP64 from populations [19, N] (post-stream state)."""
-    import numpy as np
+def _velocity_of(sim):
+    """(3, N) FP64 velocity of the fused engine's current post-stream populations, on the device."""
+    import torch
     from fluxcore3d_gb300.geometry import C_NP
-    f = np.asarray(f, dtype=np.float64).reshape(19, -1)
-    rho = f.sum(0)
-    return [(C_NP[:, a].astype(np.float64) @ f / rho).reshape(shape) for a in range(3)]
+    sim.sync_f()
+    f = sim.f.reshape(19, -1).double()
+    c = torch.tensor(C_NP, dtype=torch.float64, device=f.device)
+    return (c.t() @ f) / f.sum(0)
 
 
 def _wall_heat(T, k, solid, D):
@@ -266,88 +336,91 @@ def _wall_heat(T, k, solid, D):
 
 
 def accuracy_run(args, dev):
-    """FP16- and FP32-storage GPU runs against an FP64 run of the plain method (the CPU oracle in
-    double precision) from the same initial state on a reduced pin fin (128x64x64, 8x4 pins of
-    radius 3.5 and height 40, MRT, analytic link fractions): velocity error after `accuracy_steps`
-    steps, then the thermal system of each velocity field solved to a 1e-10 FP64 residual, and the
-    temperature, wall heat flow and Nusselt number of each against the FP64 run's."""
-    import numpy as np
+    """FP32-, FP16- and BF16-storage runs of the fused engine against an FP64 run of the plain method
+    (fluxcore3d_gb300.lattice64: the reference step sequence in double precision on the device), from
+    the same initial state, on the full 256x128x128 pin fin with MRT-Smagorinsky, to steady state
+    (`accuracy_steps` steps): velocity error, then the thermal system of each velocity field solved to a
+    1e-10 FP64 residual, and the temperature, wall heat flow and Nusselt number of each against the
+    FP64 run's.  Plain MRT at this Reynolds number does not reach a steady state (it diverges in FP32
+    and FP64 alike after about 600 steps), so the steady-state comparison uses the reference's own
+    default collision, MRT with the Smagorinsky model."""
     import torch
     from fluxcore3d_gb300 import case as cases
     from fluxcore3d_gb300 import thermal_bench
     from fluxcore3d_gb300.diagnostics import heat_balance, lbm_mass
+    from fluxcore3d_gb300.lattice64 import Lattice64
     from fluxcore3d_gb300.solver import mg_pcg
     from fluxcore3d_gb300.solver.lbm_cuda_ext import LBMCUDAUpgrade
-    from oracle.lbm import OracleLBM
     steps = args.accuracy_steps
-    ref = cases.pin_fin(device=dev, storage="fp32", **ACC_CASE)
-    shape = (ref.nx, ref.ny, ref.nz)
-    d = ref.ibb_data
-    links = {k: getattr(d, k).cpu().numpy() for k in
-             ("fluid_flat", "dir_i", "dir_opp", "w_i", "w_second", "q_ge_half", "ff_flat", "ff_valid")}
-    t = time.perf_counter()
-    orc = OracleLBM(ref.nx, ref.ny, ref.nz, ref.f.cpu().numpy(), ref.solid_flow.cpu().numpy(), collision="mrt",
-                    omega=float(ref.omega_plus), S=ref._mrt_S.cpu().numpy(), sigma=ref._sponge_sigma.cpu().numpy(),
-                    links=links, domain_walls=ref.cfg.domain_walls, u_in_lat=ref.u_in_lat, real="f64")
-    orc.step(steps)
-    fp64_s = time.perf_counter() - t
-    vel = {"fp64": _velocity_from_f(orc.f, shape)}
-    mass = {}
-    for storage in ("fp32", "fp16"):
-        sim = cases.pin_fin(device=dev, storage=storage, **ACC_CASE)
-        sim.cfg.macro_stride = 1
+    shape = (args.nx, args.ny, args.nz)
+    sims = {}
+    for storage in ("fp32", "fp16", "bf16"):
+        sim = cases.pin_fin(device=dev, storage=storage, collision="mrt_smag", nx=args.nx, ny=args.ny, nz=args.nz)
+        sim.cfg.macro_stride = args.macro_stride
+        if storage == "fp32":
+            lat = Lattice64(sim)
         LBMCUDAUpgrade.patch(sim)
+        sims[storage] = sim
+    ref = sims["fp32"]
+    torch.cuda.synchronize()
+    t = time.perf_counter()
+    lat.step(steps - 1000)
+    prev = lat.velocity()
+    lat.step(1000)
+    torch.cuda.synchronize()
+    fp64_s = time.perf_counter() - t
+    lat.check()
+    vel = {"fp64": lat.velocity()}
+    fluid = ~ref.solid_flow.reshape(-1)
+    steady = float(torch.linalg.norm((vel["fp64"] - prev)[:, fluid]) / torch.linalg.norm(vel["fp64"][:, fluid]))
+    mass = {}
+    for storage, sim in sims.items():
         m0 = lbm_mass(sim)
         for _ in range(steps):
             sim.step(do_thermal=False)
         mass[storage] = (lbm_mass(sim) - m0) / m0
-        sim.sync_f()
-        vel[storage] = _velocity_from_f(sim.f.cpu().numpy(), shape)
-    fluid = ~ref.solid_flow.cpu().numpy()
-    U64 = np.stack(vel["fp64"])[:, fluid]
-    out = {"workload": "pin fin 128x64x64 (8x4 pins r=3.5, h=40), MRT + Bouzidi IBB, u=0.08, Re=200",
-           "steps": steps, "fp64_run": f"CPU oracle in FP64, {os.cpu_count()} threads, {fp64_s:.1f} s",
-           "velocity_rel_l2": {}, "temperature_rel_max": {}, "temperature_rel_l2": {}, "wall_heat_flow_rel": {},
-           "nusselt": {}, "nusselt_rel": {}, "heat_balance": {}, "mass_rel_change": {}}
-    k = ref.k.cpu().numpy().astype(np.float64)
+        if sim._fc.check_device_error():
+            raise RuntimeError(f"accuracy run ({storage}): device error word set")
+        vel[storage] = _velocity_of(sim)
+    U64 = vel["fp64"][:, fluid]
+    out = {"workload": "pin fin 256x128x128 (16x8 pins r=3.5 h=80, seed 1), MRT-Smagorinsky (Cs=0.1) + Bouzidi "
+                       "IBB, u=0.08, Re=200",
+           "steps": steps, "fp64_run": f"device FP64 run of the reference step sequence, {fp64_s:.1f} s",
+           "fp64_velocity_change_last_1000_steps": steady,
+           "velocity_rel_l2": {}, "velocity_rel_max": {}, "temperature_rel_max": {}, "temperature_rel_l2": {},
+           "wall_heat_flow_rel": {}, "nusselt": {}, "nusselt_rel": {}, "heat_balance": {}, "mass_rel_change": {}}
+    k = ref.k.cpu().numpy().astype("float64")
     solid = ref.solid.cpu().numpy()
     T, heat = {}, {}
-    for name in ("fp64", "fp32", "fp16"):
+    for name in ("fp64", "fp32", "fp16", "bf16"):
         if name != "fp64":
-            U = np.stack(vel[name])[:, fluid]
-            out["velocity_rel_l2"][name] = float(np.linalg.norm(U - U64) / np.linalg.norm(U64))
-        u, v, w = (torch.from_numpy(a.astype(np.float32)).to(dev) for a in vel[name])
-        mg, b = thermal_bench.thermal_system(ref, u, v, w)
-        x, info = mg_pcg.bicgstab_mg_f64(mg, b, tol=1e-10, max_it=400)
-        T[name] = x.reshape(shape).cpu().numpy().astype(np.float64)
+            U = vel[name][:, fluid]
+            out["velocity_rel_l2"][name] = float(torch.linalg.norm(U - U64) / torch.linalg.norm(U64))
+            out["velocity_rel_max"][name] = float((U - U64).abs().max() / U64.abs().max())
+        u = vel[name].to(torch.float32).reshape((3,) + shape)
+        mg, b = thermal_bench.thermal_system(ref, u[0], u[1], u[2])
+        x, info = mg_pcg.bicgstab_mg_f64(mg, b, tol=1e-10, max_it=600)
+        T[name] = x.reshape(shape).cpu().numpy().astype("float64")
         hb = heat_balance(mg, x, b / 1000.0, 1000.0)
-        out["heat_balance"][name] = {k: (float(f"{v:.6g}")) for k, v in hb.items()}
+        out["heat_balance"][name] = {kk: (float(f"{vv:.6g}")) for kk, vv in hb.items()}
         heat[name] = _wall_heat(T[name], k, solid, 2 * 3.5)
         out["nusselt"][name] = round(heat[name][2], 6)
-    for name in ("fp32", "fp16"):
+    import numpy as np
+    for name in ("fp32", "fp16", "bf16"):
         dT = T[name] - T["fp64"]
         out["temperature_rel_max"][name] = float(np.abs(dT).max() / np.abs(T["fp64"]).max())
         out["temperature_rel_l2"][name] = float(np.linalg.norm(dT) / np.linalg.norm(T["fp64"]))
         out["wall_heat_flow_rel"][name] = float(abs(heat[name][0] - heat["fp64"][0]) / abs(heat["fp64"][0]))
         out["nusselt_rel"][name] = float(abs(heat[name][2] - heat["fp64"][2]) / abs(heat["fp64"][2]))
     out["wall_faces"] = heat["fp64"][1]
-    out["mass_rel_change"] = {k: float(f"{v:.6g}") for k, v in mass.items()}
+    out["mass_rel_change"] = {kk: float(f"{vv:.6g}") for kk, vv in mass.items()}
     return out
 
 
 def cpu_baseline_sample(args):
-    """A bounded sample of the same workload on the host cores (oracle, FP32)."""
-    import numpy as np
-    from oracle.lbm import OracleLBM
-    sim = make_case(setup_device(), "fp32", args)
-    d = sim.ibb_data
-    links = {k: getattr(d, k).cpu().numpy() for k in
-             ("fluid_flat", "dir_i", "dir_opp", "w_i", "w_second", "q_ge_half", "ff_flat", "ff_valid")}
-    orc = OracleLBM(sim.nx, sim.ny, sim.nz, sim.f.cpu().numpy(), sim.solid_flow.cpu().numpy(),
-                    collision=args.collision, omega=float(sim.omega_plus),
-                    S=sim._mrt_S.cpu().numpy() if hasattr(sim, "_mrt_S") else None,
-                    sigma=sim._sponge_sigma.cpu().numpy() if sim.cfg.sponge_length > 0 else None, links=links,
-                    domain_walls=sim.cfg.domain_walls, u_in_lat=sim.u_in_lat, real="f32")
+    """A bounded sample of the same workload on the host cores (oracle, FP32), case built on the host."""
+    sim = host_case(args)
+    orc = oracle_of(sim)
     orc.step(1)
     n = args.cpu_steps
     t = time.perf_counter()
@@ -374,6 +447,9 @@ def main():
                     help="main pass: TMA-staged tiles (default) or per-thread global loads")
     ap.add_argument("--link-pass", default="inline", choices=("inline", "separate"),
                     help="link cells inside the main pass (default) or in their own kernel (direct pass only)")
+    ap.add_argument("--restart-every", type=int, default=400,
+                    help="reset the lattice to its initial state (untimed) before it passes this many steps "
+                         "(plain MRT at this Reynolds number diverges after ~600 steps); 0 = never")
     ap.add_argument("--cpu-steps", type=int, default=3)
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
@@ -382,7 +458,7 @@ def main():
     ap.add_argument("--no-io", action="store_true", help="skip the snapshot / checkpoint timings")
     ap.add_argument("--no-accuracy", action="store_true", help="skip the FP16/FP32 vs FP64 accuracy report")
     ap.add_argument("--no-learned", action="store_true", help="skip the learned-preconditioner training / A-B")
-    ap.add_argument("--accuracy-steps", type=int, default=600)
+    ap.add_argument("--accuracy-steps", type=int, default=10000)
     ap.add_argument("--storages", default="fp16,fp32", help="population storages to time (first = headline)")
     ap.add_argument("--profile", action="store_true",
                     help="short run for ncu captures: headline storage only, no e2e / thermal / CPU legs")
@@ -413,15 +489,15 @@ def main():
     for storage in storages:
         sim = make_case(dev, storage, args)
         LBMCUDAUpgrade.patch(sim)
+        restarter = Restarter(sim, args.restart_every)
+        restarter.before(args.warmup)
         for _ in range(args.warmup):
             sim.step(do_thermal=False)
         torch.cuda.synchronize()
         sampler = ClockSampler(local) if storage == storages[0] else None
         if sampler:
             sampler.start()
-        if ws > 1:
-            torch.distributed.barrier()
-        total_ms = time_steps(sim, args.steps)
+        total_ms, blocks = time_steps(sim, args.steps, dev, ws=ws, restarter=restarter)
         if ws > 1:
             tt = torch.tensor([total_ms], device=dev)
             torch.distributed.all_reduce(tt, op=torch.distributed.ReduceOp.MAX)
@@ -430,9 +506,16 @@ def main():
         sbytes = 4 if storage == "fp32" else 2
         traffic = lbm_traffic(sim, sim._fc, sbytes)
         err = sim._fc.check_device_error()
-        passes = sim._fc.time_passes(max(20, min(args.steps, 200)))
+        import math
+        from fluxcore3d_gb300.diagnostics import lbm_mass
+        finite = math.isfinite(lbm_mass(sim))            # FP64 sum of every population of the state
+        n_pass = max(20, min(args.steps, 200))
+        restarter.before(n_pass)
+        passes = sim._fc.time_passes(n_pass)
         per_step = sim._fc.launches_per_step()
-        results[storage] = dict(total_ms=total_ms, passes=passes, traffic=traffic, clocks=clocks, launches=per_step,
+        results[storage] = dict(total_ms=total_ms, blocks=blocks, restarts=restarter.restarts, finite=finite,
+                                passes=passes, traffic=traffic, clocks=clocks,
+                                launches=per_step,
                                 N=sim.nx * sim.ny * sim.nz, planes=len(sim._fc.planes),
                                 links=sim._fc.n_links, err=err)
         del sim
@@ -464,10 +547,13 @@ def main():
         "vs_baseline": None,
         "dtype": "f16-storage/f32-compute",
         "data": "synthetic",
-        "config": {"workload": WORKLOAD, "cells": N, "fluid_cells": tr["n_fluid"], "links": r["links"],
-                   "link_cells": tr["n_link_cells"],
-                   "collision": args.collision, "macro_stride": args.macro_stride,
-                   "l2_flush": "inputs larger than L2 (2 x 159 MB populations)", "parallelism": "replicas"},
+        "config": bench_config(args),
+        "case": {"fluid_cells": tr["n_fluid"], "links": r["links"], "link_cells": tr["n_link_cells"],
+                 "storage": storages[0], "timed_blocks": r["blocks"], "restarts": r["restarts"],
+                 "state_finite_after_timing": r["finite"],
+                 "restart_every": args.restart_every,
+                 "timing": f"median of {r['blocks']} blocks of {args.steps} steps (CUDA events), "
+                           f"blocks repeated to span >= 1 s"},
         "roofline": {"bound": "hbm", "achieved": round(achieved, 1), "peak": hbm_peak, "unit": "GB/s",
                      "frac": round(achieved / hbm_peak, 4), "traffic": traffic,
                      "kernel": KERNEL[args.staging],
@@ -479,7 +565,7 @@ def main():
                      "step_achieved": round(step_gbs, 1)},
 
         "clocks": r["clocks"],
-        "gpu_launches": args.steps * launches_per_step,
+        "gpu_launches": r["blocks"] * args.steps * launches_per_step,
         "device_error": r["err"],
     }
     for st_name in storages[1:]:
@@ -528,9 +614,10 @@ def main():
         torch.distributed.destroy_process_group()
 
 
-def e2e_run(args, dev):
+def e2e_run(args, dev, min_seconds=1.0):
     """Public API end to end: initial populations uploaded from pinned host memory, K steps
-    through sim.step(), final macro fields read back; bytes are reported per step."""
+    through sim.step(), final macro fields read back into pinned host memory; bytes are reported
+    per step.  The block is repeated until the blocks span `min_seconds`; the median is reported."""
     import torch
     from fluxcore3d_gb300.solver.lbm_cuda_ext import LBMCUDAUpgrade
     sim = make_case(dev, "fp16", args)
@@ -540,21 +627,31 @@ def e2e_run(args, dev):
     for _ in range(args.warmup):
         sim.step(do_thermal=False)
     torch.cuda.synchronize()
-    t = time.perf_counter()
-    sim.f.copy_(host_f, non_blocking=True)
-    sim._fc.invalidate()
-    for _ in range(args.steps):
-        sim.step(do_thermal=False)
-    out[0].copy_(sim.rho, non_blocking=True)
-    out[1].copy_(sim.u, non_blocking=True)
-    out[2].copy_(sim.v, non_blocking=True)
-    out[3].copy_(sim.wv, non_blocking=True)
-    torch.cuda.synchronize()
-    dt = time.perf_counter() - t
+
+    def block():
+        t = time.perf_counter()
+        sim.f.copy_(host_f, non_blocking=True)
+        sim._fc.invalidate()
+        for _ in range(args.steps):
+            sim.step(do_thermal=False)
+        out[0].copy_(sim.rho, non_blocking=True)
+        out[1].copy_(sim.u, non_blocking=True)
+        out[2].copy_(sim.v, non_blocking=True)
+        out[3].copy_(sim.wv, non_blocking=True)
+        torch.cuda.synchronize()
+        return time.perf_counter() - t
+
+    times = [block()]
+    while sum(times) < min_seconds and len(times) < 20000:
+        times.append(block())
+    dt = statistics.median(times)
     N = sim.nx * sim.ny * sim.nz
     return {"value": round(N * args.steps / dt / 1e6, 1), "unit": "MLUPS",
             "h2d_bytes_per_step": int(host_f.numel() * 4 // args.steps),
-            "d2h_bytes_per_step": int(out.numel() * 4 // args.steps)}
+            "d2h_bytes_per_step": int(out.numel() * 4 // args.steps),
+            "blocks": len(times),
+            "block": f"upload of the FP32 populations, {args.steps} sim.step() calls, read-back of rho/u/v/w; "
+                     f"median over the blocks (wall clock)"}
 
 
 def thermal_run(args, dev):

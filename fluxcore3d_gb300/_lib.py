@@ -97,6 +97,14 @@ SIGNATURES: dict[str, tuple] = {
     "fc_lbm_convective_bc": (i32, [vp, vp, i32, i32, i32, i32, i32, i32, i32, f32, i32, i32, vp, i64, vp]),
     "fc_lbm_convective_noalloc_max_plane": (i64, []),
     "fc_lbm_convective_bc_noalloc": (i32, [vp, vp, i32, i32, i32, i32, i32, i32, i32, f32, i32, i32, vp]),
+    # lattice, FP64 run of the plain method
+    "fc_lbm64_macro_collide": (i32, [i32, vp, vp, vp, vp, vp, vp, vp, f32, f32, f32, vp, f32, f32, i64, vp]),
+    "fc_lbm64_stream_pull": (i32, [vp, vp, i32, i32, i32, i32, i32, i32, vp]),
+    "fc_lbm64_sponge": (i32, [vp, vp, vp, vp, vp, vp, i64, vp]),
+    "fc_lbm64_ibb": (i32, [vp, vp, vp, vp, vp, vp, vp, vp, vp, vp, i64, i64, vp, vp]),
+    "fc_lbm64_reset_solid": (i32, [vp, vp, i64, vp]),
+    "fc_lbm64_zou_he_bc": (i32, [vp, vp, i32, i32, i32, i32, i32, i32, i32, f64, f64, i32, vp]),
+    "fc_lbm64_convective_bc": (i32, [vp, vp, i32, i32, i32, i32, i32, i32, i32, f64, i32, i32, vp, i64, vp]),
     # lattice, fused
     "fc_lbm_fused_step": (i32, [C.POINTER(StepArgs), vp]),
     "fc_lbm_link_gather": (i32, [C.POINTER(StepArgs), vp, C.c_int64, i32, vp]),

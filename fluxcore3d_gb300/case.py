@@ -227,14 +227,17 @@ def channel_cube(device="cuda", collision="bgk", storage="fp32", nx=64, ny=32, n
 
 
 def pin_fin(device="cuda", collision="mrt", storage="fp16", nx=256, ny=128, nz=128, u=0.08, Re=200.0,
-            radius=3.5, height=80, base=8, seed=1, sponge_length=40, k_ratio=200.0, n_pins=(16, 8)):
-    """Pin-fin heat sink: base plate + 16x8 jittered cylinders, analytic link fractions."""
+            radius=3.5, height=80, base=8, seed=1, sponge_length=40, k_ratio=200.0, n_pins=(16, 8),
+            ibb_builder=None):
+    """Pin-fin heat sink: base plate + 16x8 jittered cylinders, analytic link fractions.
+    `ibb_builder(solid, G)` makes the link data (default: the device link builder and FP64
+    bisection of the level set G)."""
     cfg = CaseConfig(nx=nx, ny=ny, nz=nz, collision=collision, lbm_storage=storage,
                      domain_walls=["+Z", "-Z"], sponge_length=sponge_length)
     G = geo.pin_fin_levelset(nx, ny, nz, n_pins=n_pins, radius=radius, height=height, base=base, seed=seed,
                              device=device)
     solid = geo.mask_from_levelset((nx, ny, nz), G, device=device)
-    ibb = geo.ibb_from_level_set(solid, G)
+    ibb = (ibb_builder or geo.ibb_from_level_set)(solid, G)
     sf = stamp_walls(cfg, solid)
     nu = u * (2 * radius) / Re
     return LatticeCase(cfg, u, nu, solid, sf, ibb, device=device, seed=seed, k_ratio=k_ratio)

@@ -36,17 +36,24 @@ __host__ __device__ constexpr float mrt_row_norm2(int k) {
          : k == 12 ? 24.f : k <= 15 ? 4.f : 8.f;
 }
 
-struct Macro {
-    float rho, ux, uy, uz, inv_rho;
+// The per-cell operators below are templates on the arithmetic type R: float is
+// the reference's FP32 kernel arithmetic, double the FP64 run of the plain
+// method that the reduced-precision results are measured against.  Constants
+// keep the reference's FP32 values (weights, S rates) in both.
+template <class R>
+struct MacroT {
+    R rho, ux, uy, uz, inv_rho;
 };
+using Macro = MacroT<float>;
 
-__device__ __forceinline__ Macro macros_of(const float f[19]) {
-    Macro m;
-    float rho = 0.f;
+template <class R>
+__device__ __forceinline__ MacroT<R> macros_of(const R f[19]) {
+    MacroT<R> m;
+    R rho = R(0);
 #pragma unroll
     for (int q = 0; q < 19; ++q) rho += f[q];
     // momentum sums in direction order (c components are +-1 or 0)
-    float jx = 0.f, jy = 0.f, jz = 0.f;
+    R jx = R(0), jy = R(0), jz = R(0);
 #pragma unroll
     for (int q = 0; q < 19; ++q) {
         if (cx(q) == 1) jx += f[q];
@@ -57,7 +64,7 @@ __device__ __forceinline__ Macro macros_of(const float f[19]) {
         if (cz(q) == -1) jz -= f[q];
     }
     m.rho = rho;
-    m.inv_rho = 1.f / (rho + 1e-12f);
+    m.inv_rho = R(1) / (rho + R(1e-12));
     m.ux = jx * m.inv_rho;
     m.uy = jy * m.inv_rho;
     m.uz = jz * m.inv_rho;
@@ -65,92 +72,94 @@ __device__ __forceinline__ Macro macros_of(const float f[19]) {
 }
 
 // f_eq for all 19 directions: w_q rho (1 + cu + cu^2/2 - 3/2 u.u), cu = 3 c.u
-__device__ __forceinline__ void equilibrium(float rho, float ux, float uy, float uz, float feq[19]) {
-    const float usq = 1.5f * (ux * ux + uy * uy + uz * uz);
-    const float tx = 3.f * ux, ty = 3.f * uy, tz = 3.f * uz;
+template <class R>
+__device__ __forceinline__ void equilibrium(R rho, R ux, R uy, R uz, R feq[19]) {
+    const R usq = R(1.5) * (ux * ux + uy * uy + uz * uz);
+    const R tx = R(3) * ux, ty = R(3) * uy, tz = R(3) * uz;
 #pragma unroll
     for (int q = 0; q < 19; ++q) {
-        float cu = 0.f;
+        R cu = R(0);
         if (cx(q) == 1) cu += tx;
         if (cx(q) == -1) cu -= tx;
         if (cy(q) == 1) cu += ty;
         if (cy(q) == -1) cu -= ty;
         if (cz(q) == 1) cu += tz;
         if (cz(q) == -1) cu -= tz;
-        feq[q] = wq(q) * rho * (1.f + cu + 0.5f * cu * cu - usq);
+        feq[q] = R(wq(q)) * rho * (R(1) + cu + R(0.5) * cu * cu - usq);
     }
 }
 
 // Relax the non-equilibrium part n = f - f_eq through the moment basis and
 // return df = M^-1 S M n (conserved channels excluded).  g[k] = S_k m_k / |M_k|^2.
-__device__ __forceinline__ void mrt_df(const float n[19], const float s[19], float df[19]) {
-    const float Fx = n[1] + n[2], Fy = n[3] + n[4], Fz = n[5] + n[6];
-    const float sf = Fx + Fy + Fz;
-    const float Sxy = n[7] + n[8] + n[9] + n[10];
-    const float Sxz = n[11] + n[12] + n[13] + n[14];
-    const float Syz = n[15] + n[16] + n[17] + n[18];
-    const float se = Sxy + Sxz + Syz;
-    const float jxe = (n[7] + n[8] - n[9] - n[10]) + (n[11] + n[12] - n[13] - n[14]);
-    const float jye = (n[7] - n[8] + n[9] - n[10]) + (n[15] + n[16] - n[17] - n[18]);
-    const float jze = (n[11] - n[12] + n[13] - n[14]) + (n[15] - n[16] + n[17] - n[18]);
+template <class R>
+__device__ __forceinline__ void mrt_df(const R n[19], const R s[19], R df[19]) {
+    const R Fx = n[1] + n[2], Fy = n[3] + n[4], Fz = n[5] + n[6];
+    const R sf = Fx + Fy + Fz;
+    const R Sxy = n[7] + n[8] + n[9] + n[10];
+    const R Sxz = n[11] + n[12] + n[13] + n[14];
+    const R Syz = n[15] + n[16] + n[17] + n[18];
+    const R se = Sxy + Sxz + Syz;
+    const R jxe = (n[7] + n[8] - n[9] - n[10]) + (n[11] + n[12] - n[13] - n[14]);
+    const R jye = (n[7] - n[8] + n[9] - n[10]) + (n[15] + n[16] - n[17] - n[18]);
+    const R jze = (n[11] - n[12] + n[13] - n[14]) + (n[15] - n[16] + n[17] - n[18]);
 
-    const float m1 = -30.f * n[0] - 11.f * sf + 8.f * se;
-    const float m2 = 12.f * n[0] - 4.f * sf + se;
-    const float m4 = -4.f * (n[1] - n[2]) + jxe;
-    const float m6 = -4.f * (n[3] - n[4]) + jye;
-    const float m8 = -4.f * (n[5] - n[6]) + jze;
-    const float m9 = 2.f * Fx - Fy - Fz + Sxy + Sxz - 2.f * Syz;
-    const float m10 = -4.f * Fx + 2.f * Fy + 2.f * Fz + Sxy + Sxz - 2.f * Syz;
-    const float m11 = Fy - Fz + Sxy - Sxz;
-    const float m12 = -2.f * Fy + 2.f * Fz + Sxy - Sxz;
-    const float m13 = n[7] - n[8] - n[9] + n[10];
-    const float m14 = n[15] - n[16] - n[17] + n[18];
-    const float m15 = n[11] - n[12] - n[13] + n[14];
-    const float m16 = n[7] + n[8] - n[9] - n[10] - n[11] - n[12] + n[13] + n[14];
-    const float m17 = -n[7] + n[8] - n[9] + n[10] + n[15] + n[16] - n[17] - n[18];
-    const float m18 = n[11] - n[12] + n[13] - n[14] - n[15] + n[16] - n[17] + n[18];
+    const R m1 = R(-30) * n[0] - R(11) * sf + R(8) * se;
+    const R m2 = R(12) * n[0] - R(4) * sf + se;
+    const R m4 = R(-4) * (n[1] - n[2]) + jxe;
+    const R m6 = R(-4) * (n[3] - n[4]) + jye;
+    const R m8 = R(-4) * (n[5] - n[6]) + jze;
+    const R m9 = R(2) * Fx - Fy - Fz + Sxy + Sxz - R(2) * Syz;
+    const R m10 = R(-4) * Fx + R(2) * Fy + R(2) * Fz + Sxy + Sxz - R(2) * Syz;
+    const R m11 = Fy - Fz + Sxy - Sxz;
+    const R m12 = R(-2) * Fy + R(2) * Fz + Sxy - Sxz;
+    const R m13 = n[7] - n[8] - n[9] + n[10];
+    const R m14 = n[15] - n[16] - n[17] + n[18];
+    const R m15 = n[11] - n[12] - n[13] + n[14];
+    const R m16 = n[7] + n[8] - n[9] - n[10] - n[11] - n[12] + n[13] + n[14];
+    const R m17 = -n[7] + n[8] - n[9] + n[10] + n[15] + n[16] - n[17] - n[18];
+    const R m18 = n[11] - n[12] + n[13] - n[14] - n[15] + n[16] - n[17] + n[18];
 
-    // divide by squared row norms of M
-    const float g1 = s[1] * m1 * (1.f / 2394.f);
-    const float g2 = s[2] * m2 * (1.f / 252.f);
-    const float g4 = s[4] * m4 * (1.f / 40.f);
-    const float g6 = s[6] * m6 * (1.f / 40.f);
-    const float g8 = s[8] * m8 * (1.f / 40.f);
-    const float g9 = s[9] * m9 * (1.f / 36.f);
-    const float g10 = s[10] * m10 * (1.f / 72.f);
-    const float g11 = s[11] * m11 * (1.f / 12.f);
-    const float g12 = s[12] * m12 * (1.f / 24.f);
-    const float g13 = s[13] * m13 * 0.25f;
-    const float g14 = s[14] * m14 * 0.25f;
-    const float g15 = s[15] * m15 * 0.25f;
-    const float g16 = s[16] * m16 * 0.125f;
-    const float g17 = s[17] * m17 * 0.125f;
-    const float g18 = s[18] * m18 * 0.125f;
+    // divide by squared row norms of M (the reciprocals are rounded once, to R)
+    const R g1 = s[1] * m1 * (R(1) / R(2394));
+    const R g2 = s[2] * m2 * (R(1) / R(252));
+    const R g4 = s[4] * m4 * (R(1) / R(40));
+    const R g6 = s[6] * m6 * (R(1) / R(40));
+    const R g8 = s[8] * m8 * (R(1) / R(40));
+    const R g9 = s[9] * m9 * (R(1) / R(36));
+    const R g10 = s[10] * m10 * (R(1) / R(72));
+    const R g11 = s[11] * m11 * (R(1) / R(12));
+    const R g12 = s[12] * m12 * (R(1) / R(24));
+    const R g13 = s[13] * m13 * R(0.25);
+    const R g14 = s[14] * m14 * R(0.25);
+    const R g15 = s[15] * m15 * R(0.25);
+    const R g16 = s[16] * m16 * R(0.125);
+    const R g17 = s[17] * m17 * R(0.125);
+    const R g18 = s[18] * m18 * R(0.125);
 
-    df[0] = -30.f * g1 + 12.f * g2;
-    const float face = -11.f * g1 - 4.f * g2;
-    const float fx_ = face + 2.f * g9 - 4.f * g10;
-    df[1] = fx_ - 4.f * g4;
-    df[2] = fx_ + 4.f * g4;
-    const float fyz = face - g9 + 2.f * g10;
-    const float fy_ = fyz + g11 - 2.f * g12;
-    const float fz_ = fyz - g11 + 2.f * g12;
-    df[3] = fy_ - 4.f * g6;
-    df[4] = fy_ + 4.f * g6;
-    df[5] = fz_ - 4.f * g8;
-    df[6] = fz_ + 4.f * g8;
-    const float edge = 8.f * g1 + g2;
-    const float exy = edge + g9 + g10 + g11 + g12;
+    df[0] = R(-30) * g1 + R(12) * g2;
+    const R face = R(-11) * g1 - R(4) * g2;
+    const R fx_ = face + R(2) * g9 - R(4) * g10;
+    df[1] = fx_ - R(4) * g4;
+    df[2] = fx_ + R(4) * g4;
+    const R fyz = face - g9 + R(2) * g10;
+    const R fy_ = fyz + g11 - R(2) * g12;
+    const R fz_ = fyz - g11 + R(2) * g12;
+    df[3] = fy_ - R(4) * g6;
+    df[4] = fy_ + R(4) * g6;
+    df[5] = fz_ - R(4) * g8;
+    df[6] = fz_ + R(4) * g8;
+    const R edge = R(8) * g1 + g2;
+    const R exy = edge + g9 + g10 + g11 + g12;
     df[7] = exy + g4 + g6 + g13 + g16 - g17;
     df[8] = exy + g4 - g6 - g13 + g16 + g17;
     df[9] = exy - g4 + g6 - g13 - g16 - g17;
     df[10] = exy - g4 - g6 + g13 - g16 + g17;
-    const float exz = edge + g9 + g10 - g11 - g12;
+    const R exz = edge + g9 + g10 - g11 - g12;
     df[11] = exz + g4 + g8 + g15 - g16 + g18;
     df[12] = exz + g4 - g8 - g15 - g16 - g18;
     df[13] = exz - g4 + g8 - g15 + g16 + g18;
     df[14] = exz - g4 - g8 + g15 + g16 - g18;
-    const float eyz = edge - 2.f * g9 - 2.f * g10;
+    const R eyz = edge - R(2) * g9 - R(2) * g10;
     df[15] = eyz + g6 + g8 + g14 + g17 - g18;
     df[16] = eyz + g6 - g8 - g14 + g17 + g18;
     df[17] = eyz - g6 + g8 - g14 - g17 - g18;
@@ -159,44 +168,45 @@ __device__ __forceinline__ void mrt_df(const float n[19], const float s[19], flo
 
 // Collide one fluid cell in place.  Returns the pre-collision macros and
 // leaves feq (at those macros) for the sponge stage.
-template <int MODE>
-__device__ __forceinline__ Macro collide(float f[19], float feq[19], const CollideParams& p) {
-    const Macro m = macros_of(f);
+template <int MODE, class R>
+__device__ __forceinline__ MacroT<R> collide(R f[19], R feq[19], const CollideParams& p) {
+    const MacroT<R> m = macros_of(f);
     equilibrium(m.rho, m.ux, m.uy, m.uz, feq);
     if (MODE == CM_BGK) {
+        const R om = R(p.omega);
 #pragma unroll
-        for (int q = 0; q < 19; ++q) f[q] = f[q] + p.omega * (feq[q] - f[q]);
+        for (int q = 0; q < 19; ++q) f[q] = f[q] + om * (feq[q] - f[q]);
     } else if (MODE == CM_TRT) {
-        float out[19];
+        const R op = R(p.omega_plus), omn = R(p.omega_minus);
+        R out[19];
 #pragma unroll
         for (int q = 0; q < 19; ++q) {
             const int o = opp(q);
-            const float fp = 0.5f * (f[q] + f[o]);
-            const float fm = 0.5f * (f[q] - f[o]);
-            const float ep = 0.5f * (feq[q] + feq[o]);
-            const float em = 0.5f * (feq[q] - feq[o]);
-            out[q] = (fp + p.omega_plus * (ep - fp)) + (fm + p.omega_minus * (em - fm));
+            const R fp = R(0.5) * (f[q] + f[o]);
+            const R fm = R(0.5) * (f[q] - f[o]);
+            const R ep = R(0.5) * (feq[q] + feq[o]);
+            const R em = R(0.5) * (feq[q] - feq[o]);
+            out[q] = (fp + op * (ep - fp)) + (fm + omn * (em - fm));
         }
 #pragma unroll
         for (int q = 0; q < 19; ++q) f[q] = out[q];
     } else {
-        float n[19], df[19], s[19];
+        R n[19], df[19], s[19];
 #pragma unroll
-        for (int q = 0; q < 19; ++q) { n[q] = f[q] - feq[q]; s[q] = p.S[q]; }
+        for (int q = 0; q < 19; ++q) { n[q] = f[q] - feq[q]; s[q] = R(p.S[q]); }
         if (MODE == CM_MRT_SMAG) {
-            float Pxx = 0.f, Pyy = 0.f, Pzz = 0.f, Pxy = 0.f, Pxz = 0.f, Pyz = 0.f;
+            R Pxx = R(0), Pyy = R(0), Pzz = R(0), Pxy = R(0), Pxz = R(0), Pyz = R(0);
 #pragma unroll
             for (int q = 0; q < 19; ++q) {
-                const float a = (float)cx(q), b = (float)cy(q), c = (float)cz(q);
+                const R a = R(cx(q)), b = R(cy(q)), c = R(cz(q));
                 Pxx += n[q] * a * a; Pyy += n[q] * b * b; Pzz += n[q] * c * c;
                 Pxy += n[q] * a * b; Pxz += n[q] * a * c; Pyz += n[q] * b * c;
             }
-            const float piF = sqrtf(Pxx * Pxx + Pyy * Pyy + Pzz * Pzz +
-                                    2.f * (Pxy * Pxy + Pxz * Pxz + Pyz * Pyz));
-            const float nu0 = (1.f / p.omega0 - 0.5f) / 3.f;
-            const float disc = nu0 * nu0 + 4.f * p.Cs_dx2 * (piF * m.inv_rho) * 4.5f;
-            const float nu_eff = 0.5f * (nu0 + sqrtf(fmaxf(disc, nu0 * nu0)));
-            const float om = fminf(1.99f, 1.f / (3.f * nu_eff + 0.5f));
+            const R piF = sqrt(Pxx * Pxx + Pyy * Pyy + Pzz * Pzz + R(2) * (Pxy * Pxy + Pxz * Pxz + Pyz * Pyz));
+            const R nu0 = (R(1) / R(p.omega0) - R(0.5)) / R(3);
+            const R disc = nu0 * nu0 + R(4) * R(p.Cs_dx2) * (piF * m.inv_rho) * R(4.5);
+            const R nu_eff = R(0.5) * (nu0 + sqrt(fmax(disc, nu0 * nu0)));
+            const R om = fmin(R(1.99), R(1) / (R(3) * nu_eff + R(0.5)));
             s[9] = om; s[11] = om; s[13] = om; s[14] = om; s[15] = om;
         }
         mrt_df(n, s, df);

@@ -38,10 +38,13 @@ inline unsigned grid_for(long long n) { return (unsigned)((n + BLOCK - 1) / BLOC
 //  Family 1: per-operation kernels (reference call surface)
 // ============================================================================
 
-template <int MODE>
+// The per-operation kernels are templates on the population type R: float
+// serves the reference call surface, double the FP64 run of the plain method
+// (fc_lbm64_*), which the reduced-precision runs are measured against.
+template <int MODE, class R>
 __global__ void __launch_bounds__(BLOCK) k_macro_collide(
-    const float* __restrict__ f, float* __restrict__ f_post, float* __restrict__ rho,
-    float* __restrict__ u, float* __restrict__ v, float* __restrict__ w,
+    const R* __restrict__ f, R* __restrict__ f_post, R* __restrict__ rho,
+    R* __restrict__ u, R* __restrict__ v, R* __restrict__ w,
     const uint8_t* __restrict__ solid, CollideParams p, const float* __restrict__ S_dev, long long N) {
     const long long idx = (long long)blockIdx.x * blockDim.x + threadIdx.x;
     if (idx >= N) return;
@@ -51,21 +54,22 @@ __global__ void __launch_bounds__(BLOCK) k_macro_collide(
     }
     if (solid[idx]) {
 #pragma unroll
-        for (int q = 0; q < 19; ++q) f_post[q * N + idx] = wq(q);
-        rho[idx] = 1.f; u[idx] = 0.f; v[idx] = 0.f; w[idx] = 0.f;
+        for (int q = 0; q < 19; ++q) f_post[q * N + idx] = R(wq(q));
+        rho[idx] = R(1); u[idx] = R(0); v[idx] = R(0); w[idx] = R(0);
         return;
     }
-    float fi[19], feq[19];
+    R fi[19], feq[19];
 #pragma unroll
     for (int q = 0; q < 19; ++q) fi[q] = __ldg(f + q * N + idx);
-    const Macro m = collide<MODE>(fi, feq, p);
+    const MacroT<R> m = collide<MODE>(fi, feq, p);
     rho[idx] = m.rho; u[idx] = m.ux; v[idx] = m.uy; w[idx] = m.uz;
 #pragma unroll
     for (int q = 0; q < 19; ++q) f_post[q * N + idx] = fi[q];
 }
 
+template <class R>
 __global__ void __launch_bounds__(BLOCK) k_stream_pull(
-    const float* __restrict__ fin, float* __restrict__ fout, int nx, int ny, int nz,
+    const R* __restrict__ fin, R* __restrict__ fout, int nx, int ny, int nz,
     int px, int py, int pz) {
     const long long N = (long long)nx * ny * nz;
     const long long idx = (long long)blockIdx.x * blockDim.x + threadIdx.x;
@@ -87,15 +91,16 @@ __global__ void __launch_bounds__(BLOCK) k_stream_pull(
     }
 }
 
+template <class R>
 __global__ void __launch_bounds__(BLOCK) k_sponge(
-    float* __restrict__ f, const float* __restrict__ rho, const float* __restrict__ u,
-    const float* __restrict__ v, const float* __restrict__ w, const float* __restrict__ sigma,
+    R* __restrict__ f, const R* __restrict__ rho, const R* __restrict__ u,
+    const R* __restrict__ v, const R* __restrict__ w, const float* __restrict__ sigma,
     long long N) {
     const long long idx = (long long)blockIdx.x * blockDim.x + threadIdx.x;
     if (idx >= N) return;
-    const float sg = sigma[idx];
-    if (sg <= 0.f) return;
-    float feq[19];
+    const R sg = R(sigma[idx]);
+    if (sg <= R(0)) return;
+    R feq[19];
     equilibrium(rho[idx], u[idx], v[idx], w[idx], feq);
 #pragma unroll
     for (int q = 0; q < 19; ++q) {
@@ -104,8 +109,9 @@ __global__ void __launch_bounds__(BLOCK) k_sponge(
     }
 }
 
+template <class R>
 __global__ void __launch_bounds__(BLOCK) k_ibb_links(
-    const float* __restrict__ fpost, float* __restrict__ fstream,
+    const R* __restrict__ fpost, R* __restrict__ fstream,
     const int* __restrict__ fluid_flat, const int* __restrict__ dir_i,
     const int* __restrict__ dir_opp, const float* __restrict__ w1,
     const float* __restrict__ w2, const uint8_t* __restrict__ q_ge_half,
@@ -119,29 +125,30 @@ __global__ void __launch_bounds__(BLOCK) k_ibb_links(
         if (dev_err) atomicOr(dev_err, DEV_ERR_INDEX);
         return;
     }
-    const float a = fpost[qo * N + xf];
-    float bb;
+    const R a = fpost[qo * N + xf];
+    R bb;
     if (q_ge_half[l]) {
-        bb = w1[l] * a + w2[l] * fpost[qi * N + xf];
+        bb = R(w1[l]) * a + R(w2[l]) * fpost[qi * N + xf];
     } else if (ff_valid[l]) {
         const long long xff = ff_flat[l];
         if (xff < 0 || xff >= N) {
             if (dev_err) atomicOr(dev_err, DEV_ERR_INDEX);
             return;
         }
-        bb = w1[l] * a + w2[l] * fpost[qo * N + xff];
+        bb = R(w1[l]) * a + R(w2[l]) * fpost[qo * N + xff];
     } else {
         bb = a;
     }
     fstream[qi * N + xf] = bb;
 }
 
-__global__ void __launch_bounds__(BLOCK) k_reset_solid(float* __restrict__ f,
-                                                       const uint8_t* __restrict__ solid, long long N) {
+template <class R>
+__global__ void __launch_bounds__(BLOCK) k_reset_solid(R* __restrict__ f, const uint8_t* __restrict__ solid,
+                                                       long long N) {
     const long long idx = (long long)blockIdx.x * blockDim.x + threadIdx.x;
     if (idx >= N || !solid[idx]) return;
 #pragma unroll
-    for (int q = 0; q < 19; ++q) f[q * N + idx] = wq(q);
+    for (int q = 0; q < 19; ++q) f[q * N + idx] = R(wq(q));
 }
 
 // plane node (a,b) -> flat index of plane `p` along `axis`
@@ -159,28 +166,29 @@ __device__ __forceinline__ float q_diag(int c) { return c != 0 ? 0.66666667f : -
 // whose both branches read it), those of its interior neighbour fin, loaded
 // by the caller so that every load of the node is in flight at once.  Writes
 // the node's new populations to f and, when out is given, to out too.
-__device__ __forceinline__ void zou_he_core(const float fi[19], const float fin[19], float* __restrict__ f,
+template <class R>
+__device__ __forceinline__ void zou_he_core(const R fi[19], const R fin[19], R* __restrict__ f,
                                             long long N, long long flat_bc, int axis, int plane_idx, int bc_type,
-                                            float u_in, float rho_out, int sign, float* out) {
+                                            R u_in, R rho_out, int sign, R* out) {
     const int unknown = (plane_idx == 0) ? 1 : -1;
     const int known = -unknown;
-    float s0 = 0.f, sk = 0.f;
+    R s0 = R(0), sk = R(0);
 #pragma unroll
     for (int q = 0; q < 19; ++q) {
         const int c = axis == 0 ? cx(q) : (axis == 1 ? cy(q) : cz(q));
         if (c == 0) s0 += fi[q];
         if (c == known) sk += fi[q];
     }
-    float rho_bc, uax, ub = 0.f, vb = 0.f, wb = 0.f;
+    R rho_bc, uax, ub = R(0), vb = R(0), wb = R(0);
     if (bc_type == 0) {
         uax = u_in;
-        rho_bc = (s0 + 2.f * sk) / (1.f - fabsf(u_in) + 1e-12f);
-        rho_bc = fminf(fmaxf(rho_bc, 0.2f), 5.0f);
+        rho_bc = (s0 + R(2) * sk) / (R(1) - fabs(u_in) + R(1e-12));
+        rho_bc = fmin(fmax(rho_bc, R(0.2)), R(5.0));
         if (axis == 0) ub = uax; else if (axis == 1) vb = uax; else wb = uax;
     } else {
         rho_bc = rho_out;
-        uax = (float)known * ((s0 + 2.f * sk) / (rho_bc + 1e-12f) - 1.f);
-        if (uax * (float)sign < 0.f) {
+        uax = R(known) * ((s0 + R(2) * sk) / (rho_bc + R(1e-12)) - R(1));
+        if (uax * R(sign) < R(0)) {
 #pragma unroll
             for (int q = 0; q < 19; ++q) {
                 f[q * N + flat_bc] = fin[q];
@@ -188,43 +196,43 @@ __device__ __forceinline__ void zou_he_core(const float fi[19], const float fin[
             }
             return;
         }
-        const Macro mi = macros_of(fin);
+        const MacroT<R> mi = macros_of(fin);
         if (axis == 0) { ub = uax; vb = mi.uy; wb = mi.uz; }
         else if (axis == 1) { ub = mi.ux; vb = uax; wb = mi.uz; }
         else { ub = mi.ux; vb = mi.uy; wb = uax; }
     }
-    float feq[19];
+    R feq[19];
     equilibrium(rho_bc, ub, vb, wb, feq);
-    float g[19];
+    R g[19];
 #pragma unroll
     for (int q = 0; q < 19; ++q) {
         const int c = axis == 0 ? cx(q) : (axis == 1 ? cy(q) : cz(q));
         g[q] = (c == unknown) ? fi[opp(q)] + feq[q] - feq[opp(q)] : fi[q];
     }
-    float Pxx = 0.f, Pyy = 0.f, Pzz = 0.f, Pxy = 0.f, Pxz = 0.f, Pyz = 0.f;
+    R Pxx = R(0), Pyy = R(0), Pzz = R(0), Pxy = R(0), Pxz = R(0), Pyz = R(0);
 #pragma unroll
     for (int q = 0; q < 19; ++q) {
-        const float fn = g[q] - feq[q];
-        Pxx += fn * q_diag(cx(q));
-        Pyy += fn * q_diag(cy(q));
-        Pzz += fn * q_diag(cz(q));
-        Pxy += fn * (float)(cx(q) * cy(q));
-        Pxz += fn * (float)(cx(q) * cz(q));
-        Pyz += fn * (float)(cy(q) * cz(q));
+        const R fn = g[q] - feq[q];
+        Pxx += fn * R(q_diag(cx(q)));
+        Pyy += fn * R(q_diag(cy(q)));
+        Pzz += fn * R(q_diag(cz(q)));
+        Pxy += fn * R(cx(q) * cy(q));
+        Pxz += fn * R(cx(q) * cz(q));
+        Pyz += fn * R(cy(q) * cz(q));
     }
 #pragma unroll
     for (int q = 0; q < 19; ++q) {
-        const float sq = q_diag(cx(q)) * Pxx + q_diag(cy(q)) * Pyy + q_diag(cz(q)) * Pzz +
-                         2.f * ((float)(cx(q) * cy(q)) * Pxy + (float)(cx(q) * cz(q)) * Pxz +
-                                (float)(cy(q) * cz(q)) * Pyz);
-        const float v = feq[q] + wq(q) * sq * 4.5f;
+        const R sq = R(q_diag(cx(q))) * Pxx + R(q_diag(cy(q))) * Pyy + R(q_diag(cz(q))) * Pzz +
+                     R(2) * (R(cx(q) * cy(q)) * Pxy + R(cx(q) * cz(q)) * Pxz + R(cy(q) * cz(q)) * Pyz);
+        const R v = feq[q] + R(wq(q)) * sq * R(4.5);
         f[q * N + flat_bc] = v;
         if (out) out[q] = v;
     }
 }
 
-__device__ __forceinline__ void load_zou_he(const float* __restrict__ f, long long N, long long flat_bc,
-                                            long long flat_in, int bc_type, float fi[19], float fin[19]) {
+template <class R>
+__device__ __forceinline__ void load_zou_he(const R* __restrict__ f, long long N, long long flat_bc,
+                                            long long flat_in, int bc_type, R fi[19], R fin[19]) {
 #pragma unroll
     for (int q = 0; q < 19; ++q) fi[q] = f[q * N + flat_bc];
     if (bc_type != 0) {
@@ -233,17 +241,19 @@ __device__ __forceinline__ void load_zou_he(const float* __restrict__ f, long lo
     }
 }
 
-__device__ void zou_he_node(float* __restrict__ f, long long N, long long flat_bc, long long flat_in,
-                            int axis, int plane_idx, int bc_type, float u_in, float rho_out, int sign,
-                            float* out = nullptr) {
-    float fi[19], fin[19];
+template <class R>
+__device__ void zou_he_node(R* __restrict__ f, long long N, long long flat_bc, long long flat_in,
+                            int axis, int plane_idx, int bc_type, R u_in, R rho_out, int sign,
+                            R* out = nullptr) {
+    R fi[19], fin[19];
     load_zou_he(f, N, flat_bc, flat_in, bc_type, fi, fin);
     zou_he_core(fi, fin, f, N, flat_bc, axis, plane_idx, bc_type, u_in, rho_out, sign, out);
 }
 
+template <class R>
 __global__ void __launch_bounds__(BLOCK) k_zou_he(
-    float* __restrict__ f, const uint8_t* __restrict__ solid, int nx, int ny, int nz, int axis,
-    int plane_idx, int interior_idx, int bc_type, float u_in, float rho_out, int sign, int n1, int n2) {
+    R* __restrict__ f, const uint8_t* __restrict__ solid, int nx, int ny, int nz, int axis,
+    int plane_idx, int interior_idx, int bc_type, R u_in, R rho_out, int sign, int n1, int n2) {
     const int t = blockIdx.x * blockDim.x + threadIdx.x;
     if (t >= n1 * n2) return;
     const int a = t / n2, b = t - (t / n2) * n2;
@@ -256,8 +266,9 @@ __global__ void __launch_bounds__(BLOCK) k_zou_he(
 
 // Convective outlet, pass 1: zero-gradient copy of the incoming populations
 // and per-block partial sums (FP64, fixed tree order => deterministic).
+template <class R>
 __global__ void __launch_bounds__(BLOCK) k_convective_pass1(
-    float* __restrict__ f, const uint8_t* __restrict__ solid, int nx, int ny, int nz, int axis,
+    R* __restrict__ f, const uint8_t* __restrict__ solid, int nx, int ny, int nz, int axis,
     int outlet_idx, int interior_idx, int unknown_cax, int n1, int n2,
     double* __restrict__ part_rho, int* __restrict__ part_cnt) {
     __shared__ double s_rho[BLOCK];
@@ -271,11 +282,11 @@ __global__ void __launch_bounds__(BLOCK) k_convective_pass1(
         const long long fo = plane_flat(axis, outlet_idx, a, b, ny, nz);
         const long long fi = plane_flat(axis, interior_idx, a, b, ny, nz);
         if (!solid[fo]) {
-            float rn = 0.f;
+            R rn = R(0);
 #pragma unroll
             for (int q = 0; q < 19; ++q) {
                 const int cq = axis == 0 ? cx(q) : (axis == 1 ? cy(q) : cz(q));
-                float val = f[q * N + fo];
+                R val = f[q * N + fo];
                 if (cq == unknown_cax) { val = f[q * N + fi]; f[q * N + fo] = val; }
                 rn += val;
             }
@@ -298,9 +309,10 @@ __global__ void __launch_bounds__(BLOCK) k_convective_pass1(
 
 // Convective outlet, pass 2: every block reduces the partials in the same
 // order, then rescales its fluid outlet nodes by rho_out * count / sum(rho).
+template <class R>
 __global__ void __launch_bounds__(BLOCK) k_convective_pass2(
-    float* __restrict__ f, const uint8_t* __restrict__ solid, int nx, int ny, int nz, int axis,
-    int outlet_idx, float rho_out, int n1, int n2, const double* __restrict__ part_rho,
+    R* __restrict__ f, const uint8_t* __restrict__ solid, int nx, int ny, int nz, int axis,
+    int outlet_idx, double rho_out, int n1, int n2, const double* __restrict__ part_rho,
     const int* __restrict__ part_cnt, int n_parts) {
     __shared__ double s_rho[BLOCK];
     __shared__ int s_cnt[BLOCK];
@@ -322,7 +334,7 @@ __global__ void __launch_bounds__(BLOCK) k_convective_pass2(
     const int t = blockIdx.x * blockDim.x + threadIdx.x;
     if (t >= n1 * n2) return;
     if (cnt < 1 || sum < 1e-10) return;
-    const float corr = (float)((double)rho_out * (double)cnt / sum);
+    const R corr = (R)(rho_out * (double)cnt / sum);
     const int a = t / n2, b = t - (t / n2) * n2;
     const long long N = (long long)nx * ny * nz;
     const long long fo = plane_flat(axis, outlet_idx, a, b, ny, nz);
@@ -853,6 +865,111 @@ long long fc_lbm_convective_workspace_bytes(int n1, int n2) {
 int fc_lbm_convective_bc(float* f, const uint8_t* solid, int nx, int ny, int nz, int axis, int outlet_idx,
                          int interior_idx, int unknown_cax, float rho_out_lat, int n1, int n2,
                          void* workspace, long long workspace_bytes, void* stream) {
+    if (!f || !solid || !workspace || nx < 1 || ny < 1 || nz < 1) return FC_ERR_ARG;
+    int e1, e2;
+    if (plane_dims(axis, nx, ny, nz, &e1, &e2)) return FC_ERR_ARG;
+    if (e1 != n1 || e2 != n2) return FC_ERR_ARG;
+    const int na = axis == 0 ? nx : (axis == 1 ? ny : nz);
+    if (outlet_idx < 0 || outlet_idx >= na || interior_idx < 0 || interior_idx >= na) return FC_ERR_ARG;
+    if (unknown_cax != 1 && unknown_cax != -1) return FC_ERR_ARG;
+    if (workspace_bytes < fc_lbm_convective_workspace_bytes(n1, n2)) return FC_ERR_ARG;
+    if (reinterpret_cast<uintptr_t>(workspace) % 8 != 0) return FC_ERR_ARG;
+    const int nb = (int)grid_for((long long)n1 * n2);
+    double* part_rho = reinterpret_cast<double*>(workspace);
+    int* part_cnt = reinterpret_cast<int*>(part_rho + nb);
+    cudaStream_t st = (cudaStream_t)stream;
+    k_convective_pass1<<<nb, BLOCK, 0, st>>>(f, solid, nx, ny, nz, axis, outlet_idx, interior_idx, unknown_cax,
+                                             n1, n2, part_rho, part_cnt);
+    int rc = launch_status();
+    if (rc) return rc;
+    k_convective_pass2<<<nb, BLOCK, 0, st>>>(f, solid, nx, ny, nz, axis, outlet_idx, rho_out_lat, n1, n2,
+                                             part_rho, part_cnt, nb);
+    return launch_status();
+}
+
+// ---------------------------------------------------------------------------
+// FP64 run of the plain method: the per-operation kernels above instantiated
+// for double populations and macros (rates, sponge profile and link weights stay
+// the reference's FP32 values, promoted).  Same argument meaning and checks as
+// the FP32 entry points; collision selects BGK/TRT/MRT/MRT-Smagorinsky.
+// ---------------------------------------------------------------------------
+int fc_lbm64_macro_collide(int collision, const double* f, double* f_post, double* rho, double* u, double* v,
+                           double* w, const uint8_t* solid, float omega, float omega_plus, float omega_minus,
+                           const float* S_dev, float Cs_dx2, float omega0, long long n_cells, void* stream) {
+    if (!f || !f_post || !rho || !u || !v || !w || !solid || n_cells < 0) return FC_ERR_ARG;
+    if ((collision == CM_MRT || collision == CM_MRT_SMAG) && !S_dev) return FC_ERR_ARG;
+    if (n_cells == 0) return FC_OK;
+    CollideParams p{};
+    p.omega = omega; p.omega_plus = omega_plus; p.omega_minus = omega_minus;
+    p.Cs_dx2 = Cs_dx2; p.omega0 = omega0;
+    cudaStream_t st = (cudaStream_t)stream;
+    const unsigned g = grid_for(n_cells);
+    switch (collision) {
+        case CM_BGK: k_macro_collide<CM_BGK><<<g, BLOCK, 0, st>>>(f, f_post, rho, u, v, w, solid, p, nullptr, n_cells); break;
+        case CM_TRT: k_macro_collide<CM_TRT><<<g, BLOCK, 0, st>>>(f, f_post, rho, u, v, w, solid, p, nullptr, n_cells); break;
+        case CM_MRT: k_macro_collide<CM_MRT><<<g, BLOCK, 0, st>>>(f, f_post, rho, u, v, w, solid, p, S_dev, n_cells); break;
+        case CM_MRT_SMAG:
+            k_macro_collide<CM_MRT_SMAG><<<g, BLOCK, 0, st>>>(f, f_post, rho, u, v, w, solid, p, S_dev, n_cells);
+            break;
+        default: return FC_ERR_ARG;
+    }
+    return launch_status();
+}
+
+int fc_lbm64_stream_pull(const double* f_in, double* f_out, int nx, int ny, int nz, int px, int py, int pz,
+                         void* stream) {
+    if (!f_in || !f_out || nx < 1 || ny < 1 || nz < 1 || f_in == f_out) return FC_ERR_ARG;
+    const long long N = (long long)nx * ny * nz;
+    k_stream_pull<<<grid_for(N), BLOCK, 0, (cudaStream_t)stream>>>(f_in, f_out, nx, ny, nz, px, py, pz);
+    return launch_status();
+}
+
+int fc_lbm64_sponge(double* f, const double* rho, const double* u, const double* v, const double* w,
+                    const float* sigma, long long n_cells, void* stream) {
+    if (!f || !rho || !u || !v || !w || !sigma || n_cells < 0) return FC_ERR_ARG;
+    if (n_cells == 0) return FC_OK;
+    k_sponge<<<grid_for(n_cells), BLOCK, 0, (cudaStream_t)stream>>>(f, rho, u, v, w, sigma, n_cells);
+    return launch_status();
+}
+
+int fc_lbm64_ibb(const double* f_post, double* f_stream, const int32_t* fluid_flat, const int32_t* dir_i,
+                 const int32_t* dir_opp, const float* w1, const float* w2, const uint8_t* q_ge_half,
+                 const int32_t* ff_flat, const uint8_t* ff_valid, long long n_links, long long n_cells,
+                 unsigned* dev_err, void* stream) {
+    if (n_links < 0 || n_cells < 0) return FC_ERR_ARG;
+    if (n_links == 0) return FC_OK;
+    if (!f_post || !f_stream || !fluid_flat || !dir_i || !dir_opp || !w1 || !w2 || !q_ge_half || !ff_flat ||
+        !ff_valid)
+        return FC_ERR_ARG;
+    k_ibb_links<<<grid_for(n_links), BLOCK, 0, (cudaStream_t)stream>>>(
+        f_post, f_stream, fluid_flat, dir_i, dir_opp, w1, w2, q_ge_half, ff_flat, ff_valid, n_links, n_cells,
+        dev_err);
+    return launch_status();
+}
+
+int fc_lbm64_reset_solid(double* f, const uint8_t* solid, long long n_cells, void* stream) {
+    if (!f || !solid || n_cells < 0) return FC_ERR_ARG;
+    if (n_cells == 0) return FC_OK;
+    k_reset_solid<<<grid_for(n_cells), BLOCK, 0, (cudaStream_t)stream>>>(f, solid, n_cells);
+    return launch_status();
+}
+
+int fc_lbm64_zou_he_bc(double* f, const uint8_t* solid, int nx, int ny, int nz, int axis, int plane_idx,
+                       int interior_idx, int bc_type, double u_in_lat, double rho_out_lat, int sign, void* stream) {
+    int n1, n2;
+    if (!f || !solid || nx < 1 || ny < 1 || nz < 1) return FC_ERR_ARG;
+    if (plane_dims(axis, nx, ny, nz, &n1, &n2)) return FC_ERR_ARG;
+    const int na = axis == 0 ? nx : (axis == 1 ? ny : nz);
+    if (plane_idx < 0 || plane_idx >= na || interior_idx < 0 || interior_idx >= na) return FC_ERR_ARG;
+    if (bc_type != 0 && bc_type != 1) return FC_ERR_ARG;
+    k_zou_he<<<grid_for((long long)n1 * n2), BLOCK, 0, (cudaStream_t)stream>>>(
+        f, solid, nx, ny, nz, axis, plane_idx, interior_idx, bc_type, u_in_lat, rho_out_lat, sign, n1, n2);
+    return launch_status();
+}
+
+int fc_lbm64_convective_bc(double* f, const uint8_t* solid, int nx, int ny, int nz, int axis, int outlet_idx,
+                           int interior_idx, int unknown_cax, double rho_out_lat, int n1, int n2, void* workspace,
+                           long long workspace_bytes, void* stream) {
     if (!f || !solid || !workspace || nx < 1 || ny < 1 || nz < 1) return FC_ERR_ARG;
     int e1, e2;
     if (plane_dims(axis, nx, ny, nz, &e1, &e2)) return FC_ERR_ARG;

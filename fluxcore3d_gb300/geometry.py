@@ -148,14 +148,24 @@ def ibb_from_voxels(solid: torch.Tensor, pitch: float = 1.0, origin=(0.0, 0.0, 0
 def ibb_from_level_set(solid: torch.Tensor, levelset, n_bisect: int = 40) -> IBBData:
     """Links of `solid` with q from an analytic level set G(x) (negative = fluid, positive =
     solid, G(cell centre) > 0 <=> solid), refined by FP64 bisection to the exact crossing."""
-    dev = solid.device
-    nx, ny, nz = solid.shape
     ff, di, do, fff, fv = build_links(solid)
+    q = level_set_fractions(levelset, ff, di, solid.shape, n_bisect)
+    ge, w1, w2 = bfl_weights_from_q(q)
+    return IBBData(int(ff.numel()), ff, di, do, ge, w1, w2, fff, fv)
+
+
+def level_set_fractions(levelset, fluid_flat: torch.Tensor, dir_i: torch.Tensor, shape,
+                        n_bisect: int = 40) -> torch.Tensor:
+    """FP32 link fractions q in (0, 1]: FP64 bisection of G along x_f + t c_q for t in [0, 1] (the
+    crossing lies in that interval because x_f is fluid and x_f + c_q solid), on the links' device."""
+    dev = fluid_flat.device
+    nx, ny, nz = shape
+    ff = fluid_flat
     i = (ff // (ny * nz)).to(torch.float64)
     j = ((ff // nz) % ny).to(torch.float64)
     k = (ff % nz).to(torch.float64)
     x0 = torch.stack([i, j, k], dim=1)
-    c = torch.tensor(C_NP, device=dev, dtype=torch.float64)[di]
+    c = torch.tensor(C_NP, device=dev, dtype=torch.float64)[dir_i]
     lo = torch.zeros(ff.numel(), device=dev, dtype=torch.float64)
     hi = torch.ones_like(lo)
     for _ in range(n_bisect):
@@ -163,9 +173,7 @@ def ibb_from_level_set(solid: torch.Tensor, levelset, n_bisect: int = 40) -> IBB
         inside = levelset(x0 + mid[:, None] * c) > 0
         hi = torch.where(inside, mid, hi)
         lo = torch.where(inside, lo, mid)
-    q = hi.clamp(1e-6, 1.0).to(torch.float32)
-    ge, w1, w2 = bfl_weights_from_q(q)
-    return IBBData(int(ff.numel()), ff, di, do, ge, w1, w2, fff, fv)
+    return hi.clamp(1e-6, 1.0).to(torch.float32)
 
 
 # --------------------------------------------------------------------------

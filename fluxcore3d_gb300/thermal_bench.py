@@ -32,6 +32,8 @@ def thermal_system(sim, u, v, w, dt=1000.0, flux=5e-3):
     mg = NLevelGeometricMGSolver(dev, torch.float32, 0, +1, 1.0, omega=0.6, n_pre=2, n_post=2, n_coarse=20)
     vel = []
     for t in (u, v, w):
+        if not bool(torch.isfinite(t).all()):
+            raise ValueError("thermal_system: the velocity field is not finite (did the lattice run diverge?)")
         t = t.to(device=dev, dtype=torch.float32).clone()
         t[sim.solid_flow] = 0.0
         vel.append(t)
@@ -40,9 +42,11 @@ def thermal_system(sim, u, v, w, dt=1000.0, flux=5e-3):
 
 
 def build_system(dev, nx=256, ny=128, nz=128, lbm_steps=3000, dt=1000.0, flux=5e-3, k_ratio=200.0):
+    """Velocity from `lbm_steps` steps of the FP16 lattice with MRT-Smagorinsky (plain MRT at Re = 200
+    on this pin fin diverges after about 600 steps), then the thermal system on it."""
     from . import case as cases
     from .solver.lbm_cuda_ext import LBMCUDAUpgrade
-    sim = cases.pin_fin(device=dev, nx=nx, ny=ny, nz=nz, storage="fp16", k_ratio=k_ratio)
+    sim = cases.pin_fin(device=dev, nx=nx, ny=ny, nz=nz, storage="fp16", collision="mrt_smag", k_ratio=k_ratio)
     LBMCUDAUpgrade.patch(sim)
     for _ in range(lbm_steps):
         sim.step(do_thermal=False)

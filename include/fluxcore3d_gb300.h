@@ -71,6 +71,28 @@ long long fc_lbm_convective_workspace_bytes(int n1, int n2);
 int fc_lbm_convective_bc(float* f, const uint8_t* solid, int nx, int ny, int nz, int axis, int outlet_idx,
                          int interior_idx, int unknown_cax, float rho_out_lat, int n1, int n2,
                          void* workspace, long long workspace_bytes, void* stream);
+/* FP64 run of the plain method: the per-operation kernels above on double populations and
+ * macros, for reporting the error of the FP32 and FP16/BF16 runs against an FP64 run of the
+ * same step sequence (no counterpart in the reference, which is FP32 only).  Rates, sponge
+ * profile and link weights keep their FP32 values.  collision: 0 BGK, 1 TRT, 2 MRT, 3 MRT +
+ * Smagorinsky; S_dev (19 floats on the device) is read for 2 and 3. */
+int fc_lbm64_macro_collide(int collision, const double* f, double* f_post, double* rho, double* u, double* v,
+                           double* w, const uint8_t* solid, float omega, float omega_plus, float omega_minus,
+                           const float* S_dev, float Cs_dx2, float omega0, long long n_cells, void* stream);
+int fc_lbm64_stream_pull(const double* f_in, double* f_out, int nx, int ny, int nz, int px, int py, int pz,
+                         void* stream);
+int fc_lbm64_sponge(double* f, const double* rho, const double* u, const double* v, const double* w,
+                    const float* sigma, long long n_cells, void* stream);
+int fc_lbm64_ibb(const double* f_post, double* f_stream, const int32_t* fluid_flat, const int32_t* dir_i,
+                 const int32_t* dir_opp, const float* w1, const float* w2, const uint8_t* q_ge_half,
+                 const int32_t* ff_flat, const uint8_t* ff_valid, long long n_links, long long n_cells,
+                 unsigned* dev_err, void* stream);
+int fc_lbm64_reset_solid(double* f, const uint8_t* solid, long long n_cells, void* stream);
+int fc_lbm64_zou_he_bc(double* f, const uint8_t* solid, int nx, int ny, int nz, int axis, int plane_idx,
+                       int interior_idx, int bc_type, double u_in_lat, double rho_out_lat, int sign, void* stream);
+int fc_lbm64_convective_bc(double* f, const uint8_t* solid, int nx, int ny, int nz, int axis, int outlet_idx,
+                           int interior_idx, int unknown_cax, double rho_out_lat, int n1, int n2, void* workspace,
+                           long long workspace_bytes, void* stream);
 /* Convective outlet that allocates nothing: no counterpart in the reference.  For callers
  * that may not allocate device memory once their time loop runs (a host that hands out all
  * GPU memory from its own pre-reserved arena, or a path where an allocation would

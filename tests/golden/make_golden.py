@@ -278,14 +278,19 @@ def tracer(ref_root: str):
 
 
 if __name__ == "__main__":
-    args = [a for a in sys.argv[1:] if not a.startswith("--")]
-    root = args[0] if args else "/root/reference"
-    only = sys.argv[sys.argv.index("--only") + 1] if "--only" in sys.argv else None
-    if only == "ibb_pitch":
+    import argparse
+    ap = argparse.ArgumentParser(description=__doc__.splitlines()[0])
+    ap.add_argument("reference_root", help="root of the fluxcore3D source tree (read only)")
+    ap.add_argument("--only", choices=("main", "ibb_pitch", "voxels", "tracer"), default=None)
+    a = ap.parse_args()
+    root = a.reference_root
+    if a.only == "main":
+        main(root)
+    elif a.only == "ibb_pitch":
         ibb_pitch(root)
-    elif only == "voxels":
+    elif a.only == "voxels":
         voxels(root)
-    elif only == "tracer":
+    elif a.only == "tracer":
         tracer(root)
     else:
         main(root)
