@@ -113,12 +113,14 @@ __global__ void __launch_bounds__(BLOCK) k_mop_t(const T* __restrict__ x, const 
     const int jN = j < g.ny - 1 ? j + 1 : j - 1, jS = j > 0 ? j - 1 : lowg(g, 1);
     const int kU = k < g.nz - 1 ? k + 1 : k - 1, kD = k > 0 ? k - 1 : lowg(g, 2);
     const T xc = x[idx];
-    const T L = (T)diagL[idx] * xc - (T)aE[idx] * x[iE * nynz + (long long)j * g.nz + k] -
-                (T)aW[idx] * x[iW * nynz + (long long)j * g.nz + k] -
-                (T)aN[idx] * x[i * nynz + (long long)jN * g.nz + k] -
-                (T)aS[idx] * x[i * nynz + (long long)jS * g.nz + k] -
-                (T)aU[idx] * x[i * nynz + (long long)j * g.nz + kU] -
-                (T)aD[idx] * x[i * nynz + (long long)j * g.nz + kD];
+    // flux form sum_n a_n (x_c - x_n): exact on constant fields (diagL = sum_n a_n is
+    // not, once rounded to FP32), as in the multigrid kernels
+    const T L = (T)aE[idx] * (xc - x[iE * nynz + (long long)j * g.nz + k]) +
+                (T)aW[idx] * (xc - x[iW * nynz + (long long)j * g.nz + k]) +
+                (T)aN[idx] * (xc - x[i * nynz + (long long)jN * g.nz + k]) +
+                (T)aS[idx] * (xc - x[i * nynz + (long long)jS * g.nz + k]) +
+                (T)aU[idx] * (xc - x[i * nynz + (long long)j * g.nz + kU]) +
+                (T)aD[idx] * (xc - x[i * nynz + (long long)j * g.nz + kD]);
     T m = xc + dt * L;
     if (b) m = b[idx] - m;
     if (mask && mask[idx] == 0.f) m = (T)0;

@@ -4,6 +4,13 @@
 // Operator (reference solver/nlevel_mg_cuda.py:417-507 and mg_kernels.cu:55-106):
 //   L(T)_c = diagL_c T_c - sum_n a_n,c T_n          (7-point, per-cell a_E..a_D)
 //   M(T)   = T + dt L(T)                             ("mop")
+// with diagL = sum_n a_n.  Every kernel here evaluates L in the equivalent
+// flux form sum_n a_n,c (T_c - T_n): in FP32 the rounded diagL differs from the
+// sum of the rounded a_n by up to an ulp, so the reference's form applies a
+// spurious source (diagL - sum a_n) T_c that is proportional to the absolute
+// temperature (T ~ 25 against a rise of ~2) and biases the steady state by a
+// few 1e-6 relative; the flux form is exact on constant fields.  diagL is still
+// used for the Jacobi weights, as in the reference.
 // Ghost cells: the high face of every axis mirrors the cell below it; the low
 // face mirrors the cell above it except on the flow axis when the inlet sits at
 // index 0, where the cell itself is the ghost (mg_kernels.cu:37-44).
@@ -64,17 +71,17 @@ struct Coef {
 // The 7-point operator and the damped-Jacobi update with every rounding
 // explicit (no compiler contraction), so the one-cell, two-cell and
 // single-CTA smoothers give the same bits:
-//   L  = dg*xc - aE*xe - aW*xw - aN*xn - aS*xs - aU*xu - aD*xd  (left to right)
+//   L  = aE*(xc-xe) + aW*(xc-xw) + aN*(xc-xn) + aS*(xc-xs) + aU*(xc-xu) + aD*(xc-xd)
+//        (left to right, each product fused into the running sum)
 //   lo = xc + dt*L,  x' = xc + inv*(b - lo),  r = b - lo.
-__device__ __forceinline__ float stencil_L(float dg, float xc, float ae, float xe, float aw, float xw, float an,
-                                           float xn, float as, float xs, float au, float xu, float ad, float xd) {
-    float s = __fmul_rn(dg, xc);
-    s = __fmaf_rn(-ae, xe, s);
-    s = __fmaf_rn(-aw, xw, s);
-    s = __fmaf_rn(-an, xn, s);
-    s = __fmaf_rn(-as, xs, s);
-    s = __fmaf_rn(-au, xu, s);
-    return __fmaf_rn(-ad, xd, s);
+__device__ __forceinline__ float stencil_L(float xc, float ae, float xe, float aw, float xw, float an, float xn,
+                                           float as, float xs, float au, float xu, float ad, float xd) {
+    float s = __fmul_rn(ae, __fsub_rn(xc, xe));
+    s = __fmaf_rn(aw, __fsub_rn(xc, xw), s);
+    s = __fmaf_rn(an, __fsub_rn(xc, xn), s);
+    s = __fmaf_rn(as, __fsub_rn(xc, xs), s);
+    s = __fmaf_rn(au, __fsub_rn(xc, xu), s);
+    return __fmaf_rn(ad, __fsub_rn(xc, xd), s);
 }
 __device__ __forceinline__ float m_apply(float xc, float dt, float L) { return __fmaf_rn(dt, L, xc); }
 __device__ __forceinline__ float jacobi(float xc, float iv, float bc, float lo) {
@@ -82,7 +89,7 @@ __device__ __forceinline__ float jacobi(float xc, float iv, float bc, float lo) 
 }
 
 __device__ __forceinline__ float apply_Lf(const Coef& a, const float* __restrict__ x, const Nb7& n, float xc) {
-    return stencil_L(__ldg(a.diagL + n.c), xc, __ldg(a.aE + n.c), x[n.e], __ldg(a.aW + n.c), x[n.w],
+    return stencil_L(xc, __ldg(a.aE + n.c), x[n.e], __ldg(a.aW + n.c), x[n.w],
                      __ldg(a.aN + n.c), x[n.n], __ldg(a.aS + n.c), x[n.s], __ldg(a.aU + n.c), x[n.u],
                      __ldg(a.aD + n.c), x[n.d]);
 }
@@ -162,7 +169,7 @@ __global__ void __launch_bounds__(BLOCK) k_smooth_first2(float* __restrict__ xo,
     const Nb7 nb = nb7(g, i, j, k);
     auto x1 = [&](long long q) { return jacobi(0.f, __ldg(inv + q), __ldg(b + q), 0.f); };
     const float tc = x1(nb.c);
-    const float L = stencil_L(__ldg(a.diagL + nb.c), tc, __ldg(a.aE + nb.c), x1(nb.e), __ldg(a.aW + nb.c), x1(nb.w),
+    const float L = stencil_L(tc, __ldg(a.aE + nb.c), x1(nb.e), __ldg(a.aW + nb.c), x1(nb.w),
                               __ldg(a.aN + nb.c), x1(nb.n), __ldg(a.aS + nb.c), x1(nb.s), __ldg(a.aU + nb.c),
                               x1(nb.u), __ldg(a.aD + nb.c), x1(nb.d));
     xo[idx] = jacobi(tc, __ldg(inv + idx), __ldg(b + idx), m_apply(tc, dt, L));
@@ -221,11 +228,11 @@ __global__ void __launch_bounds__(PAIR_X * PAIR_Y) k_smooth2(const float* __rest
     };
     const float2 xc = X2(p.c), xe = X2(p.e), xw = X2(p.w), xn = X2(p.n), xs = X2(p.s);
     const float xd0 = X1(p.d0), xu1 = X1(p.u1);
-    const float2 dg = ld2(a.diagL, p.c), ae = ld2(a.aE, p.c), aw = ld2(a.aW, p.c), an = ld2(a.aN, p.c);
+    const float2 ae = ld2(a.aE, p.c), aw = ld2(a.aW, p.c), an = ld2(a.aN, p.c);
     const float2 as = ld2(a.aS, p.c), au = ld2(a.aU, p.c), ad = ld2(a.aD, p.c);
     const float2 iv = ld2(inv, p.c), bc = ld2(b, p.c);
-    const float L0 = stencil_L(dg.x, xc.x, ae.x, xe.x, aw.x, xw.x, an.x, xn.x, as.x, xs.x, au.x, xc.y, ad.x, xd0);
-    const float L1 = stencil_L(dg.y, xc.y, ae.y, xe.y, aw.y, xw.y, an.y, xn.y, as.y, xs.y, au.y, xu1, ad.y, xc.x);
+    const float L0 = stencil_L(xc.x, ae.x, xe.x, aw.x, xw.x, an.x, xn.x, as.x, xs.x, au.x, xc.y, ad.x, xd0);
+    const float L1 = stencil_L(xc.y, ae.y, xe.y, aw.y, xw.y, an.y, xn.y, as.y, xs.y, au.y, xu1, ad.y, xc.x);
     *reinterpret_cast<float2*>(xo + p.c) = make_float2(jacobi(xc.x, iv.x, bc.x, m_apply(xc.x, dt, L0)),
                                                        jacobi(xc.y, iv.y, bc.y, m_apply(xc.y, dt, L1)));
 }
@@ -255,19 +262,19 @@ __global__ void __launch_bounds__(SMALL_THREADS) k_smooth_small(float* __restric
         const int c = threadIdx.x;
         const bool act = c < n;
         Nb7 nb{0, 0, 0, 0, 0, 0, 0};
-        float dg = 0.f, ae = 0.f, aw = 0.f, an = 0.f, as = 0.f, au = 0.f, ad = 0.f, iv = 0.f, bc = 0.f;
+        float ae = 0.f, aw = 0.f, an = 0.f, as = 0.f, au = 0.f, ad = 0.f, iv = 0.f, bc = 0.f;
         if (act) {
             int i, j, k;
             coords(g, c, i, j, k);
             nb = nb7(g, i, j, k);
-            dg = __ldg(a.diagL + c); ae = __ldg(a.aE + c); aw = __ldg(a.aW + c); an = __ldg(a.aN + c);
+            ae = __ldg(a.aE + c); aw = __ldg(a.aW + c); an = __ldg(a.aN + c);
             as = __ldg(a.aS + c); au = __ldg(a.aU + c); ad = __ldg(a.aD + c);
             iv = __ldg(inv + c); bc = __ldg(b + c);
         }
         for (int sw = s0; sw < n_sweeps; ++sw) {
             if (act) {
                 const float tc = cur[c];
-                const float L = stencil_L(dg, tc, ae, cur[nb.e], aw, cur[nb.w], an, cur[nb.n], as, cur[nb.s], au,
+                const float L = stencil_L(tc, ae, cur[nb.e], aw, cur[nb.w], an, cur[nb.n], as, cur[nb.s], au,
                                           cur[nb.u], ad, cur[nb.d]);
                 nxt[c] = jacobi(tc, iv, bc, m_apply(tc, dt, L));
             }
@@ -504,8 +511,8 @@ __global__ void __launch_bounds__(BLOCK) k_residual_sq(const float* __restrict__
 
 // Heat-balance integrals in FP64 over the non-Dirichlet cells (mask != 0):
 // part[3 b + 0] = sum src, [3 b + 1] = sum L(T) (the operator's net outflow of
-// heat, boundary fluxes included), [3 b + 2] = sum T.  L in FP64 from the FP32
-// coefficients and temperatures.
+// heat, boundary fluxes included), [3 b + 2] = sum T.  L in FP64 (flux form)
+// from the FP32 coefficients and temperatures.
 __global__ void __launch_bounds__(BLOCK) k_heat_balance(const float* __restrict__ T, const float* __restrict__ src,
                                                         const float* __restrict__ mask, Coef a, Lvl g,
                                                         double* __restrict__ part) {
@@ -517,10 +524,9 @@ __global__ void __launch_bounds__(BLOCK) k_heat_balance(const float* __restrict_
         coords(g, idx, i, j, k);
         const Nb7 n = nb7(g, i, j, k);
         const double tc = T[idx];
-        vl = (double)__ldg(a.diagL + idx) * tc - (double)__ldg(a.aE + idx) * (double)T[n.e] -
-             (double)__ldg(a.aW + idx) * (double)T[n.w] - (double)__ldg(a.aN + idx) * (double)T[n.n] -
-             (double)__ldg(a.aS + idx) * (double)T[n.s] - (double)__ldg(a.aU + idx) * (double)T[n.u] -
-             (double)__ldg(a.aD + idx) * (double)T[n.d];
+        vl = (double)__ldg(a.aE + idx) * (tc - (double)T[n.e]) + (double)__ldg(a.aW + idx) * (tc - (double)T[n.w]) +
+             (double)__ldg(a.aN + idx) * (tc - (double)T[n.n]) + (double)__ldg(a.aS + idx) * (tc - (double)T[n.s]) +
+             (double)__ldg(a.aU + idx) * (tc - (double)T[n.u]) + (double)__ldg(a.aD + idx) * (tc - (double)T[n.d]);
         vs = src ? (double)__ldg(src + idx) : 0.0;
         vt = tc;
     }

@@ -123,10 +123,13 @@ __global__ void __launch_bounds__(BLOCK) k_steady_part(const float* __restrict__
         const int jN = j < g.ny - 1 ? j + 1 : j - 1, jS = j > 0 ? j - 1 : lowg(g, 1);
         const int kU = k < g.nz - 1 ? k + 1 : k - 1, kD = k > 0 ? k - 1 : lowg(g, 2);
         const float tc = T[idx];
-        const float L = diagL[idx] * tc - aE[idx] * T[iE * nynz + (long long)j * g.nz + k] -
-                        aW[idx] * T[iW * nynz + (long long)j * g.nz + k] - aN[idx] * T[i * nynz + (long long)jN * g.nz + k] -
-                        aS[idx] * T[i * nynz + (long long)jS * g.nz + k] - aU[idx] * T[i * nynz + (long long)j * g.nz + kU] -
-                        aD[idx] * T[i * nynz + (long long)j * g.nz + kD];
+        // flux form, as in the multigrid kernels (exact on constant fields)
+        const float L = aE[idx] * (tc - T[iE * nynz + (long long)j * g.nz + k]) +
+                        aW[idx] * (tc - T[iW * nynz + (long long)j * g.nz + k]) +
+                        aN[idx] * (tc - T[i * nynz + (long long)jN * g.nz + k]) +
+                        aS[idx] * (tc - T[i * nynz + (long long)jS * g.nz + k]) +
+                        aU[idx] * (tc - T[i * nynz + (long long)j * g.nz + kU]) +
+                        aD[idx] * (tc - T[i * nynz + (long long)j * g.nz + kD]);
         const float lo = tc + dt * L;
         const float LT = (lo - tc) / dt;
         const float ss = src[idx] / dt;

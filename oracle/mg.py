@@ -95,8 +95,9 @@ class OracleMG:
     """NLevelGeometricMGSolver (nlevel_mg_cuda.py:38-307) on numpy arrays."""
 
     def __init__(self, k, rcp, u, v, w, mask, ax, sign, s, omega=0.8, n_pre=2, n_post=2, n_coarse=20,
-                 min_coarse_cells=4, max_levels=None, real=np.float64):
+                 min_coarse_cells=4, max_levels=None, real=np.float64, flux=False):
         self.dt_ = real
+        self.flux = flux
         self.ax, self.sign, self.s, self.omega = ax, sign, s, omega
         self.n_pre, self.n_post, self.n_coarse = n_pre, n_post, n_coarse
         self.levels = []
@@ -125,8 +126,18 @@ class OracleMG:
             lv["inv"] = (r(self.omega) / d) * lv["mask"]
 
     def L(self, lv, x):
+        """The 7-point operator.  flux=False: diag*x - sum_n a_n x_n, the reference's form
+        (mg_kernels.cu:55-106); flux=True: sum_n a_n (x - x_n), equal in exact arithmetic
+        (diag = sum_n a_n) and the form the CUDA kernels evaluate, which stays exact on
+        constant fields once the coefficients are rounded."""
         a = lv["a"]
         ax, oi = self.ax, lv["out_idx"]
+        if self.flux:
+            s = None
+            for name, dim, st in (("E", 0, 1), ("W", 0, -1), ("N", 1, 1), ("S", 1, -1), ("U", 2, 1), ("D", 2, -1)):
+                t = a[name] * (x - shift(x, dim, st, ax, oi))
+                s = t if s is None else s + t
+            return s
         return (lv["diag"] * x - a["E"] * shift(x, 0, 1, ax, oi) - a["W"] * shift(x, 0, -1, ax, oi)
                 - a["N"] * shift(x, 1, 1, ax, oi) - a["S"] * shift(x, 1, -1, ax, oi)
                 - a["U"] * shift(x, 2, 1, ax, oi) - a["D"] * shift(x, 2, -1, ax, oi))

@@ -52,9 +52,10 @@ def test_heat_balance_integrals_and_closure(cuda):
     a = {key: lv[key].cpu().numpy().astype(np.float64) for key in ("aE", "aW", "aN", "aS", "aU", "aD", "diagL")}
     Tn = T.cpu().numpy().astype(np.float64)
     ax, oi = mg.ax, lv["out_idx"]
-    L = (a["diagL"] * Tn - a["aE"] * shift(Tn, 0, 1, ax, oi) - a["aW"] * shift(Tn, 0, -1, ax, oi)
-         - a["aN"] * shift(Tn, 1, 1, ax, oi) - a["aS"] * shift(Tn, 1, -1, ax, oi)
-         - a["aU"] * shift(Tn, 2, 1, ax, oi) - a["aD"] * shift(Tn, 2, -1, ax, oi))
+    # the operator in flux form sum_n a_n (T - T_n), as the kernels evaluate it
+    L = (a["aE"] * (Tn - shift(Tn, 0, 1, ax, oi)) + a["aW"] * (Tn - shift(Tn, 0, -1, ax, oi))
+         + a["aN"] * (Tn - shift(Tn, 1, 1, ax, oi)) + a["aS"] * (Tn - shift(Tn, 1, -1, ax, oi))
+         + a["aU"] * (Tn - shift(Tn, 2, 1, ax, oi)) + a["aD"] * (Tn - shift(Tn, 2, -1, ax, oi)))
     m = mask.cpu().numpy()
     assert abs(hb["heat_out_through_boundaries"] - L[m].sum()) <= 1e-9 * np.abs(L[m]).sum()
     assert abs(hb["heat_generated"] - src.cpu().numpy().astype(np.float64)[m].sum()) <= 1e-9 * hb["heat_generated"]

@@ -44,7 +44,7 @@ def both(prob, ax=0, sign=1, dt=3.0, s=1.0, **kw):
     mg = NLevelGeometricMGSolver(dev, torch.float32, ax, sign, s, omega=0.6, **kw)
     T = lambda a: torch.tensor(a, device=dev)
     mg.build_if_needed(T(k), T(rcp), T(u), T(v), T(w), T(mask), dt)
-    ref = omg.OracleMG(k, rcp, u, v, w, mask, ax, sign, s, omega=0.6, real=np.float32, **kw)
+    ref = omg.OracleMG(k, rcp, u, v, w, mask, ax, sign, s, omega=0.6, real=np.float32, flux=True, **kw)
     ref.set_dt(dt)
     return mg, ref
 
@@ -232,7 +232,7 @@ def test_thermal_pseudo_time_steps_match_oracle(cuda):
     patch_thermal_fused(sim)
     ref = omg.OracleMG(sim.k.cpu().numpy(), sim.rho_cp.cpu().numpy(), sim.u.cpu().numpy(), sim.v.cpu().numpy(),
                        sim.wv.cpu().numpy(), sim._build_update_mask_thermal().cpu().numpy(), 0, 1, 1.0, omega=0.6,
-                       real=np.float32)
+                       real=np.float32, flux=True)
     T = sim.T.cpu().numpy()
     T0 = sim._build_T_dirichlet_field().cpu().numpy()
     mask = sim._build_update_mask_thermal().cpu().numpy()

@@ -199,3 +199,17 @@ def test_tracer_oracle_matches_reference():
         if it == 0:
             assert np.array_equal(phi.view(np.uint32), d["field1"].view(np.uint32))
     assert np.array_equal(phi.view(np.uint32), d["field25"].view(np.uint32))
+
+
+def test_oracle_flux_form_equals_reference_form_in_fp64():
+    """The flux form of the operator (sum_n a_n (T - T_n), what the CUDA kernels evaluate) equals the
+    reference's diag*T - sum_n a_n T_n in FP64 on the golden multigrid problem: same operator."""
+    d = load("mg_solve.npz")
+    args = (d["k"], d["rcp"], d["u"], d["v"], d["w"], d["mask"], 0, 1, float(d["s"]))
+    ref = omg.OracleMG(*args, omega=0.6, real=np.float64)
+    flx = omg.OracleMG(*args, omega=0.6, real=np.float64, flux=True)
+    T = np.random.default_rng(0).random(d["k"].shape) + 25.0
+    for lr, lf in zip(ref.levels, flx.levels):
+        Tl = T[tuple(slice(0, n) for n in lr["shape"])]
+        a, b = ref.L(lr, Tl), flx.L(lf, Tl)
+        assert float(np.abs(a - b).max()) <= 1e-12 * float(np.abs(a).max() + 1.0)
