@@ -129,6 +129,9 @@ SIGNATURES: dict[str, tuple] = {
     "fc_mg_build_coeffs": (i32, [vp] * 5 + [i32, i32, i32, i32, i32, f32, f32] + [vp] * 7 + [vp]),
     "fc_mg_restrict_mean": (i32, [vp, i32, i32, i32, vp, i32, vp]),
     "fc_mg_inv_diag": (i32, [vp, vp, vp, f32, f32, i64, vp]),
+    "fc_mg_coarse_dense_bytes": (i64, [i32, i32, i32]),
+    "fc_mg_coarse_dense_build": (i32, [vp, vp, vp, vp, vp, vp, vp, vp, f32, i32, i32, i32, i32, i32, vp, i64, vp]),
+    "fc_mg_coarse_dense_apply": (i32, [vp, vp, vp, vp, i32, vp]),
     # krylov
     "fc_vec_workspace_bytes": (i64, [i64]),
     "fc_vec_dot": (i32, [i32, vp, vp, i64, vp, vp, i64, vp, vp]),

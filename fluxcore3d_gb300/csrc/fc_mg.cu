@@ -635,6 +635,88 @@ __global__ void __launch_bounds__(BLOCK) k_inv_diag(const float* __restrict__ di
     inv[idx] = (omega / d) * mask[idx];
 }
 
+// ---- FP64 exact solve of the coarsest level ---------------------------------
+// A = I + dt L of the level in FP64 (built from the FP32 couplings with the
+// operator's ghosting, diagonal = 1 + dt sum_n a_n as in the flux form; rows of
+// Dirichlet cells are identity rows), inverted in place by Gauss-Jordan
+// elimination without pivoting: A is strictly diagonally dominant by rows
+// (1 + dt sum_n a_n against dt sum_n a_n), so every pivot is positive and no
+// growth occurs.  One launch per pivot updates every element; the pivot row and
+// column it needs are double-buffered copies written by the previous launch,
+// so no element is read after another thread overwrote it.
+constexpr int CD_MAX_CELLS = 4096;
+constexpr int CD_TX = 32, CD_TY = 8;
+
+__global__ void __launch_bounds__(BLOCK) k_cd_assemble(Coef a, const float* __restrict__ mask, double dt, Lvl g,
+                                                       double* __restrict__ A, int n) {
+    const int c = blockIdx.x * blockDim.x + threadIdx.x;
+    if (c >= n) return;
+    double* row = A + (long long)c * n;
+    if (mask[c] == 0.f) {
+        row[c] = 1.0;
+        return;
+    }
+    int i, j, k;
+    coords(g, c, i, j, k);
+    const Nb7 nb = nb7(g, i, j, k);
+    // a ghost neighbour can be the cell itself or another neighbour: accumulate
+    const double ae = __ldg(a.aE + c), aw = __ldg(a.aW + c), an = __ldg(a.aN + c);
+    const double as = __ldg(a.aS + c), au = __ldg(a.aU + c), ad = __ldg(a.aD + c);
+    row[c] += 1.0 + dt * (ae + aw + an + as + au + ad);
+    row[nb.e] -= dt * ae;
+    row[nb.w] -= dt * aw;
+    row[nb.n] -= dt * an;
+    row[nb.s] -= dt * as;
+    row[nb.u] -= dt * au;
+    row[nb.d] -= dt * ad;
+}
+
+// row and column 0 into the first buffer pair
+__global__ void __launch_bounds__(BLOCK) k_cd_seed(const double* __restrict__ A, int n, double* __restrict__ row,
+                                                   double* __restrict__ col) {
+    const int t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= n) return;
+    row[t] = A[t];
+    col[t] = A[(long long)t * n];
+}
+
+// One Gauss-Jordan step on pivot p (row/col: row p and column p before the step);
+// also stores row p+1 and column p+1 after the step into the other buffers.
+__global__ void __launch_bounds__(CD_TX * CD_TY) k_cd_pivot(double* __restrict__ A, int n, int p,
+                                                             const double* __restrict__ row,
+                                                             const double* __restrict__ col,
+                                                             double* __restrict__ row_next,
+                                                             double* __restrict__ col_next) {
+    const int j = blockIdx.x * CD_TX + threadIdx.x;
+    const int i = blockIdx.y * CD_TY + threadIdx.y;
+    if (i >= n || j >= n) return;
+    const double inv = 1.0 / row[p];
+    double v;
+    if (i == p) v = (j == p) ? inv : row[j] * inv;
+    else if (j == p) v = -col[i] * inv;
+    else v = fma(-col[i], row[j] * inv, A[(long long)i * n + j]);
+    A[(long long)i * n + j] = v;
+    if (i == p + 1) row_next[j] = v;
+    if (j == p + 1) col_next[i] = v;
+}
+
+// x_i = mask_i * sum_j inv_ij mask_j b_j in FP64: one warp per row, b staged in shared memory
+__global__ void __launch_bounds__(256) k_cd_apply(const double* __restrict__ inv, const float* __restrict__ b,
+                                                  const float* __restrict__ mask, float* __restrict__ x, int n) {
+    extern __shared__ double bs[];
+    for (int t = threadIdx.x; t < n; t += blockDim.x) bs[t] = mask[t] != 0.f ? (double)b[t] : 0.0;
+    __syncthreads();
+    const int row = blockIdx.x * 8 + (threadIdx.x >> 5);
+    const int lane = threadIdx.x & 31;
+    if (row >= n) return;
+    const double* r = inv + (long long)row * n;
+    double s = 0.0;
+    for (int j = lane; j < n; j += 32) s = fma(__ldg(r + j), bs[j], s);
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
+    if (lane == 0) x[row] = mask[row] != 0.f ? (float)s : 0.f;
+}
+
 int level_ok(const Lvl& g) {
     if (g.nx < 2 || g.ny < 2 || g.nz < 2) return FC_ERR_ARG;
     if ((long long)g.nx * g.ny * g.nz >= (1LL << 31)) return FC_ERR_ARG;
@@ -857,6 +939,53 @@ int fc_mg_inv_diag(const float* diagL, const float* mask, float* inv_diagM, floa
     if (!diagL || !mask || !inv_diagM || n < 0) return FC_ERR_ARG;
     if (n == 0) return FC_OK;
     k_inv_diag<<<grid_for(n), BLOCK, 0, (cudaStream_t)stream>>>(diagL, mask, inv_diagM, dt, omega, n);
+    return launch_status();
+}
+
+// FP64 exact solve of the coarsest level: the dense inverse (n*n doubles) plus two
+// pivot row/column buffer pairs (4 n doubles) in one caller allocation.
+long long fc_mg_coarse_dense_bytes(int nx, int ny, int nz) {
+    const long long n = (long long)nx * ny * nz;
+    if (nx < 1 || ny < 1 || nz < 1 || n > CD_MAX_CELLS) return -1;
+    return (n * n + 4 * n) * (long long)sizeof(double);
+}
+
+int fc_mg_coarse_dense_build(const float* aE, const float* aW, const float* aN, const float* aS, const float* aU,
+                             const float* aD, const float* diagL, const float* mask, float dt, int nx, int ny, int nz,
+                             int ax, int out_idx, double* inv, long long inv_bytes, void* stream) {
+    Lvl g{nx, ny, nz, ax, out_idx};
+    if (level_ok(g) || !aE || !aW || !aN || !aS || !aU || !aD || !mask || !inv) return FC_ERR_ARG;
+    (void)diagL;   // the flux-form diagonal is the sum of the couplings
+    const long long need = fc_mg_coarse_dense_bytes(nx, ny, nz);
+    if (need < 0) return FC_ERR_TOO_LARGE;
+    if (inv_bytes < need || (reinterpret_cast<uintptr_t>(inv) & 7)) return FC_ERR_ARG;
+    const int n = nx * ny * nz;
+    cudaStream_t st = (cudaStream_t)stream;
+    if (cudaMemsetAsync(inv, 0, sizeof(double) * (size_t)n * n, st) != cudaSuccess) return FC_ERR_LAUNCH;
+    Coef a{aE, aW, aN, aS, aU, aD, diagL};
+    k_cd_assemble<<<grid_for(n), BLOCK, 0, st>>>(a, mask, (double)dt, g, inv, n);
+    int rc = launch_status();
+    if (rc) return rc;
+    double* buf = inv + (size_t)n * n;       // row0, col0, row1, col1
+    k_cd_seed<<<grid_for(n), BLOCK, 0, st>>>(inv, n, buf, buf + n);
+    rc = launch_status();
+    if (rc) return rc;
+    const dim3 grid((unsigned)((n + CD_TX - 1) / CD_TX), (unsigned)((n + CD_TY - 1) / CD_TY));
+    for (int p = 0; p < n; ++p) {
+        double* cur = buf + (size_t)(p & 1) * 2 * n;
+        double* nxt = buf + (size_t)((p + 1) & 1) * 2 * n;
+        k_cd_pivot<<<grid, dim3(CD_TX, CD_TY), 0, st>>>(inv, n, p, cur, cur + n, nxt, nxt + n);
+        rc = launch_status();
+        if (rc) return rc;
+    }
+    return FC_OK;
+}
+
+int fc_mg_coarse_dense_apply(const double* inv, const float* b, const float* mask, float* x, int n, void* stream) {
+    if (!inv || !b || !mask || !x || n < 1) return FC_ERR_ARG;
+    if (n > CD_MAX_CELLS) return FC_ERR_TOO_LARGE;
+    k_cd_apply<<<(unsigned)((n + 7) / 8), 256, sizeof(double) * (size_t)n, (cudaStream_t)stream>>>(inv, b, mask, x,
+                                                                                                  n);
     return launch_status();
 }
 

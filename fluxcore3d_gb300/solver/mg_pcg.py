@@ -254,6 +254,12 @@ def _vcycle_pc(mg_solver) -> Callable[[Tensor, Tensor], None]:
     return apply
 
 
+def _coarse_key(mg):
+    """What a captured V-cycle bakes in about the coarsest-level solve (the FP64 inverse's buffer)."""
+    inv = getattr(mg, "_coarse_inv", None)
+    return (getattr(mg, "coarse_solve", "jacobi"), inv.data_ptr() if inv is not None else 0)
+
+
 class _GraphVcyclePC:
     """The V-cycle preconditioner r64 -> z64 replayed from one CUDA graph per (r64, z64) buffer
     pair (two conversions and the ~40 launches of a 5-level V-cycle become one launch).  The
@@ -268,7 +274,7 @@ class _GraphVcyclePC:
     def _version(self):
         mg = self.mg
         return (id(mg._levels), mg._dt_cache, tuple(lv["x"].data_ptr() for lv in mg._levels), mg.n_pre, mg.n_post,
-                mg.n_coarse)
+                mg.n_coarse, _coarse_key(mg))
 
     def __call__(self, r64: Tensor, z64: Tensor) -> None:
         ver = self._version()
@@ -370,7 +376,7 @@ def _bicg_solve(mg, V: _Vec, b: Tensor, x: Tensor, bnorm: float, tol: float, max
         W["host"][slot:slot + 1].copy_(sc[7:8], non_blocking=True)
 
     gkey = (id(mg._levels), dt, tuple(lv["x"].data_ptr() for lv in mg._levels), mask.data_ptr(), mg.n_pre,
-            mg.n_post, mg.n_coarse)
+            mg.n_post, mg.n_coarse, _coarse_key(mg))
     graphs = W["graphs"].get(gkey)
     if graphs is None:
         W["graphs"].clear()

@@ -15,8 +15,13 @@ prolongation fused with the correction and mask, zero-guess first sweep).
 The residual norm of `solve` is accumulated in FP64.  The per-level neighbour
 buffers of the reference's torch fallback are not allocated.
 
-Extra constructor option: max_levels (None = coarsen until the smallest
-half-extent is <= min_coarse_cells, as the reference does).
+Extra constructor options: max_levels (None = coarsen until the smallest
+half-extent is <= min_coarse_cells, as the reference does) and coarse_solve:
+"jacobi" (default, the reference's n_coarse damped-Jacobi sweeps in FP32) or
+"fp64" (the coarsest level solved exactly in FP64: its operator is assembled
+and inverted on the device whenever the hierarchy or dt changes, and every
+V-cycle applies the inverse as an FP64 matrix-vector product; levels of at
+most 4096 cells).
 """
 from __future__ import annotations
 
@@ -38,7 +43,7 @@ except ImportError:  # pragma: no cover
 class NLevelGeometricMGSolver:
     def __init__(self, device, dtype, flow_axis: int, flow_sign: int, thermal_dt_scale: float,
                  omega: float = 0.8, n_pre: int = 2, n_post: int = 2, n_coarse: int = 20,
-                 min_coarse_cells: int = 4, max_levels: Optional[int] = None):
+                 min_coarse_cells: int = 4, max_levels: Optional[int] = None, coarse_solve: str = "jacobi"):
         self.device = torch.device(device)
         self.dtype = dtype
         self.ax = int(flow_axis)
@@ -50,6 +55,10 @@ class NLevelGeometricMGSolver:
         self.n_coarse = int(n_coarse)
         self.min_coarse_cells = int(min_coarse_cells)
         self.max_levels = max_levels
+        if coarse_solve not in ("jacobi", "fp64"):
+            raise ValueError("coarse_solve must be 'jacobi' or 'fp64'")
+        self.coarse_solve = coarse_solve
+        self._coarse_inv = None
         self._ready = False
         self._dt_cache: Optional[float] = None
         self._shape_cache: Optional[tuple] = None
@@ -179,7 +188,22 @@ class NLevelGeometricMGSolver:
         for lv in self._levels:
             _lib.call("fc_mg_inv_diag", ptr(lv["diagL"]), ptr(lv["mask_f"]), ptr(lv["inv_diagM"]), float(dt),
                       self.omega, lv["mask_f"].numel(), st)
+        if self.coarse_solve == "fp64" and self._nlevels > 1:
+            self._build_coarse_inverse(float(dt))
         self._ready = True
+
+    def _build_coarse_inverse(self, dt: float) -> None:
+        """FP64 inverse of the coarsest level's A = I + dt L (Dirichlet rows identity)."""
+        lv = self._levels[-1]
+        nx, ny, nz = lv["shape"]
+        need = int(_lib.call("fc_mg_coarse_dense_bytes", nx, ny, nz))
+        if need < 0:
+            raise ValueError(f"coarse_solve='fp64': the coarsest level {lv['shape']} has more than 4096 cells; "
+                             "raise max_levels or use coarse_solve='jacobi'")
+        if self._coarse_inv is None or self._coarse_inv.numel() * 8 < need:
+            self._coarse_inv = torch.empty((need + 7) // 8, dtype=torch.float64, device=self.device)
+        _lib.call("fc_mg_coarse_dense_build", *self._cptrs(lv), ptr(lv["mask_f"]), float(dt), nx, ny, nz, self.ax,
+                  lv["out_idx"], ptr(self._coarse_inv), self._coarse_inv.numel() * 8, stream_ptr())
 
     # ---------------------------------------------------------------- V-cycle
     def _smooth_n(self, level: int, n_sweeps: int, from_zero: bool = False) -> None:
@@ -219,7 +243,11 @@ class NLevelGeometricMGSolver:
     def _vcycle(self, level: int, zero_guess: bool = False) -> None:
         lv = self._levels[level]
         if level == self._nlevels - 1:
-            self._smooth_n(level, self.n_coarse, from_zero=zero_guess)
+            if self.coarse_solve == "fp64" and level > 0:
+                _lib.call("fc_mg_coarse_dense_apply", ptr(self._coarse_inv), ptr(lv["b_buf"]), ptr(lv["mask_f"]),
+                          ptr(lv["x"]), lv["mask_f"].numel(), stream_ptr())
+            else:
+                self._smooth_n(level, self.n_coarse, from_zero=zero_guess)
             return
         self._smooth_n(level, self.n_pre, from_zero=zero_guess)
         nx, ny, nz = lv["shape"]

@@ -284,6 +284,19 @@ int fc_mg_build_coeffs(const float* k, const float* rho_cp, const float* u, cons
                        float* aS, float* aU, float* aD, float* diagL, void* stream);
 /* replaces _restrict_2x (solver/nlevel_mg_cuda.py:511-519); as_mask thresholds the mean at 0.999 (:255) */
 int fc_mg_restrict_mean(const float* src, int nx, int ny, int nz, float* dst, int as_mask, void* stream);
+/* FP64 exact solve of the coarsest multigrid level (no counterpart in the reference, which
+ * gives the coarsest level n_coarse damped-Jacobi sweeps in FP32, solver/nlevel_mg_cuda.py:271-307).
+ * build: A = I + dt L of the level (7-point couplings, operator ghosting, flux-form diagonal
+ * 1 + dt sum_n a_n, identity rows where mask == 0; diagL is not read) assembled in FP64 and
+ * inverted in place by Gauss-Jordan elimination (A is strictly diagonally dominant by rows: no
+ * pivoting), into `inv` of fc_mg_coarse_dense_bytes() bytes (the n x n inverse followed by 4 n
+ * work doubles); levels of at most 4096 cells (-1 / status 4 beyond).
+ * apply: x = mask * inv (mask * b), accumulated in FP64, one warp per row. */
+long long fc_mg_coarse_dense_bytes(int nx, int ny, int nz);
+int fc_mg_coarse_dense_build(const float* aE, const float* aW, const float* aN, const float* aS, const float* aU,
+                             const float* aD, const float* diagL, const float* mask, float dt, int nx, int ny, int nz,
+                             int ax, int out_idx, double* inv, long long inv_bytes, void* stream);
+int fc_mg_coarse_dense_apply(const double* inv, const float* b, const float* mask, float* x, int n, void* stream);
 /* replaces _update_inv_diag  (solver/nlevel_mg_cuda.py:262-267) */
 int fc_mg_inv_diag(const float* diagL, const float* mask, float* inv_diagM, float dt, float omega, long long n,
                    void* stream);

@@ -95,9 +95,10 @@ class OracleMG:
     """NLevelGeometricMGSolver (nlevel_mg_cuda.py:38-307) on numpy arrays."""
 
     def __init__(self, k, rcp, u, v, w, mask, ax, sign, s, omega=0.8, n_pre=2, n_post=2, n_coarse=20,
-                 min_coarse_cells=4, max_levels=None, real=np.float64, flux=False):
+                 min_coarse_cells=4, max_levels=None, real=np.float64, flux=False, coarse_solve="jacobi"):
         self.dt_ = real
         self.flux = flux
+        self.coarse_solve = coarse_solve
         self.ax, self.sign, self.s, self.omega = ax, sign, s, omega
         self.n_pre, self.n_post, self.n_coarse = n_pre, n_post, n_coarse
         self.levels = []
@@ -154,10 +155,37 @@ class OracleMG:
         for _ in range(n):
             lv["x"] = lv["x"] + lv["inv"] * (lv["b"] - self.mop(lv, lv["x"]))
 
+    def coarse_matrix(self, lv):
+        """A = I + dt L of a level as a dense FP64 matrix, column j = the operator applied (in FP64) to
+        the unit vector e_j, so the operator's ghosting is whatever L does."""
+        n = int(np.prod(lv["shape"]))
+        a64 = {kk: np.asarray(vv, np.float64) for kk, vv in lv["a"].items()}
+        lv64 = dict(lv, a=a64, diag=np.asarray(lv["diag"], np.float64))
+        A = np.empty((n, n))
+        e = np.zeros(n)
+        for j in range(n):
+            e[j] = 1.0
+            x = e.reshape(lv["shape"])
+            A[:, j] = (x + float(self.dt) * self.L(lv64, x)).reshape(-1)
+            e[j] = 0.0
+        return A
+
+    def coarse_exact(self, lv):
+        """The 'fp64' coarse solve: A x = b exactly in FP64 on the cells with mask 1, x = 0 elsewhere."""
+        m = np.asarray(lv["mask"]).reshape(-1) != 0
+        A = self.coarse_matrix(lv)
+        b = np.asarray(lv["b"], np.float64).reshape(-1)
+        x = np.zeros(b.size)
+        x[m] = np.linalg.solve(A[np.ix_(m, m)], b[m])
+        return x.reshape(lv["shape"]).astype(self.dt_)
+
     def vcycle(self, level=0):
         lv = self.levels[level]
         if level == len(self.levels) - 1:
-            self.smooth(lv, self.n_coarse)
+            if self.coarse_solve == "fp64" and level > 0:
+                lv["x"] = self.coarse_exact(lv)
+            else:
+                self.smooth(lv, self.n_coarse)
             return
         self.smooth(lv, self.n_pre)
         r = (lv["b"] - self.mop(lv, lv["x"])) * lv["mask"]

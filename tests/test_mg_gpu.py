@@ -93,6 +93,40 @@ def test_vcycle_solve_matches_oracle(cuda, shape):
     assert info["it"] == ir["it"] == 8
 
 
+@pytest.mark.parametrize("ax,sign", [(0, 1), (2, -1)])
+def test_coarse_fp64_solve_is_exact(cuda, ax, sign):
+    """coarse_solve='fp64': the coarsest level's FP64 inverse applied to a right-hand side equals the
+    exact FP64 solution of A x = b on the cells with mask 1 (numpy dense solve of the oracle's
+    flux-form operator), within the FP32 rounding of the output."""
+    prob = problem((32, 24, 20), ax, sign, seed=3)
+    mg, ref = both(prob, ax, sign, coarse_solve="fp64")
+    lv, lr = mg._levels[-1], ref.levels[-1]
+    assert lv["mask_f"].numel() == 8 * 6 * 5
+    rng = np.random.default_rng(4)
+    b = rng.random(lv["shape"]).astype(np.float32)
+    lv["b_buf"].copy_(torch.tensor(b, device="cuda"))
+    lr["b"] = b.astype(np.float64)
+    mg._vcycle(len(mg._levels) - 1, zero_guess=True)
+    xr = ref.coarse_exact(lr)
+    got = lv["x"].cpu().numpy()
+    assert rel(got, xr) < 1e-6
+    assert np.all(got[lr["mask"] == 0] == 0)
+
+
+def test_vcycle_fp64_coarse_matches_oracle_and_converges_no_slower(cuda):
+    """Six V-cycles with the exact FP64 coarse solve match the oracle's, and reach a residual no
+    larger than the reference's 20 FP32 Jacobi sweeps on the coarsest level."""
+    prob = problem((40, 24, 20), seed=5)
+    mg, ref = both(prob, coarse_solve="fp64")
+    b = prob[-1]
+    x, info = mg.solve(torch.tensor(b, device="cuda"), None, max_cycles=6, tol=0.0)
+    xr, ir = ref.solve(b, None, max_cycles=6, tol=0.0)
+    assert rel(x.cpu().numpy(), xr) < 1e-5
+    mj, _ = both(prob)
+    _, ij = mj.solve(torch.tensor(b, device="cuda"), None, max_cycles=6, tol=0.0)
+    assert info["res_rel"] <= ij["res_rel"] * (1 + 1e-4)
+
+
 @pytest.mark.parametrize("shape,from_zero", [((24, 16, 16), False), ((24, 16, 16), True), ((12, 8, 8), True),
                                               ((10, 6, 4), False)])
 def test_small_level_smoother_equals_sweep_sequence(cuda, shape, from_zero):
