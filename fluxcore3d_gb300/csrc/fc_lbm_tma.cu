@@ -10,14 +10,17 @@
 // tile one thread issues 19 tensor copies (cp.async.bulk.tensor): population
 // q's box starts at plane i - c_x(q), row j0 - c_y(q), so the box already holds
 // exactly what the tile pulls along x and y and the k shift becomes an index
-// offset inside a whole row.  One more tensor copy brings the tile's flag
+// offset inside a whole row.  A row longer than a box may be (256 elements) is
+// seen through the tensor map as `nseg` segments of nz / nseg elements (a 5-D
+// view: segment element, segment, row, plane, population), so one copy still
+// brings whole rows.  One more tensor copy brings the tile's flag
 // bytes, and two plain bulk copies bring the tile's slice of this step's
 // gathered interpolated bounce-back values (storage form) and of the static
 // table saying which staged element each of them replaces.  Link cells and
 // links are stored in cell order, so a tile's links are one contiguous range;
 // fc_lbm_tile_links precomputes it with the first link of every chunk.
-// Persistent CTAs of 4 warps (3 per SM) rotate over 2 shared-memory stages
-// tracked by mbarriers; warps run through the tiles independently and the last
+// Persistent CTAs of 4 warps (3 per SM) rotate over 3 shared-memory stages
+// (2 for FP32 storage, whose stages are twice as large) tracked by mbarriers; warps run through the tiles independently and the last
 // warp done with a stage refills it, so no CTA-wide barrier sits in the loop.
 //
 // Cells.  Before a warp reads its chunk it writes the chunk's link values into
@@ -48,7 +51,7 @@ namespace {
 constexpr int TS_THREADS = 128;
 constexpr int TS_MIN_BLOCKS = 3;           // 3 CTAs of 4 warps per SM (<= 170 registers a thread)
 constexpr int TS_WARPS = TS_THREADS / 32;
-constexpr int TS_RANGE_CACHE = 64;         // per-CTA cache of the records of its first tiles
+constexpr int TS_RANGE_CACHE = 16;         // per-CTA cache of the records of its first tiles
 constexpr int TS_HEAD_BYTES = 128 + TS_RANGE_CACHE * 32;   // mbarriers, stage counters, record cache
 constexpr unsigned TS_SPIN = 1u << 24;     // bound on mbarrier polls (seconds of waiting at most)
 constexpr int TS_TILE_CELLS = 512;         // most cells of a tile (tj = 512 / nz rows)
@@ -69,7 +72,9 @@ struct Layout {
     static constexpr uint32_t POS = INFO + 128u;
     static constexpr uint32_t VAL = POS + TS_LK_CAP * 2u;
     static constexpr uint32_t STAGE = VAL + TS_LK_CAP * SB;
-    static constexpr int STAGES = 2;
+    // 16-bit storage: 3 stages of 24.6 KB, so that 3 CTAs (9 stages, 6 of them
+    // loading while 3 are consumed) fit in the SM's 228 KB; FP32: 2 of 46 KB
+    static constexpr int STAGES = KIND == ST_F32 ? 2 : 3;
     static_assert(STAGE % 128 == 0, "stage size keeps every stage 128-byte aligned");
 };
 
@@ -125,21 +130,21 @@ __device__ __forceinline__ bool bar_wait(uint32_t bar, unsigned parity, unsigned
     return false;
 }
 
+__device__ __forceinline__ void tma_load_5d(uint32_t dst, const CUtensorMap* tm, int c0, int c1, int c2, int c3,
+                                            int c4, uint32_t bar) {
+    asm volatile(
+        "cp.async.bulk.tensor.5d.shared::cluster.global.mbarrier::complete_tx::bytes"
+        " [%0], [%1, {%2, %3, %4, %5, %6}], [%7];" ::"r"(dst),
+        "l"(reinterpret_cast<uint64_t>(tm)), "r"(c0), "r"(c1), "r"(c2), "r"(c3), "r"(c4), "r"(bar)
+        : "memory");
+}
+
 __device__ __forceinline__ void tma_load_4d(uint32_t dst, const CUtensorMap* tm, int c0, int c1, int c2, int c3,
                                             uint32_t bar) {
     asm volatile(
         "cp.async.bulk.tensor.4d.shared::cluster.global.mbarrier::complete_tx::bytes"
         " [%0], [%1, {%2, %3, %4, %5}], [%6];" ::"r"(dst),
         "l"(reinterpret_cast<uint64_t>(tm)), "r"(c0), "r"(c1), "r"(c2), "r"(c3), "r"(bar)
-        : "memory");
-}
-
-__device__ __forceinline__ void tma_load_3d(uint32_t dst, const CUtensorMap* tm, int c0, int c1, int c2,
-                                            uint32_t bar) {
-    asm volatile(
-        "cp.async.bulk.tensor.3d.shared::cluster.global.mbarrier::complete_tx::bytes"
-        " [%0], [%1, {%2, %3, %4}], [%5];" ::"r"(dst),
-        "l"(reinterpret_cast<uint64_t>(tm)), "r"(c0), "r"(c1), "r"(c2), "r"(bar)
         : "memory");
 }
 
@@ -180,9 +185,10 @@ __device__ __forceinline__ TileInfo tile_info(const FusedArgs& a, const TileRec&
     return ti;
 }
 
-// One tile into one stage: 19 population boxes (x coordinate 0, so every copy
-// starts on a 16-byte boundary; rows or planes outside the grid read as zero
-// and are never used), the tile's flag bytes, and its link slots and values.
+// One tile into one stage: 19 population boxes (segment-element and segment
+// coordinates 0, so every copy starts on a 16-byte boundary; rows or planes
+// outside the grid read as zero and are never used), the tile's flag bytes,
+// and its link slots and values.
 // The staged link range ends at most 7 entries past the tile's last link;
 // link_pos and link_val hold n_links + 8 entries, so the copies stay inside.
 template <int KIND>
@@ -199,8 +205,8 @@ __device__ __forceinline__ void issue_tile(const FusedArgs& a, const CUtensorMap
     bar_expect_tx(bar, tx);   // release: the info record is visible to whoever sees the phase complete
     const uint32_t st = su32(stage);
 #pragma unroll
-    for (int q = 0; q < 19; ++q) tma_load_4d(st + q * LY::Q, tp, 0, j0 - cy(q), i - cx(q), q, bar);
-    tma_load_3d(st + LY::FLAG, tf, 0, j0, i, bar);
+    for (int q = 0; q < 19; ++q) tma_load_5d(st + q * LY::Q, tp, 0, 0, j0 - cy(q), i - cx(q), q, bar);
+    tma_load_4d(st + LY::FLAG, tf, 0, 0, j0, i, bar);
     if (n_st > 0) {
         bulk_load(st + LY::POS, a.link_pos + ti.lb0, (uint32_t)n_st * 2u, bar);
         bulk_load(st + LY::VAL, reinterpret_cast<const unsigned char*>(a.link_val) + (size_t)ti.lb0 * LY::SB,
@@ -617,9 +623,14 @@ TileGeo tile_geo(const Geo& g, int storage) {
 template <int KIND>
 size_t smem_bytes() { return TS_HEAD_BYTES + (size_t)Layout<KIND>::STAGES * Layout<KIND>::STAGE; }
 
+// a row is read as nseg box segments of at most 256 elements each
+int row_segments(int nz) { return (nz + 255) / 256; }
+
 bool grid_fits(const Geo& g) {
-    // whole-row boxes (at most 256 elements), 16-byte flag rows, int cell indices
-    return g.nz % 16 == 0 && g.nz <= 256 && g.nz >= 16 && g.N < (1LL << 31);
+    // whole rows within a tile (at most 512 cells), segments of a multiple of
+    // 16 elements (16-byte flag segments), int cell indices
+    if (g.nz < 16 || g.nz > TS_TILE_CELLS || g.N >= (1LL << 31)) return false;
+    return g.nz % (16 * row_segments(g.nz)) == 0;
 }
 
 template <int S, int M>
@@ -719,25 +730,28 @@ int launch_fused_tma(const FusedArgs& a, int storage, int collision, cudaStream_
     const TileGeo tg = tile_geo(g, storage);
     const int sb = storage_bytes(storage);
     CUtensorMap tp, tf;
+    const int nseg = row_segments(g.nz), seg = g.nz / nseg;
     {
-        const cuuint64_t dims[4] = {(cuuint64_t)g.nz, (cuuint64_t)g.ny, (cuuint64_t)g.nx, 19};
-        const cuuint64_t strides[3] = {(cuuint64_t)g.nz * sb, (cuuint64_t)g.nynz * sb, (cuuint64_t)g.N * sb};
-        const cuuint32_t box[4] = {(cuuint32_t)g.nz, (cuuint32_t)tg.tj, 1, 1};
-        const cuuint32_t es[4] = {1, 1, 1, 1};
+        // (segment element, segment, row, plane, population): a row is nseg contiguous segments
+        const cuuint64_t dims[5] = {(cuuint64_t)seg, (cuuint64_t)nseg, (cuuint64_t)g.ny, (cuuint64_t)g.nx, 19};
+        const cuuint64_t strides[4] = {(cuuint64_t)seg * sb, (cuuint64_t)g.nz * sb, (cuuint64_t)g.nynz * sb,
+                                       (cuuint64_t)g.N * sb};
+        const cuuint32_t box[5] = {(cuuint32_t)seg, (cuuint32_t)nseg, (cuuint32_t)tg.tj, 1, 1};
+        const cuuint32_t es[5] = {1, 1, 1, 1, 1};
         const CUtensorMapDataType dt = storage == ST_F32    ? CU_TENSOR_MAP_DATA_TYPE_FLOAT32
                                        : storage == ST_F16S ? CU_TENSOR_MAP_DATA_TYPE_FLOAT16
                                                             : CU_TENSOR_MAP_DATA_TYPE_BFLOAT16;
-        if (encode_tiled()(&tp, dt, 4, const_cast<void*>(a.pin[0]), dims, strides, box, es,
+        if (encode_tiled()(&tp, dt, 5, const_cast<void*>(a.pin[0]), dims, strides, box, es,
                            CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE,
                            CU_TENSOR_MAP_L2_PROMOTION_L2_256B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) != CUDA_SUCCESS)
             return FC_ERR_UNSUPPORTED;
     }
     {
-        const cuuint64_t dims[3] = {(cuuint64_t)g.nz, (cuuint64_t)g.ny, (cuuint64_t)g.nx};
-        const cuuint64_t strides[2] = {(cuuint64_t)g.nz, (cuuint64_t)g.nynz};
-        const cuuint32_t box[3] = {(cuuint32_t)g.nz, (cuuint32_t)tg.tj, 1};
-        const cuuint32_t es[3] = {1, 1, 1};
-        if (encode_tiled()(&tf, CU_TENSOR_MAP_DATA_TYPE_UINT8, 3, const_cast<uint8_t*>(a.flags), dims, strides, box,
+        const cuuint64_t dims[4] = {(cuuint64_t)seg, (cuuint64_t)nseg, (cuuint64_t)g.ny, (cuuint64_t)g.nx};
+        const cuuint64_t strides[3] = {(cuuint64_t)seg, (cuuint64_t)g.nz, (cuuint64_t)g.nynz};
+        const cuuint32_t box[4] = {(cuuint32_t)seg, (cuuint32_t)nseg, (cuuint32_t)tg.tj, 1};
+        const cuuint32_t es[4] = {1, 1, 1, 1};
+        if (encode_tiled()(&tf, CU_TENSOR_MAP_DATA_TYPE_UINT8, 4, const_cast<uint8_t*>(a.flags), dims, strides, box,
                            es, CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE,
                            CU_TENSOR_MAP_L2_PROMOTION_L2_256B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) != CUDA_SUCCESS)
             return FC_ERR_UNSUPPORTED;
