@@ -497,7 +497,8 @@ def main():
         sampler = ClockSampler(local) if storage == storages[0] else None
         if sampler:
             sampler.start()
-        total_ms, blocks = time_steps(sim, args.steps, dev, ws=ws, restarter=restarter)
+        total_ms, blocks = time_steps(sim, args.steps, dev, min_seconds=0.0 if args.profile else 1.0, ws=ws,
+                                      restarter=restarter)
         if ws > 1:
             tt = torch.tensor([total_ms], device=dev)
             torch.distributed.all_reduce(tt, op=torch.distributed.ReduceOp.MAX)
