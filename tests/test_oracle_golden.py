@@ -213,3 +213,66 @@ def test_oracle_flux_form_equals_reference_form_in_fp64():
         Tl = T[tuple(slice(0, n) for n in lr["shape"])]
         a, b = ref.L(lr, Tl), flx.L(lf, Tl)
         assert float(np.abs(a - b).max()) <= 1e-12 * float(np.abs(a).max() + 1.0)
+
+
+# ---- the reference's own plane and Smagorinsky kernels, run on the host (ref_lbm.npz) ----------
+
+def _plane_cells(shape, axis, idx):
+    i, j, k = np.meshgrid(*(np.arange(n) for n in shape), indexing="ij")
+    flat = (i * shape[1] + j) * shape[2] + k
+    return np.take(flat, idx, axis=axis).reshape(-1)
+
+
+ZH_CASES = ("inlet_x_low", "outlet_x_high", "inlet_y_high", "outlet_y_low", "outlet_z_low", "inlet_z_low")
+CV_CASES = ("x_high", "z_low", "x_high_two_blocks")
+
+
+def _close(got, want, tol):
+    return float(np.abs(got.astype(np.float64) - want).max()) <= tol * float(np.abs(want).max())
+
+
+@pytest.mark.parametrize("case", ZH_CASES)
+def test_oracle_zou_he_matches_reference_kernel(case):
+    """or_zou_he (oracle/lbm_oracle.c) against lbm_zou_he_bc_kernel (solver/lbm_kernels.cu:791-969)
+    run on the host: boundary plane within FP32 rounding, solid and backflow nodes included."""
+    d = load("ref_lbm.npz")
+    a = d[f"zh_{case}_args"]
+    shape = tuple(int(x) for x in a[:3])
+    axis, plane, inter, bct = (int(x) for x in a[3:7])
+    uin, rout, sign = float(a[7]), float(a[8]), int(a[9])
+    orc = olbm.OracleLBM(*shape, d[f"zh_{case}_in"], d["solid_%dx%dx%d" % shape])
+    f = orc.f.copy()
+    orc.L.or_zou_he(olbm._p(f), olbm._p(orc.solid), *shape, axis, plane, inter, bct, float(np.float32(uin)),
+                    float(np.float32(rout)), sign)
+    assert _close(f[:, _plane_cells(shape, axis, plane)], d[f"zh_{case}_plane"], 2e-6)
+
+
+@pytest.mark.parametrize("case", CV_CASES)
+def test_oracle_convective_matches_reference_kernel(case):
+    """or_convective against lbm_convective_bc_reduce_kernel + lbm_convective_mass_correct_kernel
+    (solver/lbm_kernels.cu:1170-1344) run on the host; the reference sums rho in FP32 with one
+    atomicAdd per block, the oracle in FP64, so the plane agrees to FP32 summation order."""
+    d = load("ref_lbm.npz")
+    a = d[f"cv_{case}_args"]
+    shape = tuple(int(x) for x in a[:3])
+    axis, o, inter, ucax = (int(x) for x in a[3:7])
+    rout = float(a[7])
+    orc = olbm.OracleLBM(*shape, d[f"cv_{case}_in"], d["solid_%dx%dx%d" % shape])
+    f = orc.f.copy()
+    orc.L.or_convective(olbm._p(f), olbm._p(orc.solid), *shape, axis, o, inter, ucax, float(np.float32(rout)))
+    assert _close(f[:, _plane_cells(shape, axis, o)], d[f"cv_{case}_plane"], 2e-6)
+
+
+def test_oracle_mrt_smagorinsky_matches_reference_kernel():
+    """Mode 3 of or_macro_collide against lbm_macro_collide_mrt_smag_kernel (solver/lbm_kernels.cu:
+    1018-1117) run on the host: post-collision populations and macros within FP32 rounding."""
+    d = load("ref_lbm.npz")
+    shape = tuple(int(x) for x in d["smag_shape"])
+    cs2, om0 = (float(x) for x in d["smag_params"])
+    orc = olbm.OracleLBM(*shape, d["smag_f"], d["solid_%dx%dx%d" % shape], collision="mrt_smag", omega=om0,
+                         S=d["smag_S"], Cs_dx2=float(np.float32(cs2)))
+    orc.params[4] = float(np.float32(om0))
+    orc.collide()
+    assert _close(orc.fp, d["smag_out_fp"], 2e-6)
+    for got, want in zip((orc.rho, orc.u, orc.v, orc.w), d["smag_out_macro"]):
+        assert _close(got, want, 2e-6)
