@@ -226,9 +226,15 @@ def chebyshev_smooth(mg_solver, level: int, n_steps: int = 2, lam_min_ratio: flo
     _lib.call("fc_vec_convert", 2, ptr(x), ptr(x_new), n, ptr(mask), 1.0, st)
 
 
-def patch_mg_pcg(mg_solver, pe_threshold: float = 1.5):
+def patch_mg_pcg(mg_solver, pe_threshold: float = 1.5, method: Optional[str] = None):
     """Replace mg_solver.solve with PCG / BiCGSTAB chosen by the reference's Peclet heuristic
-    (reference mg_pcg.py:250-275: pe = 0.1 max(diagL))."""
+    (reference mg_pcg.py:250-275: pe = 0.1 max(diagL)).
+
+    method="bicgstab_f64" (no counterpart in the reference) instead solves with the device-resident
+    FP64 BiCGSTAB around the FP32 V-cycle (bicgstab_mg_f64), certified on the FP64 true residual:
+    the FP32 stationary V-cycle iteration stalls where its FP32 residual A x loses the digits of
+    b (A = I + dt L with a large dt); FP64 residuals remove that floor.  The result is returned in
+    the right-hand side's precision."""
 
     def _solve_pcg(self, b, x0=None, max_cycles=15, tol=1e-3):
         pe = float(torch.amax(self._levels[0]["diagL"]).item()) * 0.1
@@ -236,8 +242,17 @@ def patch_mg_pcg(mg_solver, pe_threshold: float = 1.5):
             return bicgstab_mg(self, b, x0, tol=tol, max_it=max_cycles)
         return pcg_mg(self, b, x0, tol=tol, max_it=max_cycles)
 
-    mg_solver.solve = types.MethodType(_solve_pcg, mg_solver)
-    print(f"[MG-PCG] Patched mg_solver.solve -> PCG/BiCGSTAB (pe_threshold={pe_threshold})")
+    def _solve_f64(self, b, x0=None, max_cycles=15, tol=1e-3):
+        x, info = bicgstab_mg_f64(self, b, x0, tol=tol, max_it=max_cycles)
+        out = {"converged": info["converged"], "diverged": not math.isfinite(info["res_rel"]), "it": info["it"],
+               "res_rel": info["res_rel"], "res0_rel": info.get("res0_rel", float("nan"))}
+        return x.to(b.dtype), out
+
+    if method not in (None, "bicgstab_f64"):
+        raise ValueError("method must be None (the reference's PCG/BiCGSTAB choice) or 'bicgstab_f64'")
+    mg_solver.solve = types.MethodType(_solve_f64 if method == "bicgstab_f64" else _solve_pcg, mg_solver)
+    what = "FP64 BiCGSTAB (FP32 V-cycle)" if method else f"PCG/BiCGSTAB (pe_threshold={pe_threshold})"
+    print(f"[MG-PCG] Patched mg_solver.solve -> {what}")
 
 
 # ---------------------------------------------------------------------------

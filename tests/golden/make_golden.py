@@ -22,6 +22,10 @@ use them).  Fixtures written (all small .npz files):
                       on three closed meshes built by fluxcore3d_gb300.pre_post.stl
                       (box, icosphere, finned heat sink): triangles, grid and the
                       packed voxel grids; written alone by `--only voxels`
+  thermal_steady.npz  steady temperature of a heated channel from the reference's fused
+                      pseudo-time thermal step with its FP64 torch multigrid and its thermal
+                      kernels built for the host (oracle/build_ref.py); written alone by
+                      `--only thermal_steady`
   mg_solve.npz        NLevelGeometricMGSolver (torch fallback, float64): coefficients,
                       L_apply_fine, V-cycle solve, pcg_mg and bicgstab_mg results
 """
@@ -277,11 +281,115 @@ def tracer(ref_root: str):
     print("tracer.npz written to", HERE)
 
 
+def thermal_steady(ref_root: str):
+    """Steady temperature of a heated channel from the reference's own fused pseudo-time thermal step
+    (solver/thermal_cuda_ext.py:55-201, _temperature_step_mg_fused, the path the reference takes on a
+    GPU) with its multigrid in FP64 (solver/nlevel_mg_cuda.py, torch path) and its
+    thermal_reconstruct / physics_check kernels (solver/thermal_kernels.cu) compiled for the host in
+    FP64 by oracle/build_ref.py, iterated with the ramped pseudo-time step of
+    solve_thermal_steady_only (LBM_CHT.py:2388-2569: dt from 5, times 1.5 per step, at most 200)
+    until a step changes T by less than 2e-13; T after the first three steps is kept too.
+    Channel 24x16x16, solid cube 6^3 centred at (8, 8, 8), k_s/k_f = 100, velocity 0.02 along +x in
+    the fluid (zero in the solid and in the wall planes z = 0, 15), heat source 0.05 in the cube,
+    inlet x = 0 at Tin = 25."""
+    import ctypes as C
+    os.environ["PYTHONDONTWRITEBYTECODE"] = "1"
+    sys.dont_write_bytecode = True
+    _stub_modules()
+    sys.path.insert(0, ref_root)
+    sys.path.insert(0, os.path.dirname(os.path.dirname(HERE)))
+    import torch
+    import LBM_CHT as R
+    from oracle import build_ref
+    from solver import thermal_cuda_ext as TCE
+
+    lib = C.CDLL(build_ref.build_thermal(ref_root))
+    vp, i32, f64 = C.c_void_p, C.c_int, C.c_double
+    lib.ref_thermal_reconstruct64.argtypes = [vp, vp, vp, i32, i32, i32, i32, i32]
+    lib.ref_physics_check64.argtypes = [vp, f64, f64, i32]
+    lib.ref_physics_check64.restype = i32
+
+    class _HostThermal:
+        """THERMAL_CUDA's calls of the fused step, on the host kernels (FP64 tensors)."""
+
+        @staticmethod
+        def thermal_reconstruct(T0, theta, nx, ny, nz, ax, out_idx):
+            a, b = T0.contiguous(), theta.contiguous()
+            out = torch.empty_like(a)
+            lib.ref_thermal_reconstruct64(a.data_ptr(), b.data_ptr(), out.data_ptr(), nx, ny, nz, ax, out_idx)
+            return out
+
+        @staticmethod
+        def physics_check(T, T_min, T_max):
+            t = T.contiguous()
+            return torch.tensor([lib.ref_physics_check64(t.data_ptr(), T_min, T_max, t.numel())], dtype=torch.int32)
+
+        @staticmethod
+        def convergence_metrics(T_new, T_old, solid_u8):
+            dT = (T_new - T_old).abs()
+            s = solid_u8.bool()
+            return [dT[s].max().reshape(1), dT[~s].max().reshape(1)]
+
+    TCE.THERMAL_CUDA, TCE.THERMAL_CUDA_AVAILABLE = _HostThermal(), True
+
+    nx, ny, nz = 24, 16, 16
+    solid = torch.zeros((nx, ny, nz), dtype=torch.bool)
+    solid[5:11, 5:11, 5:11] = True
+    solid_flow = solid.clone()
+    solid_flow[:, :, 0] = True
+    solid_flow[:, :, -1] = True
+    nu = 0.05 * 6 / 50.0
+    alpha_f = nu / 0.71
+    k = torch.full((nx, ny, nz), alpha_f, dtype=torch.float32)
+    k[solid] = alpha_f * 100.0
+    u = torch.full((nx, ny, nz), 0.02, dtype=torch.float32)
+    u[solid_flow] = 0.0
+    src = torch.zeros((nx, ny, nz), dtype=torch.float32)
+    src[solid] = 0.05
+
+    class _Host:
+        pass
+
+    h = _Host()
+    h.cfg = types.SimpleNamespace(flow_dir="+X", temp_bc="fixed", mg_omega=0.6, mg_pre_smooth=2, mg_post_smooth=2,
+                                  mg_coarse_iters=20, domain_walls=["+Z", "-Z"], domain_outlets=[],
+                                  transverse_walls=False, flow_bc="inlet_outlet")
+    h.nx, h.ny, h.nz = nx, ny, nz
+    h.fluid = types.SimpleNamespace(tin_C=25.0)
+    h.thermal_dt_scale = 1.0
+    h.ax, h.sign = 0, +1
+    h.solid = solid
+    d = torch.float64
+    h.T = torch.full((nx, ny, nz), 25.0, dtype=d)
+    h.k, h.rho_cp = k.to(d), torch.ones((nx, ny, nz), dtype=d)
+    h.u, h.v, h.wv = u.to(d), torch.zeros((nx, ny, nz), dtype=d), torch.zeros((nx, ny, nz), dtype=d)
+    h._compute_surface_flux_sources = lambda: torch.zeros((nx, ny, nz), dtype=d)
+    h._compute_heat_source = lambda: src.to(d)
+    for name in ("_build_update_mask_thermal", "_build_T_dirichlet_field"):
+        setattr(h, name, types.MethodType(getattr(R.LBMCHT3D_Torch, name), h))
+    step = types.MethodType(TCE._temperature_step_mg_fused, h)
+    dt, T3, dT, it = 5.0, None, float("inf"), 0
+    for it in range(400):
+        Tprev = h.T.clone()
+        step(dt=dt, tol=1e-13, max_cycles=200)
+        dT = float((h.T - Tprev).abs().max())
+        dt = min(200.0, 1.5 * dt)
+        if it == 2:
+            T3 = h.T.clone()
+        if dT < 2e-13:
+            break
+    print(f"thermal_steady: {it + 1} pseudo-time steps, last dT {dT:.3e}")
+    np.savez_compressed(os.path.join(HERE, "thermal_steady.npz"), T=h.T.numpy(), T3=T3.numpy(), k=k.numpy(),
+                        u=u.numpy(), src=src.numpy(), solid=solid.numpy(), solid_flow=solid_flow.numpy(),
+                        steps=np.array(it + 1))
+    print("thermal_steady.npz written to", HERE)
+
+
 if __name__ == "__main__":
     import argparse
     ap = argparse.ArgumentParser(description=__doc__.splitlines()[0])
     ap.add_argument("reference_root", help="root of the fluxcore3D source tree (read only)")
-    ap.add_argument("--only", choices=("main", "ibb_pitch", "voxels", "tracer"), default=None)
+    ap.add_argument("--only", choices=("main", "ibb_pitch", "voxels", "tracer", "thermal_steady"), default=None)
     a = ap.parse_args()
     root = a.reference_root
     if a.only == "main":
@@ -292,8 +400,11 @@ if __name__ == "__main__":
         voxels(root)
     elif a.only == "tracer":
         tracer(root)
+    elif a.only == "thermal_steady":
+        thermal_steady(root)
     else:
         main(root)
         ibb_pitch(root)
         voxels(root)
         tracer(root)
+        thermal_steady(root)

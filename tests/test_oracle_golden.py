@@ -276,3 +276,47 @@ def test_oracle_mrt_smagorinsky_matches_reference_kernel():
     assert _close(orc.fp, d["smag_out_fp"], 2e-6)
     for got, want in zip((orc.rho, orc.u, orc.v, orc.w), d["smag_out_macro"]):
         assert _close(got, want, 2e-6)
+
+
+def test_oracle_thermal_step_matches_reference_fused_step():
+    """The oracle's restatement of the pseudo-time thermal step (oracle/mg.py thermal_step) against the
+    reference's own fused step (solver/thermal_cuda_ext.py:55-201 with its FP64 torch multigrid and its
+    thermal kernels built for the host; thermal_steady.npz): three ramped steps, FP64."""
+    d = load("thermal_steady.npz")
+    k, u, src = d["k"], d["u"], d["src"].astype(np.float64)
+    shape = k.shape
+    mask = np.ones(shape, bool)
+    mask[0] = False
+    z = np.zeros(shape, np.float32)
+    ref = omg.OracleMG(k, np.ones(shape, np.float32), u, z, z, mask, 0, 1, 1.0, omega=0.6, real=np.float64)
+    T = np.full(shape, 25.0)
+    T0 = np.full(shape, 25.0)
+    dt = 5.0
+    for _ in range(3):
+        ref.set_dt(dt)
+        T, _ = omg.thermal_step(ref, T, T0, src, mask, dt, 1e-13, 200, 0, shape[0] - 1)
+        dt *= 1.5
+    assert float(np.abs(T - d["T3"]).max()) < 1e-12
+
+
+def test_oracle_fp32_flux_form_steady_temperature_within_1e6():
+    """The steady temperature of the thermal step iterated in FP32 with the flux form (60 ramped steps,
+    FP32 V-cycles) is within 1e-6 relative L2 of the reference's own FP64 steady state
+    (thermal_steady.npz).  With the reference's diag form in FP32 it is ~4e-6 away: its rounded diagL
+    acts as a source proportional to T ~ 25."""
+    d = load("thermal_steady.npz")
+    k, u, src = d["k"], d["u"], d["src"]
+    shape = k.shape
+    mask = np.ones(shape, np.float32)
+    mask[0] = 0
+    z = np.zeros(shape, np.float32)
+    mg = omg.OracleMG(k, np.ones(shape, np.float32), u, z, z, mask, 0, 1, 1.0, omega=0.6, real=np.float32, flux=True)
+    T = np.full(shape, 25.0, np.float32)
+    T0 = np.full(shape, 25.0, np.float32)
+    dt = 5.0
+    for _ in range(60):
+        mg.set_dt(dt)
+        T, _ = omg.thermal_step(mg, T, T0, src, mask, dt, 1e-7, 100, 0, shape[0] - 1)
+        dt = min(200.0, 1.5 * dt)
+    Tr = d["T"]
+    assert np.linalg.norm(T.astype(np.float64) - Tr) / np.linalg.norm(Tr) < 1e-6
