@@ -85,6 +85,13 @@ struct TileGeo {
     int kchunks;         // 64-cell chunks per row (a lane collides cells k, k+1)
     int kc_inv;          // ceil(65536 / kchunks): chunk -> row by multiply and shift
     uint32_t base_tx;    // bytes of the population and flag boxes of one tile
+    int wrap_y;          // 1: the periodic y wrap of the first and last tile of a plane is staged
+};
+
+// Tensor maps of the population buffer: boxes of tj rows, of tj - 1 rows and of
+// one row (the last two stage the periodic y wrap of a plane's edge tiles).
+struct PopMaps {
+    CUtensorMap full, shrt, row;
 };
 
 // Per-tile record (global, from fc_lbm_tile_links): link-cell range, link
@@ -101,6 +108,7 @@ struct TileInfo {
     int nl;      // links of the tile
     int staged;  // 1: link slots and values staged, 0: the tile has no links, -1: not staged
     unsigned short pre[TS_PRE];
+    int wrap;    // 1: the rows this tile pulls across the periodic y boundary are staged
 };
 
 __device__ __forceinline__ uint32_t su32(const void* p) {
@@ -186,26 +194,47 @@ __device__ __forceinline__ TileInfo tile_info(const FusedArgs& a, const TileRec&
 }
 
 // One tile into one stage: 19 population boxes (segment-element and segment
-// coordinates 0, so every copy starts on a 16-byte boundary; rows or planes
-// outside the grid read as zero and are never used), the tile's flag bytes,
-// and its link slots and values.
+// coordinates 0, so every copy starts on a 16-byte boundary), the tile's flag
+// bytes, and its link slots and values.  A periodic x axis wraps the box's
+// plane coordinate.  With tg.wrap_y, the boxes of the first and last tile of a
+// plane that would reach row -1 or row ny are split into a box of tj - 1 rows
+// and a one-row box of the wrapped row, landing in disjoint slab rows; other
+// rows or planes outside the grid read as zero and are never used (those cells
+// take the direct-load path).
 // The staged link range ends at most 7 entries past the tile's last link;
 // link_pos and link_val hold n_links + 8 entries, so the copies stay inside.
 template <int KIND>
-__device__ __forceinline__ void issue_tile(const FusedArgs& a, const CUtensorMap* tp, const CUtensorMap* tf,
+__device__ __forceinline__ void issue_tile(const FusedArgs& a, const PopMaps* tp, const CUtensorMap* tf,
                                            const TileGeo& tg, int tile, const TileRec& rec, unsigned char* stage,
                                            uint32_t bar) {
     using LY = Layout<KIND>;
     const int i = tile / tg.tiles_j;
     const int j0 = (tile - i * tg.tiles_j) * tg.tj;
     int n_st;
-    const TileInfo ti = tile_info(a, rec, n_st);
+    TileInfo ti = tile_info(a, rec, n_st);
+    const int ny = a.g.ny, nx = a.g.nx;
+    const bool first = tg.wrap_y && j0 == 0, last = tg.wrap_y && j0 + tg.tj == ny;
+    ti.wrap = first | last;
     *reinterpret_cast<TileInfo*>(stage + LY::INFO) = ti;
     const uint32_t tx = tg.base_tx + (uint32_t)n_st * (2u + LY::SB);
     bar_expect_tx(bar, tx);   // release: the info record is visible to whoever sees the phase complete
     const uint32_t st = su32(stage);
+    const uint32_t row_bytes = (uint32_t)a.g.nz * LY::SB;
 #pragma unroll
-    for (int q = 0; q < 19; ++q) tma_load_5d(st + q * LY::Q, tp, 0, 0, j0 - cy(q), i - cx(q), q, bar);
+    for (int q = 0; q < 19; ++q) {
+        int ii = i - cx(q);
+        if (a.g.px) ii = ii < 0 ? nx - 1 : (ii >= nx ? 0 : ii);
+        const uint32_t dst = st + q * LY::Q;
+        if (cy(q) == 1 && first) {            // slab row 0 <- row ny - 1, rows 1.. <- rows 0..tj-2
+            if (tg.tj > 1) tma_load_5d(dst + row_bytes, &tp->shrt, 0, 0, 0, ii, q, bar);
+            tma_load_5d(dst, &tp->row, 0, 0, ny - 1, ii, q, bar);
+        } else if (cy(q) == -1 && last) {     // rows 0..tj-2 <- rows j0+1.., slab row tj-1 <- row 0
+            if (tg.tj > 1) tma_load_5d(dst, &tp->shrt, 0, 0, j0 + 1, ii, q, bar);
+            tma_load_5d(dst + (uint32_t)(tg.tj - 1) * row_bytes, &tp->row, 0, 0, 0, ii, q, bar);
+        } else {
+            tma_load_5d(dst, &tp->full, 0, 0, j0 - cy(q), ii, q, bar);
+        }
+    }
     tma_load_4d(st + LY::FLAG, tf, 0, 0, j0, i, bar);
     if (n_st > 0) {
         bulk_load(st + LY::POS, a.link_pos + ti.lb0, (uint32_t)n_st * 2u, bar);
@@ -310,7 +339,7 @@ __device__ __forceinline__ TileRec tile_rec(const FusedArgs& a, const TileRec* c
 
 template <int KIND, int MODE>
 __global__ void __launch_bounds__(TS_THREADS, TS_MIN_BLOCKS)
-    k_fused_tma(const __grid_constant__ FusedArgs a, const __grid_constant__ CUtensorMap tm_pop,
+    k_fused_tma(const __grid_constant__ FusedArgs a, const __grid_constant__ PopMaps tm_pop,
                 const __grid_constant__ CUtensorMap tm_flag, const TileGeo tg) {
     using LY = Layout<KIND>;
     constexpr int S = LY::STAGES;
@@ -371,7 +400,8 @@ __global__ void __launch_bounds__(TS_THREADS, TS_MIN_BLOCKS)
         const uint8_t* sflag = sb + LY::FLAG;
         const TileInfo& ti = *reinterpret_cast<const TileInfo*>(sb + LY::INFO);
         const int staged = ti.staged;
-        const bool plane_edge = (i == 0) | (i == nx - 1);
+        const bool plane_edge = ((i == 0) | (i == nx - 1)) & (a.g.px == 0);   // a periodic x wraps in the box
+        const bool wrapped = ti.wrap != 0;
         for (int ch = warp; ch < nch; ch += TS_WARPS) {
             const int r = (ch * tg.kc_inv) >> 16;
             const int k = (ch - r * tg.kchunks) * 64 + 2 * lane;   // cells k, k+1 (nz is even)
@@ -413,7 +443,7 @@ __global__ void __launch_bounds__(TS_THREADS, TS_MIN_BLOCKS)
                 }
             }
             const bool live_a = !(fa & CF_SOLID), live_b = !(fb & CF_SOLID);
-            const bool edge_row = plane_edge | (j == 0) | (j == ny - 1);
+            const bool edge_row = plane_edge | (((j == 0) | (j == ny - 1)) & !wrapped);
             const bool ea = live_a & (edge_row | ((a.g.pz == 0) & (k == 0)));
             const bool eb = live_b & (edge_row | ((a.g.pz == 0) & (k + 1 == nz - 1)));
             const bool link_a = live_a && (fa & CF_LINK), link_b = live_b && (fb & CF_LINK);
@@ -617,6 +647,9 @@ TileGeo tile_geo(const Geo& g, int storage) {
     tg.kc_inv = (65536 + tg.kchunks - 1) / tg.kchunks;
     const int cells = tg.tj * g.nz;
     tg.base_tx = (uint32_t)(19 * cells * sb + cells);
+    // the periodic y wrap is staged when every plane has a separate first and last tile of full
+    // rows and a row boundary inside a slab keeps the 128-byte alignment of tensor-copy targets
+    tg.wrap_y = (g.py != 0) && tg.tiles_j >= 2 && g.ny % tg.tj == 0 && (tg.tj == 1 || (g.nz * sb) % 128 == 0);
     return tg;
 }
 
@@ -634,7 +667,7 @@ bool grid_fits(const Geo& g) {
 }
 
 template <int S, int M>
-int launch_typed(const FusedArgs& a, const CUtensorMap& tp, const CUtensorMap& tf, const TileGeo& tg,
+int launch_typed(const FusedArgs& a, const PopMaps& tp, const CUtensorMap& tf, const TileGeo& tg,
                  cudaStream_t st) {
     auto kern = k_fused_tma<S, M>;
     static int configured = 0;
@@ -729,19 +762,23 @@ int launch_fused_tma(const FusedArgs& a, int storage, int collision, cudaStream_
     const Geo& g = a.g;
     const TileGeo tg = tile_geo(g, storage);
     const int sb = storage_bytes(storage);
-    CUtensorMap tp, tf;
+    PopMaps tp;
+    CUtensorMap tf;
     const int nseg = row_segments(g.nz), seg = g.nz / nseg;
-    {
+    for (int m = 0; m < 3; ++m) {
+        // box heights: tj rows, tj - 1 rows (at least 1), one row
+        const int rows = m == 0 ? tg.tj : (m == 1 ? (tg.tj > 1 ? tg.tj - 1 : 1) : 1);
+        CUtensorMap* map = m == 0 ? &tp.full : (m == 1 ? &tp.shrt : &tp.row);
         // (segment element, segment, row, plane, population): a row is nseg contiguous segments
         const cuuint64_t dims[5] = {(cuuint64_t)seg, (cuuint64_t)nseg, (cuuint64_t)g.ny, (cuuint64_t)g.nx, 19};
         const cuuint64_t strides[4] = {(cuuint64_t)seg * sb, (cuuint64_t)g.nz * sb, (cuuint64_t)g.nynz * sb,
                                        (cuuint64_t)g.N * sb};
-        const cuuint32_t box[5] = {(cuuint32_t)seg, (cuuint32_t)nseg, (cuuint32_t)tg.tj, 1, 1};
+        const cuuint32_t box[5] = {(cuuint32_t)seg, (cuuint32_t)nseg, (cuuint32_t)rows, 1, 1};
         const cuuint32_t es[5] = {1, 1, 1, 1, 1};
         const CUtensorMapDataType dt = storage == ST_F32    ? CU_TENSOR_MAP_DATA_TYPE_FLOAT32
                                        : storage == ST_F16S ? CU_TENSOR_MAP_DATA_TYPE_FLOAT16
                                                             : CU_TENSOR_MAP_DATA_TYPE_BFLOAT16;
-        if (encode_tiled()(&tp, dt, 5, const_cast<void*>(a.pin[0]), dims, strides, box, es,
+        if (encode_tiled()(map, dt, 5, const_cast<void*>(a.pin[0]), dims, strides, box, es,
                            CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE,
                            CU_TENSOR_MAP_L2_PROMOTION_L2_256B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) != CUDA_SUCCESS)
             return FC_ERR_UNSUPPORTED;

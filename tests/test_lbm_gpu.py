@@ -152,6 +152,39 @@ def test_staged_pass_long_rows_bit_identical_to_direct(cuda, storage, nz):
         assert np.array_equal(a, b)
 
 
+@pytest.mark.parametrize("flow_dir,shape,storage", [("+X", (40, 16, 64), "fp16"), ("+Z", (20, 16, 64), "bf16"),
+                                                    ("+Y", (24, 20, 32), "fp32"), ("-X", (30, 8, 64), "fp16"),
+                                                    ("+X", (40, 16, 32), "bf16")])
+def test_staged_pass_wrapped_edges_bit_identical_to_direct(cuda, flow_dir, shape, storage):
+    """Periodic axes staged by the tensor copies themselves: the plane coordinate of a periodic x
+    wraps, and with full tiles whose rows keep 128-byte alignment the first and last tile of each
+    plane load the periodic y wrap as a box of tj - 1 rows plus a one-row box (no direct loads for
+    those rows); other shapes keep the direct-load path for the edge rows.  Bit for bit the same as
+    the direct pass, links included."""
+    from fluxcore3d_gb300 import geometry as geo
+    from fluxcore3d_gb300.case import CaseConfig, LatticeCase, stamp_walls
+    nx, ny, nz = shape
+    out = {}
+    for staging in ("tma", "direct"):
+        cfg = CaseConfig(nx=nx, ny=ny, nz=nz, flow_dir=flow_dir, collision="mrt", lbm_storage=storage,
+                         domain_walls=[], outlet_bc_mode="pressure")
+        solid = geo.cube_mask(shape, (nx // 2, ny // 2, nz // 2), (6, 6, 6), device=cuda)
+        sim = LatticeCase(cfg, 0.05, 0.05 * 6 / 50, solid, stamp_walls(cfg, solid), geo.ibb_from_voxels(solid),
+                          device=cuda, seed=0)
+        sim.cfg.lbm_staging = staging
+        LBMCUDAUpgrade.patch(sim)
+        if staging == "tma":
+            assert sim._fc.tile_links is not None
+        for _ in range(40):
+            sim.step(do_thermal=False)
+        torch.cuda.synchronize()
+        assert sim._fc.check_device_error() == 0
+        P = sim._fc.P[sim._fc.cur]
+        out[staging] = (P.view(torch.uint8).cpu().numpy(), sim.rho.cpu().numpy(), sim.u.cpu().numpy())
+    for a, b in zip(out["tma"], out["direct"]):
+        assert np.array_equal(a, b)
+
+
 def test_fused_planes_and_concurrent_gather_bit_identical(cuda, monkeypatch):
     """Fused Zou/He + collision of the inlet/outlet planes (one launch) and the next step's link
     gather on a second stream give the same bits as the reference-order plane sequence with the
