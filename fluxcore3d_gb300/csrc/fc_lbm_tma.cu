@@ -19,8 +19,8 @@
 // table saying which staged element each of them replaces.  Link cells and
 // links are stored in cell order, so a tile's links are one contiguous range;
 // fc_lbm_tile_links precomputes it with the first link of every chunk.
-// Persistent CTAs of 4 warps (3 per SM) rotate over 3 shared-memory stages
-// (2 for FP32 storage, whose stages are twice as large) tracked by mbarriers; warps run through the tiles independently and the last
+// Persistent CTAs of 4 warps (3 per SM) rotate over 2 shared-memory stages
+// tracked by mbarriers; warps run through the tiles independently and the last
 // warp done with a stage refills it, so no CTA-wide barrier sits in the loop.
 //
 // Cells.  Before a warp reads its chunk it writes the chunk's link values into
@@ -51,7 +51,7 @@ namespace {
 constexpr int TS_THREADS = 128;
 constexpr int TS_MIN_BLOCKS = 3;           // 3 CTAs of 4 warps per SM (<= 170 registers a thread)
 constexpr int TS_WARPS = TS_THREADS / 32;
-constexpr int TS_RANGE_CACHE = 16;         // per-CTA cache of the records of its first tiles
+constexpr int TS_RANGE_CACHE = 64;         // per-CTA cache of the records of its first tiles
 constexpr int TS_HEAD_BYTES = 128 + TS_RANGE_CACHE * 32;   // mbarriers, stage counters, record cache
 constexpr unsigned TS_SPIN = 1u << 24;     // bound on mbarrier polls (seconds of waiting at most)
 constexpr int TS_TILE_CELLS = 512;         // most cells of a tile (tj = 512 / nz rows)
@@ -72,9 +72,8 @@ struct Layout {
     static constexpr uint32_t POS = INFO + 128u;
     static constexpr uint32_t VAL = POS + TS_LK_CAP * 2u;
     static constexpr uint32_t STAGE = VAL + TS_LK_CAP * SB;
-    // 16-bit storage: 3 stages of 24.6 KB, so that 3 CTAs (9 stages, 6 of them
-    // loading while 3 are consumed) fit in the SM's 228 KB; FP32: 2 of 46 KB
-    static constexpr int STAGES = KIND == ST_F32 ? 2 : 3;
+    // 2 stages (a third one, which fits 3 CTAs at 16-bit storage, measured no faster)
+    static constexpr int STAGES = 2;
     static_assert(STAGE % 128 == 0, "stage size keeps every stage 128-byte aligned");
 };
 
@@ -375,17 +374,24 @@ __global__ void __launch_bounds__(TS_THREADS, TS_MIN_BLOCKS)
         }
     }
 
-    // Warps run through the tiles independently: each waits for a stage's copies
-    // itself, and the last warp to finish with a stage refills it.
+    // Warps take the chunks of the CTA's tiles in order, chunk w, w + 4, w + 8, ... of
+    // the concatenated sequence, so the work stays balanced whatever the chunk
+    // count of a tile.  Each warp waits for a stage's copies itself, and the
+    // warp that completes a tile's last chunk refills its stage.
     const int nx = a.g.nx, ny = a.g.ny, nz = a.g.nz;
     const int nch = tg.tj * tg.kchunks;
-    int it = 0;
-    for (int t = blockIdx.x; t < tg.n_tiles; t += G, ++it) {
+    const int my_tiles = (int)blockIdx.x < tg.n_tiles ? (tg.n_tiles - 1 - (int)blockIdx.x) / G + 1 : 0;
+    const int touching = nch < TS_WARPS ? nch : TS_WARPS;   // warps that take chunks of any one tile
+    int ready_it = -1;                                       // last tile whose stage this warp saw complete
+    // (it, ch): tile iteration and chunk of this warp's current chunk, advanced by TS_WARPS chunks
+    int it = warp / nch, ch = warp - (warp / nch) * nch;
+    while (it < my_tiles) {
+        const int t = blockIdx.x + it * G;
         const int s = it % S;
         const int i = t / tg.tiles_j;
         const int j0 = (t - i * tg.tiles_j) * tg.tj;
         const float sg_plane = (a.sponge && a.sponge_axis == 0) ? __ldg(a.sponge + i) : 0.f;
-        if (!__all_sync(0xffffffffu, bar_wait(bar0 + 8 * s, (unsigned)(it / S) & 1u))) {
+        if (it != ready_it && !__all_sync(0xffffffffu, bar_wait(bar0 + 8 * s, (unsigned)(it / S) & 1u))) {
             if (lane == 0) {
                 if (a.dev_err) atomicOr(a.dev_err, DEV_ERR_TIMEOUT);
                 // let copies still in flight land before the CTA can retire (bounded)
@@ -395,6 +401,7 @@ __global__ void __launch_bounds__(TS_THREADS, TS_MIN_BLOCKS)
             }
             return;
         }
+        ready_it = it;
 
         const unsigned char* sb = stages + s * LY::STAGE;
         const uint8_t* sflag = sb + LY::FLAG;
@@ -402,7 +409,7 @@ __global__ void __launch_bounds__(TS_THREADS, TS_MIN_BLOCKS)
         const int staged = ti.staged;
         const bool plane_edge = ((i == 0) | (i == nx - 1)) & (a.g.px == 0);   // a periodic x wraps in the box
         const bool wrapped = ti.wrap != 0;
-        for (int ch = warp; ch < nch; ch += TS_WARPS) {
+        do {   // one chunk; `continue` leaves it
             const int r = (ch * tg.kc_inv) >> 16;
             const int k = (ch - r * tg.kchunks) * 64 + 2 * lane;   // cells k, k+1 (nz is even)
             const int j = j0 + r;
@@ -494,13 +501,13 @@ __global__ void __launch_bounds__(TS_THREADS, TS_MIN_BLOCKS)
                 *reinterpret_cast<float2*>(a.v + idx) = make_float2(live_a ? m.uy.v.x : 0.f, live_b ? m.uy.v.y : 0.f);
                 *reinterpret_cast<float2*>(a.w + idx) = make_float2(live_a ? m.uz.v.x : 0.f, live_b ? m.uz.v.y : 0.f);
             }
-        }
-        // this warp is done with the stage; the last one refills it with the tile
-        // S iterations ahead
+        } while (false);
+        // after its last chunk of a tile the warp is done with the stage; the last
+        // warp done refills it with the tile S iterations ahead
         __syncwarp();
-        if (lane == 0) {
+        if (lane == 0 && ch + TS_WARPS >= nch) {
             __threadfence_block();
-            if (atomicAdd(done + s, 1) == TS_WARPS - 1) {
+            if (atomicAdd(done + s, 1) == touching - 1) {
                 done[s] = 0;
                 const int tn = t + S * G;
                 if (tn < tg.n_tiles) {
@@ -509,6 +516,11 @@ __global__ void __launch_bounds__(TS_THREADS, TS_MIN_BLOCKS)
                                      stages + s * LY::STAGE, bar0 + 8 * s);
                 }
             }
+        }
+        ch += TS_WARPS;
+        while (ch >= nch) {
+            ch -= nch;
+            ++it;
         }
     }
 }

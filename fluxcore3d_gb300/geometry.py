@@ -145,11 +145,17 @@ def ibb_from_voxels(solid: torch.Tensor, pitch: float = 1.0, origin=(0.0, 0.0, 0
     return ibb_from_phi(solid, signed_distance(solid, pitch), pitch, origin)
 
 
-def ibb_from_level_set(solid: torch.Tensor, levelset, n_bisect: int = 40) -> IBBData:
+def ibb_from_level_set(solid: torch.Tensor, levelset, n_bisect: int = 40, method: str = "bisect") -> IBBData:
     """Links of `solid` with q from an analytic level set G(x) (negative = fluid, positive =
-    solid, G(cell centre) > 0 <=> solid), refined by FP64 bisection to the exact crossing."""
+    solid, G(cell centre) > 0 <=> solid): method "bisect" refines the crossing by FP64 bisection,
+    "linear" interpolates G linearly between the link's two nodes."""
     ff, di, do, fff, fv = build_links(solid)
-    q = level_set_fractions(levelset, ff, di, solid.shape, n_bisect)
+    if method == "linear":
+        q = linear_level_set_fractions(levelset, ff, di, solid.shape)
+    elif method == "bisect":
+        q = level_set_fractions(levelset, ff, di, solid.shape, n_bisect)
+    else:
+        raise ValueError("method must be 'bisect' or 'linear'")
     ge, w1, w2 = bfl_weights_from_q(q)
     return IBBData(int(ff.numel()), ff, di, do, ge, w1, w2, fff, fv)
 
@@ -174,6 +180,20 @@ def level_set_fractions(levelset, fluid_flat: torch.Tensor, dir_i: torch.Tensor,
         hi = torch.where(inside, mid, hi)
         lo = torch.where(inside, lo, mid)
     return hi.clamp(1e-6, 1.0).to(torch.float32)
+
+
+def linear_level_set_fractions(levelset, fluid_flat: torch.Tensor, dir_i: torch.Tensor, shape) -> torch.Tensor:
+    """FP32 link fractions q = G_f / (G_f - G_s) in (0, 1]: the zero of G interpolated linearly
+    between the fluid node x_f (G_f <= 0) and the solid node x_f + c_q (G_s > 0), in FP64."""
+    dev = fluid_flat.device
+    nx, ny, nz = shape
+    ff = fluid_flat
+    x0 = torch.stack([(ff // (ny * nz)).double(), ((ff // nz) % ny).double(), (ff % nz).double()], dim=1)
+    c = torch.tensor(C_NP, device=dev, dtype=torch.float64)[dir_i]
+    gf = levelset(x0)
+    gs = levelset(x0 + c)
+    q = gf / (gf - gs)
+    return q.clamp(1e-6, 1.0).to(torch.float32)
 
 
 # --------------------------------------------------------------------------
