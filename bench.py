@@ -460,6 +460,9 @@ def main():
     ap.add_argument("--no-gyroid", action="store_true",
                     help="skip the gyroid TPMS block (TRT lattice, FP64 error, 5-level thermal solve)")
     ap.add_argument("--gyroid-steps", type=int, default=6000, help="steps of the gyroid accuracy runs")
+    ap.add_argument("--no-coupled", action="store_true",
+                    help="skip the coupled flow + heat run on the 768x384x384 hybrid heat sink")
+    ap.add_argument("--coupled-steps", type=int, default=200, help="timed lattice steps of the coupled run")
     ap.add_argument("--no-learned", action="store_true", help="skip the learned-preconditioner training / A-B")
     ap.add_argument("--accuracy-steps", type=int, default=10000)
     ap.add_argument("--storages", default="fp16,fp32", help="population storages to time (first = headline)")
@@ -470,7 +473,7 @@ def main():
     if args.profile:
         args.storages = args.storages.split(",")[0]
         args.no_e2e = args.no_cpu = args.no_thermal = args.no_geometry = args.no_io = args.no_accuracy = True
-        args.no_gyroid = True
+        args.no_gyroid = args.no_coupled = True
         args.no_learned = True
     if args.impl == "reference":
         run_reference(args)
@@ -611,6 +614,9 @@ def main():
         line["learned"]["conv_fwd"] = conv_bench.run(dev, bf16_peak_tflops=peaks()[1])
     if rank == 0 and not args.no_accuracy:
         line["accuracy"] = accuracy_run(args, dev)
+    if rank == 0 and not args.no_coupled:
+        from fluxcore3d_gb300 import coupled_bench
+        line["coupled"] = coupled_bench.run(dev, steps=args.coupled_steps)
     if rank == 0 and not args.no_gyroid:
         from fluxcore3d_gb300 import gyroid_bench
         line["gyroid"] = gyroid_bench.run(dev, accuracy_steps=args.gyroid_steps, peak_gbs=peaks()[0])

@@ -16,7 +16,7 @@ import time
 import torch
 
 
-def thermal_system(sim, u, v, w, dt=1000.0, flux=5e-3):
+def thermal_system(sim, u, v, w, dt=1000.0, flux=5e-3, max_levels=None, coarse_solve="jacobi"):
     """A = I + dt L for the velocity (u, v, w) on sim's geometry (zero velocity in flow-solid
     cells), inlet plane (x = 0) Dirichlet, a uniform heat flux into the bottom layer of the solid;
     returns (mg, b)."""
@@ -29,7 +29,8 @@ def thermal_system(sim, u, v, w, dt=1000.0, flux=5e-3):
     src[:, :, 0] = flux                               # heat flux into the bottom layer of the base plate
     src[~sim.solid] = 0.0
     b = (mask.float() * dt * src).contiguous()
-    mg = NLevelGeometricMGSolver(dev, torch.float32, 0, +1, 1.0, omega=0.6, n_pre=2, n_post=2, n_coarse=20)
+    mg = NLevelGeometricMGSolver(dev, torch.float32, 0, +1, 1.0, omega=0.6, n_pre=2, n_post=2, n_coarse=20,
+                                 max_levels=max_levels, coarse_solve=coarse_solve)
     vel = []
     for t in (u, v, w):
         if not bool(torch.isfinite(t).all()):

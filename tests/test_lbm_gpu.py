@@ -324,3 +324,75 @@ def test_argument_errors_raise(cuda):
         LBM_CUDA.macro_collide_mrt(f, f.clone(), torch.zeros(8, device=cuda), torch.zeros(8, device=cuda),
                                    torch.zeros(8, device=cuda), torch.zeros(8, device=cuda),
                                    torch.zeros(8, dtype=torch.uint8, device=cuda), torch.zeros(5, device=cuda))
+
+
+def test_gyroid_trt_fp32_matches_oracle(cuda):
+    """Reduced gyroid (48x24x32, L = 12, linear-interpolation link fractions), TRT with magic
+    parameter 1/4 at FP32 storage: 200 steps of the fused engine against the FP32 oracle."""
+    sim = cases.gyroid(device=cuda, storage="fp32", nx=48, ny=24, nz=32, L=12.0)
+    orc = run_pair(sim, 200)
+    N = sim.nx * sim.ny * sim.nz
+    assert rel_l2(sim.f.reshape(19, N).cpu().numpy(), orc.f) < 1e-5
+
+
+def _fp64_gate(cuda, make, steps):
+    """Storage runs of the fused engine against the device FP64 run of the plain method from the
+    same initial state: velocity rel. L2 over fluid cells and the temperature of each velocity field
+    (the thermal system of the heat-sink benchmarks, solved to a 1e-10 FP64 residual) in max norm."""
+    from fluxcore3d_gb300 import thermal_bench
+    from fluxcore3d_gb300.lattice64 import Lattice64
+    from fluxcore3d_gb300.solver import mg_pcg
+    ref = make("fp32")
+    lat = Lattice64(ref)
+    lat.step(steps)
+    lat.check()
+    shape = (ref.nx, ref.ny, ref.nz)
+    fluid = ~ref.solid_flow.reshape(-1)
+    c = torch.tensor(cases.geo.C_NP, dtype=torch.float64, device=cuda)
+    vel = {"fp64": lat.velocity()}
+    for storage in ("fp16", "bf16"):
+        sim = make(storage)
+        LBMCUDAUpgrade.patch(sim)
+        for _ in range(steps):
+            sim.step(do_thermal=False)
+        sim.sync_f()
+        assert sim._fc.check_device_error() == 0
+        f = sim.f.reshape(19, -1).double()
+        vel[storage] = (c.t() @ f) / f.sum(0)
+    T = {}
+    for name, u in vel.items():
+        uu = u.to(torch.float32).reshape((3,) + shape)
+        mg, b = thermal_bench.thermal_system(ref, uu[0], uu[1], uu[2])
+        x, info = mg_pcg.bicgstab_mg_f64(mg, b, tol=1e-10, max_it=600)
+        assert info["converged"]
+        T[name] = x.double()
+    out = {}
+    for s in ("fp16", "bf16"):
+        out[s] = (float(torch.linalg.norm((vel[s] - vel["fp64"])[:, fluid]) / torch.linalg.norm(vel["fp64"][:, fluid])),
+                  float((T[s] - T["fp64"]).abs().max() / T["fp64"].abs().max()))
+    return out
+
+
+def test_pin_fin_fp16_bf16_gate_against_fp64(cuda):
+    """FP16/BF16 shifted storage on a reduced pin fin (128x64x64, 8x4 pins r = 3.5, h = 40, MRT with
+    the Smagorinsky model, Re = 200, u = 0.08) after 4000 steps against the FP64 run: FP16
+    temperature error <= 1e-3 (max norm, the brief's target) and velocity <= 3e-3 rel. L2; BF16 (8
+    significant bits against FP16's 11) is held to 1e-2 on temperature and 5e-2 on velocity."""
+    def make(storage):
+        return cases.pin_fin(device=cuda, storage=storage, collision="mrt_smag", nx=128, ny=64, nz=64, n_pins=(8, 4),
+                             height=40, base=4, sponge_length=20)
+    err = _fp64_gate(cuda, make, 4000)
+    assert err["fp16"][1] <= 1e-3 and err["fp16"][0] <= 3e-3, err
+    assert err["bf16"][1] <= 1e-2 and err["bf16"][0] <= 5e-2, err
+
+
+def test_gyroid_trt_fp16_bf16_error_against_fp64(cuda):
+    """The reduced gyroid (96x48x48, L = 24, TRT, tau = 0.545) at its steady state (4000 steps; the
+    FP64 velocity changes by < 3e-6 per 2000 steps beyond) against the FP64 run.  Measured: FP16
+    velocity 5.9e-3 rel. L2 and temperature 2.1e-3 in max norm (the FP16 rounding of f - w_q settles
+    into a fixed bias near tau = 1/2), BF16 4.1e-2 and 1.2e-2; held to 1.5x those."""
+    def make(storage):
+        return cases.gyroid(device=cuda, storage=storage, nx=96, ny=48, nz=48, L=24.0)
+    err = _fp64_gate(cuda, make, 4000)
+    assert err["fp16"][1] <= 3.2e-3 and err["fp16"][0] <= 9e-3, err
+    assert err["bf16"][1] <= 1.8e-2 and err["bf16"][0] <= 6.2e-2, err
