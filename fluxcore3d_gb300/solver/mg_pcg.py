@@ -259,14 +259,22 @@ def patch_mg_pcg(mg_solver, pe_threshold: float = 1.5, method: Optional[str] = N
 # FP64-certified solvers
 # ---------------------------------------------------------------------------
 def _vcycle_pc(mg_solver) -> Callable[[Tensor, Tensor], None]:
-    lv0 = mg_solver._levels[0]
+    """One V-cycle from zero as the map r64 -> z64.  The fine level is looked up at every call:
+    a rebuilt hierarchy (new coefficients) replaces the level buffers."""
     V = _vec(mg_solver)
 
     def apply(r64: Tensor, z64: Tensor) -> None:
+        lv0 = mg_solver._levels[0]
         V.convert(lv0["b_buf"], r64, lv0["mask_f"])          # FP64 residual -> FP32 right-hand side
         mg_solver._vcycle(0, zero_guess=True)
         V.convert(z64, lv0["x"], lv0["mask_f"])
     return apply
+
+
+def _hier_key(mg):
+    """Identity of the solver's current hierarchy for the captured graphs: a rebuild (new velocity,
+    new coefficients) gets a new generation even when the allocator hands back the same addresses."""
+    return (id(mg._levels), getattr(mg, "_generation", 0))
 
 
 def _coarse_key(mg):
@@ -288,7 +296,7 @@ class _GraphVcyclePC:
 
     def _version(self):
         mg = self.mg
-        return (id(mg._levels), mg._dt_cache, tuple(lv["x"].data_ptr() for lv in mg._levels), mg.n_pre, mg.n_post,
+        return (_hier_key(mg), mg._dt_cache, tuple(lv["x"].data_ptr() for lv in mg._levels), mg.n_pre, mg.n_post,
                 mg.n_coarse, _coarse_key(mg))
 
     def __call__(self, r64: Tensor, z64: Tensor) -> None:
@@ -390,7 +398,7 @@ def _bicg_solve(mg, V: _Vec, b: Tensor, x: Tensor, bnorm: float, tol: float, max
         _lib.call("fc_bicgstab_xr", k, ptr(xw), ptr(r), ptr(sh), ptr(t), n, ptr(sc), 1, ptr(ws), ws.numel(), st)
         W["host"][slot:slot + 1].copy_(sc[7:8], non_blocking=True)
 
-    gkey = (id(mg._levels), dt, tuple(lv["x"].data_ptr() for lv in mg._levels), mask.data_ptr(), mg.n_pre,
+    gkey = (_hier_key(mg), dt, tuple(lv["x"].data_ptr() for lv in mg._levels), mask.data_ptr(), mg.n_pre,
             mg.n_post, mg.n_coarse, _coarse_key(mg))
     graphs = W["graphs"].get(gkey)
     if graphs is None:

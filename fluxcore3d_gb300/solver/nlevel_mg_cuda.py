@@ -146,6 +146,8 @@ class NLevelGeometricMGSolver:
         return n - 1 if self.sign == +1 else 0
 
     def _build_hierarchy(self, k, rho_cp, u, v, w, mask) -> None:
+        # captured solver graphs bake the level buffers' addresses: every build is a new generation
+        self._generation = getattr(self, "_generation", 0) + 1
         self._levels = []
         dev = self.device
         st = stream_ptr()

@@ -347,3 +347,28 @@ def test_steady_temperature_matches_reference(cuda, solver):
     T = d["T"]
     assert rel(got, T) < 1e-6
     assert float(np.abs(got - T).max()) < 1e-5 * float((T - 25.0).max())
+
+
+def test_solver_graphs_follow_a_rebuilt_hierarchy(cuda):
+    """A hierarchy rebuilt with new coefficients (the reference's `_ready = False` pattern, used when
+    the velocity changes) must not replay solver graphs captured on the old one, even when the
+    allocator returns the same addresses: the FP64 BiCGSTAB on the rebuilt solver gives the result of
+    a fresh solver on the new coefficients."""
+    prob = problem((32, 16, 16), seed=7)
+    k, rcp, u, v, w, mask, b = prob
+    dev = torch.device("cuda")
+    T = lambda a: torch.tensor(a, device=dev)
+    mg = NLevelGeometricMGSolver(dev, torch.float32, 0, 1, 1.0, omega=0.6)
+    mg.build_if_needed(T(k), T(rcp), T(u), T(v), T(w), T(mask), 50.0)
+    x1, i1 = mg_pcg.bicgstab_mg_f64(mg, T(b), tol=1e-10, max_it=200)
+    assert i1["converged"]
+    u2 = (u * 3.0).astype(np.float32)
+    mg._ready = False
+    mg.build_if_needed(T(k), T(rcp), T(u2), T(v), T(w), T(mask), 50.0)
+    x2, i2 = mg_pcg.bicgstab_mg_f64(mg, T(b), tol=1e-10, max_it=200)
+    fresh = NLevelGeometricMGSolver(dev, torch.float32, 0, 1, 1.0, omega=0.6)
+    fresh.build_if_needed(T(k), T(rcp), T(u2), T(v), T(w), T(mask), 50.0)
+    x3, i3 = mg_pcg.bicgstab_mg_f64(fresh, T(b), tol=1e-10, max_it=200)
+    assert i2["converged"] and i3["converged"]
+    assert rel(x2.cpu().numpy(), x3.cpu().numpy()) < 1e-8
+    assert rel(x2.cpu().numpy(), x1.cpu().numpy()) > 1e-4
