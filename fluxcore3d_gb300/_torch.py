@@ -24,3 +24,23 @@ def require(t: torch.Tensor, name: str, dtype: torch.dtype | None = None, numel:
         raise RuntimeError(f"{name} must be {str(dtype).replace('torch.', '')}")
     if numel is not None and t.numel() != numel:
         raise RuntimeError(f"{name} must have {numel} elements")
+
+
+def capture_graph(fn):
+    """CUDA graph of fn() with Python's cyclic garbage collector paused during the capture.
+
+    Solver objects that own captured graphs sit in reference cycles, so only the cyclic
+    collector frees them; a collection triggered inside another capture would destroy their
+    graphs there, and a graph may not be reset while a stream captures (the capture is then
+    invalidated).  torch.cuda.graph collects once on entry, before the capture begins."""
+    import gc
+    g = torch.cuda.CUDAGraph()
+    was = gc.isenabled()
+    gc.disable()
+    try:
+        with torch.cuda.graph(g):
+            fn()
+    finally:
+        if was:
+            gc.enable()
+    return g

@@ -30,7 +30,7 @@ import torch
 
 from .. import _lib
 from .._lib import StepArgs
-from .._torch import ptr, stream_ptr
+from .._torch import capture_graph, ptr, stream_ptr
 from .face_roles import periodic_flags, resolve_face_roles, _face_ax_idx_fsign
 
 CF_SOLID, CF_LINK, CF_DEFER, CF_WRITE_S = 1, 2, 4, 8  # low nibble; high nibble = link count
@@ -408,9 +408,7 @@ class FusedLBM:
         key = (cur, self.sim.f.data_ptr())
         g = self._graphs.get(key)
         if g is None:
-            g = torch.cuda.CUDAGraph()
-            with torch.cuda.graph(g):
-                self._enqueue(cur, None)
+            g = capture_graph(lambda: self._enqueue(cur, None))
             self._graphs[key] = g
         return g
 

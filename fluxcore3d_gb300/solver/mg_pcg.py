@@ -25,7 +25,7 @@ from typing import Callable, Optional, Tuple
 import torch
 
 from .. import _lib
-from .._torch import ptr, stream_ptr
+from .._torch import capture_graph, ptr, stream_ptr
 
 Tensor = torch.Tensor
 
@@ -307,9 +307,7 @@ class _GraphVcyclePC:
         k = (r64.data_ptr(), z64.data_ptr())
         g = self.graphs.get(k)
         if g is None:
-            g = torch.cuda.CUDAGraph()
-            with torch.cuda.graph(g):
-                self.eager(r64, z64)
+            g = capture_graph(lambda: self.eager(r64, z64))
             self.graphs[k] = g
         g.replay()
 
@@ -405,10 +403,7 @@ def _bicg_solve(mg, V: _Vec, b: Tensor, x: Tensor, bnorm: float, tol: float, max
         W["graphs"].clear()
         graphs = []
         for slot in range(2):
-            g = torch.cuda.CUDAGraph()
-            with torch.cuda.graph(g):
-                iteration(slot)
-            graphs.append(g)
+            graphs.append(capture_graph(lambda: iteration(slot)))
         W["graphs"][gkey] = graphs
 
     def true_res() -> float:
