@@ -53,7 +53,10 @@ class _Layer:
 
 
 class UNetPreconditioner:
-    def __init__(self, device="cuda", seed: int = 0):
+    def __init__(self, device="cuda", seed: int = 0, zero_last: bool = False):
+        """zero_last: the output layer starts at zero, so the untrained network returns 0 (inside
+        LearnedCorrection the preconditioner is then exactly the V-cycle) and training grows the
+        correction from there instead of first shrinking a random output of the wrong scale."""
         self.device = torch.device(device)
         gen = torch.Generator().manual_seed(seed)
         self.layers = []
@@ -61,6 +64,8 @@ class UNetPreconditioner:
             kp = kpad_of(cin)
             fan_in = 27 * (INPUT_REAL_CHANNELS if name == "a" else cin)
             std = math.sqrt(2.0 / fan_in) if relu else math.sqrt(1.0 / fan_in)
+            if zero_last and name == SPEC[-1][0]:
+                std = 0.0
             w = torch.zeros((cout, kp), dtype=torch.float32)
             w3 = torch.randn((cout, 27, cin), generator=gen) * std
             if name == "a":
