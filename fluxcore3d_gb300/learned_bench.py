@@ -33,9 +33,12 @@ U_FLUID = 0.05
 DT = 1000.0
 
 
-def make_problem(n: int, seed: int, dev):
-    solid = random_spheres_mask(n, seed, rmin=max(2.0, 4.0 * n / 256 * 4), rmax=max(4.0, 16.0 * n / 256 * 2),
-                                device=dev)
+def make_problem(n: int, seed: int, dev, radii=None):
+    """Binary conductivity from random spheres (k_s/k_f = 200), uniform flow along +x in the fluid,
+    inlet plane Dirichlet, A = I + dt L with dt = 1000.  radii = (rmin, rmax); by default they scale
+    with n (2-4 cells at 32^3), the 256^3 held-out set uses 4-16 cells."""
+    rmin, rmax = radii if radii else (max(2.0, 4.0 * n / 256 * 4), max(4.0, 16.0 * n / 256 * 2))
+    solid = random_spheres_mask(n, seed, rmin=rmin, rmax=rmax, device=dev)
     k = torch.full((n, n, n), ALPHA_F, device=dev)
     k[solid] = ALPHA_F * K_RATIO
     rcp = torch.ones((n, n, n), device=dev)
@@ -165,6 +168,42 @@ def correction_quality(net: UNetPreconditioner, n: int, seeds, dev) -> list:
     return rows
 
 
+def eval_large(net: UNetPreconditioner, dev, n=256, seeds=(2001, 2002), tol=1e-8):
+    """Held-out 256^3 problems (spheres of radius 4-16 cells): the one-shot quality of the
+    V-cycle + network correction and the solve times of plain BiCGSTAB, plain FGMRES and FGMRES
+    with the learned correction (plain V-cycle fallback on stall), all to an FP64 residual `tol`."""
+    rows = []
+    rng = np.random.default_rng(4242)
+    for s in seeds:
+        mg, k, solid = make_problem(n, s, dev, radii=(4.0, 16.0))
+        b = random_rhs(n, rng, dev, solid)
+        e, _ = mg_pcg.bicgstab_mg_f64(mg, b, tol=1e-10, max_it=500)
+        e = e.float()
+        pc = LearnedCorrection(net, mg, k)
+        r1 = pc.residual_after_vcycle(b.contiguous())
+        v = mg._levels[0]["x"].clone()
+        y = net.forward(r1.reshape((1,) + tuple(r1.shape[-3:])), pc.k).reshape(v.shape)
+        nrm = float(torch.linalg.norm(e))
+        row = {"seed": int(s), "vcycle_rel_err": float(torch.linalg.norm(e - v)) / nrm,
+               "vcycle_plus_net_rel_err": float(torch.linalg.norm(e - v - y)) / nrm}
+        del e, v, y
+        for name, fn in (("plain_bicgstab", lambda: mg_pcg.bicgstab_mg_f64(mg, b, tol=tol, max_it=400)),
+                         ("plain_fgmres", lambda: mg_pcg.fgmres_mg_f64(mg, b, tol=tol, max_it=400, restart=30)),
+                         ("learned_fgmres", lambda: mg_pcg.fgmres_mg_f64(mg, b, tol=tol, max_it=400, restart=30,
+                                                                         precond=pc,
+                                                                         stall_fallback=mg_pcg._vcycle_pc(mg)))):
+            torch.cuda.synchronize()
+            t = time.perf_counter()
+            _, info = fn()
+            torch.cuda.synchronize()
+            row[name] = {"ms": round((time.perf_counter() - t) * 1e3, 1), "it": info["it"], "res": info["res_rel"],
+                         "fell_back": info.get("fell_back")}
+        rows.append(row)
+        del mg, pc
+        torch.cuda.empty_cache()
+    return rows
+
+
 def run(dev, n_train=32, n_eval=64, n_geom=24, per_geom=4, steps=1500, lr=5e-4, eval_seeds=(1001, 1002, 1003),
         correction: bool = True):
     """Train (output layer started at zero, Adam at lr with a cosine schedule) on MG-generated pairs,
@@ -187,5 +226,6 @@ def run(dev, n_train=32, n_eval=64, n_geom=24, per_geom=4, steps=1500, lr=5e-4, 
            "speedup_plain_bicgstab_over_learned": round(float(np.median([r["plain_bicgstab_ms"] / r["learned_ms"]
                                                                          for r in rows])), 3),
            "correction_quality": quality,
+           "held_out_256": eval_large(net, dev),
            "device_error": net.check_device_error()}
     return out
