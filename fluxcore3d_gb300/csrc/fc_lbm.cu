@@ -307,13 +307,11 @@ __global__ void __launch_bounds__(BLOCK) k_convective_pass1(
     if (threadIdx.x == 0) { part_rho[blockIdx.x] = s_rho[0]; part_cnt[blockIdx.x] = s_cnt[0]; }
 }
 
-// Convective outlet, pass 2: every block reduces the partials in the same
-// order, then rescales its fluid outlet nodes by rho_out * count / sum(rho).
-template <class R>
-__global__ void __launch_bounds__(BLOCK) k_convective_pass2(
-    R* __restrict__ f, const uint8_t* __restrict__ solid, int nx, int ny, int nz, int axis,
-    int outlet_idx, double rho_out, int n1, int n2, const double* __restrict__ part_rho,
-    const int* __restrict__ part_cnt, int n_parts) {
+// Convective outlet, plane totals: one block reduces the per-block partials in a
+// fixed order and leaves the sum of rho and the fluid count in slot 0 (every
+// partial is read before the slot is written).
+__global__ void __launch_bounds__(BLOCK) k_convective_total(double* __restrict__ part_rho, int* __restrict__ part_cnt,
+                                                            int n_parts) {
     __shared__ double s_rho[BLOCK];
     __shared__ int s_cnt[BLOCK];
     double r = 0.0;
@@ -329,8 +327,21 @@ __global__ void __launch_bounds__(BLOCK) k_convective_pass2(
         }
         __syncthreads();
     }
-    const double sum = s_rho[0];
-    const int cnt = s_cnt[0];
+    if (threadIdx.x == 0) {
+        part_rho[0] = s_rho[0];
+        part_cnt[0] = s_cnt[0];
+    }
+}
+
+// Convective outlet, pass 2: rescale the fluid outlet nodes by
+// rho_out * count / sum(rho), the plane totals left in slot 0.
+template <class R>
+__global__ void __launch_bounds__(BLOCK) k_convective_pass2(
+    R* __restrict__ f, const uint8_t* __restrict__ solid, int nx, int ny, int nz, int axis,
+    int outlet_idx, double rho_out, int n1, int n2, const double* __restrict__ part_rho,
+    const int* __restrict__ part_cnt) {
+    const double sum = part_rho[0];
+    const int cnt = part_cnt[0];
     const int t = blockIdx.x * blockDim.x + threadIdx.x;
     if (t >= n1 * n2) return;
     if (cnt < 1 || sum < 1e-10) return;
@@ -882,8 +893,11 @@ int fc_lbm_convective_bc(float* f, const uint8_t* solid, int nx, int ny, int nz,
                                              n1, n2, part_rho, part_cnt);
     int rc = launch_status();
     if (rc) return rc;
+    k_convective_total<<<1, BLOCK, 0, st>>>(part_rho, part_cnt, nb);
+    rc = launch_status();
+    if (rc) return rc;
     k_convective_pass2<<<nb, BLOCK, 0, st>>>(f, solid, nx, ny, nz, axis, outlet_idx, rho_out_lat, n1, n2,
-                                             part_rho, part_cnt, nb);
+                                             part_rho, part_cnt);
     return launch_status();
 }
 
@@ -987,8 +1001,11 @@ int fc_lbm64_convective_bc(double* f, const uint8_t* solid, int nx, int ny, int 
                                              n1, n2, part_rho, part_cnt);
     int rc = launch_status();
     if (rc) return rc;
+    k_convective_total<<<1, BLOCK, 0, st>>>(part_rho, part_cnt, nb);
+    rc = launch_status();
+    if (rc) return rc;
     k_convective_pass2<<<nb, BLOCK, 0, st>>>(f, solid, nx, ny, nz, axis, outlet_idx, rho_out_lat, n1, n2,
-                                             part_rho, part_cnt, nb);
+                                             part_rho, part_cnt);
     return launch_status();
 }
 
@@ -1009,8 +1026,9 @@ int fc_lbm64_convective_bc(double* f, const uint8_t* solid, int nx, int ny, int 
 // the first call made on each device (with that device current) and cached;
 // make that first call before any stream capture.  All calls share the one
 // array, so calls whose kernels overlap on the GPU (different streams without
-// ordering) race on it.  Every slot the second pass reads is written by the
-// first pass of the same call, so nothing has to be cleared between calls.
+// ordering) race on it.  Every slot the totals pass reads is written by the
+// first pass of the same call, and the totals pass writes slot 0 that the last
+// pass reads, so nothing has to be cleared between calls.
 // ---------------------------------------------------------------------------
 #define FC_NOALLOC_CONVECTIVE_MAX_BLOCKS 4096
 static __device__ __align__(256) unsigned char g_noalloc_convective_scratch[FC_NOALLOC_CONVECTIVE_MAX_BLOCKS *
@@ -1055,8 +1073,11 @@ int fc_lbm_convective_bc_noalloc(float* f, const uint8_t* solid, int nx, int ny,
                                              n1, n2, part_rho, part_cnt);
     rc = launch_status();
     if (rc) return rc;
+    k_convective_total<<<1, BLOCK, 0, st>>>(part_rho, part_cnt, nb);
+    rc = launch_status();
+    if (rc) return rc;
     k_convective_pass2<<<nb, BLOCK, 0, st>>>(f, solid, nx, ny, nz, axis, outlet_idx, rho_out_lat, n1, n2,
-                                             part_rho, part_cnt, nb);
+                                             part_rho, part_cnt);
     return launch_status();
 }
 

@@ -4,7 +4,7 @@ fc_lbm_convective_bc_noalloc serves callers that may not allocate device memory
 once their time loop runs (a host that hands out all GPU memory from its own
 pre-reserved arena, or a path where an allocation would synchronise the
 device).  It must give the same plane, bit for bit, as fc_lbm_convective_bc with a caller
-workspace (both run the same two kernels), on calls in a row that go from a
+workspace (both run the same three kernels), on calls in a row that go from a
 large plane to smaller ones, so that a later call finds the partial sums of an
 earlier, larger plane left in the shared fixed array, and it must refuse planes
 beyond its fixed capacity.
