@@ -19,7 +19,8 @@
 // table saying which staged element each of them replaces.  Link cells and
 // links are stored in cell order, so a tile's links are one contiguous range;
 // fc_lbm_tile_links precomputes it with the first link of every chunk.
-// Persistent CTAs of 4 warps (3 per SM) rotate over 2 shared-memory stages
+// Persistent CTAs of 4 warps (4 per SM at 16-bit storage, 2 at FP32) rotate over
+// 2 shared-memory stages
 // tracked by mbarriers; warps run through the tiles independently and the last
 // warp done with a stage refills it, so no CTA-wide barrier sits in the loop.
 //
@@ -49,7 +50,11 @@ namespace fc {
 namespace {
 
 constexpr int TS_THREADS = 128;
-constexpr int TS_MIN_BLOCKS = 3;           // 3 CTAs of 4 warps per SM (<= 170 registers a thread)
+// CTAs of 4 warps per SM the register budget is set for: 4 at 16-bit storage
+// (<= 128 registers a thread; 4 x 52.6 KB of stages fit the SM's shared memory),
+// 3 at FP32 (whose 95 KB of stages allow 2 CTAs per SM anyway)
+template <int KIND>
+constexpr int ts_min_blocks() { return KIND == ST_F32 ? 3 : 4; }
 constexpr int TS_WARPS = TS_THREADS / 32;
 constexpr int TS_RANGE_CACHE = 64;         // per-CTA cache of the records of its first tiles
 constexpr int TS_HEAD_BYTES = 128 + TS_RANGE_CACHE * 32;   // mbarriers, stage counters, record cache
@@ -337,7 +342,7 @@ __device__ __forceinline__ TileRec tile_rec(const FusedArgs& a, const TileRec* c
 }
 
 template <int KIND, int MODE>
-__global__ void __launch_bounds__(TS_THREADS, TS_MIN_BLOCKS)
+__global__ void __launch_bounds__(TS_THREADS, ts_min_blocks<KIND>())
     k_fused_tma(const __grid_constant__ FusedArgs a, const __grid_constant__ PopMaps tm_pop,
                 const __grid_constant__ CUtensorMap tm_flag, const TileGeo tg) {
     using LY = Layout<KIND>;
