@@ -455,9 +455,15 @@ __global__ void __launch_bounds__(TS_THREADS, ts_min_blocks<KIND>())
                 }
             }
             const bool live_a = !(fa & CF_SOLID), live_b = !(fb & CF_SOLID);
-            const bool edge_row = plane_edge | (((j == 0) | (j == ny - 1)) & !wrapped);
-            const bool ea = live_a & (edge_row | ((a.g.pz == 0) & (k == 0)));
-            const bool eb = live_b & (edge_row | ((a.g.pz == 0) & (k + 1 == nz - 1)));
+            // Direct loads where a pull leaves the staged boxes: rows across an unstaged y
+            // boundary, cells on a non-periodic z boundary, and x-boundary cells that are not
+            // inlet/outlet plane cells.  On an inlet/outlet plane the pulls that leave the
+            // grid are exactly the plane's unknown directions, which the plane kernel
+            // replaces before anything reads them (Zou/He rebuilds them, the convective
+            // outlet copies them from the interior), so those cells keep the staged values.
+            const bool edge_row = ((j == 0) | (j == ny - 1)) & !wrapped;
+            const bool ea = live_a & (edge_row | (plane_edge & !(fa & CF_DEFER)) | ((a.g.pz == 0) & (k == 0)));
+            const bool eb = live_b & (edge_row | (plane_edge & !(fb & CF_DEFER)) | ((a.g.pz == 0) & (k + 1 == nz - 1)));
             const bool link_a = live_a && (fa & CF_LINK), link_b = live_b && (fb & CF_LINK);
             const bool unstaged = staged < 0;
             if (ea | eb | (unstaged & (link_a | link_b)) | (((fa | fb) & (CF_DEFER | CF_WRITE_S)) != 0)) {
