@@ -39,10 +39,8 @@
 // DEV_ERR_TIMEOUT, waits (again bounded) for the copies it still has in flight
 // and returns, so a lost copy never hangs the device.
 #include "fc_fused.cuh"
+#include "fc_tma.cuh"
 #include "../../include/fluxcore3d_gb300.h"
-
-#include <cuda.h>
-#include <cudaTypedefs.h>
 
 #include <mutex>
 
@@ -114,59 +112,6 @@ struct TileInfo {
     unsigned short pre[TS_PRE];
     int wrap;    // 1: the rows this tile pulls across the periodic y boundary are staged
 };
-
-__device__ __forceinline__ uint32_t su32(const void* p) {
-    return static_cast<uint32_t>(__cvta_generic_to_shared(p));
-}
-
-__device__ __forceinline__ void bar_init(uint32_t bar, unsigned count) {
-    asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(bar), "r"(count) : "memory");
-}
-
-__device__ __forceinline__ void bar_expect_tx(uint32_t bar, uint32_t bytes) {
-    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(bar), "r"(bytes) : "memory");
-}
-
-__device__ __forceinline__ bool bar_wait(uint32_t bar, unsigned parity, unsigned limit = TS_SPIN) {
-    for (unsigned it = 0; it < limit; ++it) {
-        uint32_t done;
-        asm volatile(
-            "{\n\t.reg .pred p;\n\t"
-            "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
-            "selp.u32 %0, 1, 0, p;\n\t}"
-            : "=r"(done)
-            : "r"(bar), "r"(parity)
-            : "memory");
-        if (done) return true;
-    }
-    return false;
-}
-
-__device__ __forceinline__ void tma_load_5d(uint32_t dst, const CUtensorMap* tm, int c0, int c1, int c2, int c3,
-                                            int c4, uint32_t bar) {
-    asm volatile(
-        "cp.async.bulk.tensor.5d.shared::cluster.global.mbarrier::complete_tx::bytes"
-        " [%0], [%1, {%2, %3, %4, %5, %6}], [%7];" ::"r"(dst),
-        "l"(reinterpret_cast<uint64_t>(tm)), "r"(c0), "r"(c1), "r"(c2), "r"(c3), "r"(c4), "r"(bar)
-        : "memory");
-}
-
-__device__ __forceinline__ void tma_load_4d(uint32_t dst, const CUtensorMap* tm, int c0, int c1, int c2, int c3,
-                                            uint32_t bar) {
-    asm volatile(
-        "cp.async.bulk.tensor.4d.shared::cluster.global.mbarrier::complete_tx::bytes"
-        " [%0], [%1, {%2, %3, %4, %5}], [%6];" ::"r"(dst),
-        "l"(reinterpret_cast<uint64_t>(tm)), "r"(c0), "r"(c1), "r"(c2), "r"(c3), "r"(bar)
-        : "memory");
-}
-
-// plain bulk copy global -> shared (16-byte aligned ends, size a multiple of 16)
-__device__ __forceinline__ void bulk_load(uint32_t dst, const void* src, uint32_t bytes, uint32_t bar) {
-    asm volatile(
-        "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(dst),
-        "l"(reinterpret_cast<uint64_t>(src)), "r"(bytes), "r"(bar)
-        : "memory");
-}
 
 // Link slice of a tile as staged (16-byte aligned ends), or staged = -1 when
 // it is absent, invalid or too large.
@@ -639,22 +584,6 @@ __global__ void k_link_src(const FusedArgs a, uint2* src) {
 // ---------------------------------------------------------------------------
 // host side
 // ---------------------------------------------------------------------------
-using EncodeTiled = PFN_cuTensorMapEncodeTiled_v12000;
-
-EncodeTiled encode_tiled() {
-    static EncodeTiled fn = nullptr;
-    static std::once_flag once;
-    std::call_once(once, [] {
-        void* p = nullptr;
-        cudaDriverEntryPointQueryResult q;
-        if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000, cudaEnableDefault, &q) ==
-                cudaSuccess &&
-            q == cudaDriverEntryPointSuccess)
-            fn = reinterpret_cast<EncodeTiled>(p);
-    });
-    return fn;
-}
-
 int storage_bytes(int storage) { return storage == ST_F32 ? 4 : 2; }
 
 TileGeo tile_geo(const Geo& g, int storage) {
@@ -733,6 +662,21 @@ __global__ void k_wait_selftest(unsigned polls, int arrive, unsigned* status) {
 }
 
 }  // namespace
+
+// cuTensorMapEncodeTiled through the runtime's driver entry point (no -lcuda link)
+EncodeTiled encode_tiled() {
+    static EncodeTiled fn = nullptr;
+    static std::once_flag once;
+    std::call_once(once, [] {
+        void* p = nullptr;
+        cudaDriverEntryPointQueryResult q;
+        if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000, cudaEnableDefault, &q) ==
+                cudaSuccess &&
+            q == cudaDriverEntryPointSuccess)
+            fn = reinterpret_cast<EncodeTiled>(p);
+    });
+    return fn;
+}
 
 bool fused_tma_eligible(const FusedArgs& a, int storage) {
     const Geo& g = a.g;

@@ -23,6 +23,7 @@
 #include <initializer_list>
 
 #include "fc_common.cuh"
+#include "fc_tma.cuh"
 #include "../../include/fluxcore3d_gb300.h"
 
 using namespace fc;
@@ -482,6 +483,84 @@ __global__ void __launch_bounds__(PAIR_X * PAIR_Y) k_prolong4(float* __restrict_
                       prolong_cell(xc, cy, cz, i, j, k + 3, cx, xv.w, m.w, alpha));
 }
 
+// TMA-staged prolongation of an exact 2:1 coarsening (nz a multiple of 8, at
+// most 256): a CTA corrects R whole fine rows of one fine plane i (R = 2 *
+// max(1, 256 / nz), so R nz <= 512 cells, four per thread).  Everything those
+// cells interpolate from -- coarse planes pl, pl+1 and coarse rows
+// j0/2 - 1 .. (j0 + R)/2, every column -- arrives in shared memory with one
+// tensor copy (rows or planes outside the level read as zero and are never
+// used: src_2to1 clamps to the level), so the eight-point stencils read shared
+// memory instead of L1.  The fine x and mask move as float4.  The same
+// roundings as prolong_cell, so the result equals k_prolong4's bit for bit.
+// If the copy's bounded wait gives up, the CTA interpolates from global memory
+// instead (same result) and waits again, bounded, before it retires.
+constexpr int PT_THREADS = 128;
+
+__device__ __forceinline__ float prolong_cell_tile(const float* __restrict__ tile, int pl, int jc0, int rows, int cy,
+                                                   int cz, int i, int j, int k, int cx, float xv, float m,
+                                                   float alpha) {
+    int i0, i1, j0, j1, k0, k1;
+    float li, lj, lk;
+    src_2to1(i, cx, i0, i1, li);
+    src_2to1(j, cy, j0, j1, lj);
+    src_2to1(k, cz, k0, k1, lk);
+    const float hi = 1.f - li, hj = 1.f - lj, hk = 1.f - lk;
+    const int p0 = (i0 - pl) * rows * cz, p1 = (i1 - pl) * rows * cz, r0 = (j0 - jc0) * cz, r1 = (j1 - jc0) * cz;
+    auto X = [&](int p, int r, int c) { return tile[p + r + c]; };
+    auto zl = [&](int p, int r) { return __fmaf_rn(lk, X(p, r, k1), __fmul_rn(hk, X(p, r, k0))); };
+    const float y0 = __fmaf_rn(lj, zl(p0, r1), __fmul_rn(hj, zl(p0, r0)));
+    const float y1 = __fmaf_rn(lj, zl(p1, r1), __fmul_rn(hj, zl(p1, r0)));
+    const float e = __fmaf_rn(li, y1, __fmul_rn(hi, y0));
+    return __fmul_rn(__fmaf_rn(alpha, e, xv), m);
+}
+
+__global__ void __launch_bounds__(PT_THREADS) k_prolong_tma(const __grid_constant__ CUtensorMap tmc,
+                                                            float* __restrict__ x, const float* __restrict__ xc,
+                                                            const float* __restrict__ mask, int nx, int ny, int nz,
+                                                            int cx, int cy, int cz, int R, float alpha) {
+    // [2][rows][cz] coarse floats, then the mbarrier (no static shared memory, so the
+    // tile starts on the 128-byte boundary the tensor copy needs)
+    extern __shared__ __align__(128) unsigned char pt_smem[];
+    float* tile = reinterpret_cast<float*>(pt_smem);
+    const int i = blockIdx.y;
+    const int jf0 = blockIdx.x * R;
+    const int m = i >> 1;
+    const int pl = ((i & 1) == 0 && m > 0) ? m - 1 : m;   // first coarse plane of the box
+    const int jc0 = (jf0 >> 1) - 1;                       // first coarse row of the box
+    const int rows = R / 2 + 2;
+    const uint32_t tile_bytes = (uint32_t)(2 * rows * cz) * 4u;   // a multiple of 32 (cz % 4 == 0)
+    const uint32_t b = su32(pt_smem + tile_bytes);
+    if (threadIdx.x == 0) {
+        bar_init(b, 1);
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+        asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+        bar_expect_tx(b, tile_bytes);
+        tma_load_3d(su32(tile), &tmc, 0, jc0, pl, b);
+    }
+    __syncthreads();
+    const bool staged = bar_wait(b, 0u);
+    const int per_row = nz >> 2;
+    const int r = threadIdx.x / per_row;
+    const int k = (threadIdx.x - r * per_row) * 4;
+    const int j = jf0 + r;
+    if (r < R && j < ny) {
+        const int idx = (i * ny + j) * nz + k;
+        float4* xp = reinterpret_cast<float4*>(x + idx);
+        const float4 xv = *xp, mv = __ldg(reinterpret_cast<const float4*>(mask + idx));
+        if (staged)
+            *xp = make_float4(prolong_cell_tile(tile, pl, jc0, rows, cy, cz, i, j, k, cx, xv.x, mv.x, alpha),
+                              prolong_cell_tile(tile, pl, jc0, rows, cy, cz, i, j, k + 1, cx, xv.y, mv.y, alpha),
+                              prolong_cell_tile(tile, pl, jc0, rows, cy, cz, i, j, k + 2, cx, xv.z, mv.z, alpha),
+                              prolong_cell_tile(tile, pl, jc0, rows, cy, cz, i, j, k + 3, cx, xv.w, mv.w, alpha));
+        else
+            *xp = make_float4(prolong_cell(xc, cy, cz, i, j, k, cx, xv.x, mv.x, alpha),
+                              prolong_cell(xc, cy, cz, i, j, k + 1, cx, xv.y, mv.y, alpha),
+                              prolong_cell(xc, cy, cz, i, j, k + 2, cx, xv.z, mv.z, alpha),
+                              prolong_cell(xc, cy, cz, i, j, k + 3, cx, xv.w, mv.w, alpha));
+    }
+    if (!__syncthreads_and(staged) && threadIdx.x == 0) bar_wait(b, 0u);   // let a late copy land first
+}
+
 // per-block partial sums of (w * (b - M x))^2 in FP64, w = mask or 1
 __global__ void __launch_bounds__(BLOCK) k_residual_sq(const float* __restrict__ x, const float* __restrict__ b,
                                                        const float* __restrict__ mask, Coef a, float dt, Lvl g,
@@ -836,13 +915,48 @@ int fc_mg_residual_restrict(const float* x, const float* b, const float* mask, c
     return launch_status();
 }
 
+}  // extern "C"
+
+namespace {
+// Launch the TMA-staged prolongation when the level fits it (returns false, having
+// launched nothing, otherwise): nz a multiple of 8 and at most 256, the fine
+// fields 16-byte aligned, the coarse field 16-byte aligned for the tensor map.
+bool prolong_tma(float* x, const float* xc, const float* mask, int nx, int ny, int nz, int cx, int cy, int cz,
+                 float alpha, cudaStream_t st) {
+    if (nz % 8 != 0 || nz < 16 || nz > 256) return false;
+    if ((reinterpret_cast<uintptr_t>(x) | reinterpret_cast<uintptr_t>(mask) | reinterpret_cast<uintptr_t>(xc)) & 15)
+        return false;
+    const EncodeTiled enc = encode_tiled();
+    if (!enc) return false;
+    const int R = 2 * (256 / nz > 1 ? 256 / nz : 1);
+    const int rows = R / 2 + 2;
+    CUtensorMap tm;
+    const cuuint64_t dims[3] = {(cuuint64_t)cz, (cuuint64_t)cy, (cuuint64_t)cx};
+    const cuuint64_t strides[2] = {(cuuint64_t)cz * 4, (cuuint64_t)cy * cz * 4};
+    const cuuint32_t box[3] = {(cuuint32_t)cz, (cuuint32_t)rows, 2};
+    const cuuint32_t es[3] = {1, 1, 1};
+    if (enc(&tm, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 3, const_cast<float*>(xc), dims, strides, box, es,
+            CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_128B,
+            CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) != CUDA_SUCCESS)
+        return false;
+    const size_t smem = (size_t)2 * rows * cz * sizeof(float) + 8;   // tile + mbarrier
+    const dim3 grid((unsigned)((ny + R - 1) / R), (unsigned)nx);
+    k_prolong_tma<<<grid, PT_THREADS, smem, st>>>(tm, x, xc, mask, nx, ny, nz, cx, cy, cz, R, alpha);
+    return true;
+}
+}  // namespace
+
+extern "C" {
+
 int fc_mg_prolong_correct(float* x, const float* x_coarse, const float* mask, int nx, int ny, int nz, int cx,
                           int cy, int cz, float alpha, void* stream) {
     if (!x || !x_coarse || !mask || nx < 1 || ny < 1 || nz < 1 || cx < 1 || cy < 1 || cz < 1) return FC_ERR_ARG;
     if ((long long)nx * ny * nz >= (1LL << 31)) return FC_ERR_ARG;
     if (nx == 2 * cx && ny == 2 * cy && nz == 2 * cz) {
         const Lvl g{nx, ny, nz, 0, 0};
-        if (nz >= 4 * PAIR_X && nz % 4 == 0 && pair_ok(g, {x, mask}) &&
+        if (prolong_tma(x, x_coarse, mask, nx, ny, nz, cx, cy, cz, alpha, (cudaStream_t)stream)) {
+            // the TMA-staged kernel took it
+        } else if (nz >= 4 * PAIR_X && nz % 4 == 0 && pair_ok(g, {x, mask}) &&
             !((reinterpret_cast<uintptr_t>(x) | reinterpret_cast<uintptr_t>(mask)) & 15)) {
             // whole warps of four cells per thread on the wide levels
             const dim3 grid((unsigned)((nz + 4 * PAIR_X - 1) / (4 * PAIR_X)), (unsigned)((ny + PAIR_Y - 1) / PAIR_Y),

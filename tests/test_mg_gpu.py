@@ -372,3 +372,31 @@ def test_solver_graphs_follow_a_rebuilt_hierarchy(cuda):
     assert i2["converged"] and i3["converged"]
     assert rel(x2.cpu().numpy(), x3.cpu().numpy()) < 1e-8
     assert rel(x2.cpu().numpy(), x1.cpu().numpy()) > 1e-4
+
+
+@pytest.mark.parametrize("shape", [(16, 12, 128), (10, 6, 64), (8, 20, 256), (6, 8, 48)])
+def test_prolongation_tma_staged_bit_identical(cuda, shape):
+    """The TMA-staged prolongation (taken for a 16-byte aligned coarse field, nz a multiple of 8 up to
+    256) and the direct-load kernels (taken when the coarse field is only 4-byte aligned) give the same
+    bits, partial last row-blocks and the clamped first/last coarse rows and planes included."""
+    from fluxcore3d_gb300 import _lib
+    from fluxcore3d_gb300._torch import ptr, stream_ptr
+    nx, ny, nz = shape
+    N = nx * ny * nz
+    nc = (nx // 2) * (ny // 2) * (nz // 2)
+    g = torch.Generator(device="cpu").manual_seed(5)
+    xc0 = torch.randn(nc, generator=g).to(cuda)
+    x0 = torch.randn(N, generator=g).to(cuda)
+    m0 = (torch.rand(N, generator=g) > 0.2).float().to(cuda)
+    out = []
+    for off in (0, 1):   # coarse offset 0: 16-byte aligned (TMA); 1: 4-byte aligned (direct loads)
+        bc = torch.zeros(nc + 4, device=cuda)
+        xc = bc[off:off + nc]
+        xc.copy_(xc0)
+        x = x0.clone()
+        _lib.call("fc_mg_prolong_correct", ptr(x), ptr(xc), ptr(m0), nx, ny, nz, nx // 2, ny // 2, nz // 2, 0.75,
+                  stream_ptr())
+        torch.cuda.synchronize()
+        out.append(x)
+    assert torch.equal(out[0].view(torch.int32), out[1].view(torch.int32))
+    assert not torch.equal(out[0], x0)
