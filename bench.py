@@ -318,32 +318,6 @@ def _velocity_of(sim):
     return (c.t() @ f) / f.sum(0)
 
 
-def _wall_heat(T, k, solid, D):
-    """Heat flow through the solid/fluid faces (harmonic-mean conductance times the temperature
-    jump, summed over the 6-neighbour faces), the face count, and the Nusselt number
-    Nu = (Q / A) * D / (k_f * mean wall temperature rise over the inlet)."""
-    import numpy as np
-    q, n, tw = 0.0, 0, 0.0
-    for ax in range(3):
-        a = [slice(None)] * 3
-        b = [slice(None)] * 3
-        a[ax] = slice(0, -1)
-        b[ax] = slice(1, None)
-        sa, sb = solid[tuple(a)], solid[tuple(b)]
-        face = sa != sb
-        ka, kb = k[tuple(a)], k[tuple(b)]
-        kh = 2.0 * ka * kb / (ka + kb)
-        Ta, Tb = T[tuple(a)], T[tuple(b)]
-        ts = np.where(sa, Ta, Tb)
-        tf = np.where(sa, Tb, Ta)
-        q += float((kh * (ts - tf))[face].sum())
-        n += int(face.sum())
-        tw += float((0.5 * (ts + tf))[face].sum())
-    k_f = float(k[~solid].min())
-    tw /= max(n, 1)
-    return q, n, (q / n) * D / (k_f * tw)
-
-
 def accuracy_run(args, dev):
     """FP32-, FP16- and BF16-storage runs of the fused engine against an FP64 run of the plain method
     (fluxcore3d_gb300.lattice64: the reference step sequence in double precision on the device), from
@@ -356,7 +330,7 @@ def accuracy_run(args, dev):
     import torch
     from fluxcore3d_gb300 import case as cases
     from fluxcore3d_gb300 import thermal_bench
-    from fluxcore3d_gb300.diagnostics import heat_balance, lbm_mass
+    from fluxcore3d_gb300.diagnostics import heat_balance, lbm_mass, wall_heat
     from fluxcore3d_gb300.lattice64 import Lattice64
     from fluxcore3d_gb300.solver import mg_pcg
     from fluxcore3d_gb300.solver.lbm_cuda_ext import LBMCUDAUpgrade
@@ -412,7 +386,7 @@ def accuracy_run(args, dev):
         T[name] = x.reshape(shape).cpu().numpy().astype("float64")
         hb = heat_balance(mg, x, b / 1000.0, 1000.0)
         out["heat_balance"][name] = {kk: (float(f"{vv:.6g}")) for kk, vv in hb.items()}
-        heat[name] = _wall_heat(T[name], k, solid, 2 * 3.5)
+        heat[name] = wall_heat(T[name], k, solid, 2 * 3.5)
         out["nusselt"][name] = round(heat[name][2], 6)
     import numpy as np
     for name in ("fp32", "fp16", "bf16"):

@@ -41,3 +41,29 @@ def heat_balance(mg, T: torch.Tensor, src: torch.Tensor, dt: float) -> dict:
     q_store = t_sum / float(dt)
     return {"heat_generated": q_src, "heat_out_through_boundaries": q_out, "heat_stored": q_store,
             "imbalance_rel": abs(q_src - q_out - q_store) / max(abs(q_src), 1e-300)}
+
+
+def wall_heat(T, k, solid, D):
+    """Host-side post-processing of a solved temperature field (numpy arrays T, k, solid): heat flow through the solid/fluid faces (harmonic-mean conductance times the temperature
+    jump, summed over the 6-neighbour faces), the face count, and the Nusselt number
+    Nu = (Q / A) * D / (k_f * mean wall temperature rise over the inlet)."""
+    import numpy as np
+    q, n, tw = 0.0, 0, 0.0
+    for ax in range(3):
+        a = [slice(None)] * 3
+        b = [slice(None)] * 3
+        a[ax] = slice(0, -1)
+        b[ax] = slice(1, None)
+        sa, sb = solid[tuple(a)], solid[tuple(b)]
+        face = sa != sb
+        ka, kb = k[tuple(a)], k[tuple(b)]
+        kh = 2.0 * ka * kb / (ka + kb)
+        Ta, Tb = T[tuple(a)], T[tuple(b)]
+        ts = np.where(sa, Ta, Tb)
+        tf = np.where(sa, Tb, Ta)
+        q += float((kh * (ts - tf))[face].sum())
+        n += int(face.sum())
+        tw += float((0.5 * (ts + tf))[face].sum())
+    k_f = float(k[~solid].min())
+    tw /= max(n, 1)
+    return q, n, (q / n) * D / (k_f * tw)

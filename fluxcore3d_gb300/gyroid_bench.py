@@ -7,7 +7,8 @@ Reported:
   accuracy     FP32 and FP16 storage runs against the device FP64 run of the plain method
                (fluxcore3d_gb300.lattice64) from the same initial state after `steps` steps: velocity
                (relative L2 over fluid cells) and the temperature that each velocity field gives
-               (relative max and L2), the thermal system solved to a 1e-10 FP64 residual;
+               (relative max and L2), the thermal system solved to a 1e-10 FP64 residual, with the
+               wall heat flow and the Nusselt number on the gyroid's L/4 = 12 cells;
   thermal      the steady thermal solve on the FP64 velocity with the 5-level geometric multigrid to
                a 1e-8 FP64 relative residual: plain FP64 BiCGSTAB around the FP32 V-cycle, the mixed
                solver (FP64 refinement around FP32 BiCGSTAB), and the plain solver with the exact FP64
@@ -119,15 +120,23 @@ def accuracy_block(dev, steps, **kw):
         del sim
     U64 = vel["fp64"][:, fluid]
     out = {"steps": steps, "fp64_run_s": round(fp64_s, 2), "fp64_velocity_change_last_500_steps": change,
-           "velocity_rel_l2": {}, "temperature_rel_max": {}, "temperature_rel_l2": {}}
-    T = {}
+           "velocity_rel_l2": {}, "temperature_rel_max": {}, "temperature_rel_l2": {}, "wall_heat_flow_rel": {},
+           "nusselt": {}, "nusselt_rel": {}}
+    from .diagnostics import wall_heat
+    T, heat = {}, {}
+    k_np = ref.k.cpu().numpy().astype("float64")
+    solid_np = ref.solid.cpu().numpy()
     for name, u in vel.items():
         T[name] = _temperature(ref, u)[0]
+        heat[name] = wall_heat(T[name].reshape(ref.nx, ref.ny, ref.nz).cpu().numpy(), k_np, solid_np, 12.0)
+        out["nusselt"][name] = round(heat[name][2], 6)
     for name in ("fp32", "fp16"):
         out["velocity_rel_l2"][name] = float(torch.linalg.norm(vel[name][:, fluid] - U64) / torch.linalg.norm(U64))
         dT = T[name] - T["fp64"]
         out["temperature_rel_max"][name] = float(dT.abs().max() / T["fp64"].abs().max())
         out["temperature_rel_l2"][name] = float(torch.linalg.norm(dT) / torch.linalg.norm(T["fp64"]))
+        out["wall_heat_flow_rel"][name] = abs(heat[name][0] - heat["fp64"][0]) / abs(heat["fp64"][0])
+        out["nusselt_rel"][name] = abs(heat[name][2] - heat["fp64"][2]) / abs(heat["fp64"][2])
     return out, ref, vel["fp64"]
 
 
