@@ -77,12 +77,23 @@ class StepArgs(C.Structure):
         ("link_src", C.c_void_p),
         ("n_link_src", C.c_int64),
         ("skip_link_gather", C.c_int32),
+        ("tracer_in", vp),
+        ("tracer_out", vp),
+        ("tracer_u", vp),
+        ("tracer_v", vp),
+        ("tracer_w", vp),
+        ("tracer_solid", vp),
+        ("tracer_dissipation", f32),
     ]
+
+
+ABI_VERSION = 2   # FC_ABI_VERSION of the header these mirrors follow
 
 
 # name -> (restype, argtypes)
 SIGNATURES: dict[str, tuple] = {
     "fc_abi_version": (i32, []),
+    "fc_lbm_step_args_size": (i64, []),
     # lattice, per-operation
     "fc_lbm_macro_collide_bgk": (i32, [vp, vp, vp, vp, vp, vp, vp, f32, i64, vp]),
     "fc_lbm_macro_collide_trt": (i32, [vp, vp, vp, vp, vp, vp, vp, f32, f32, i64, vp]),
@@ -222,6 +233,11 @@ def _load():
             continue
         fn.restype = res
         fn.argtypes = args
+    size_fn = getattr(L, "fc_lbm_step_args_size", None)
+    if L.fc_abi_version() != ABI_VERSION or size_fn is None or size_fn() != C.sizeof(StepArgs):
+        _LOAD_ERROR = (f"{path} was built from another version of the interface "
+                       f"(ABI {L.fc_abi_version()}, expected {ABI_VERSION}): rebuild it")
+        return
     _LIB = L
 
 

@@ -89,6 +89,14 @@ struct FusedArgs {
     int has_links;
     CollideParams cp;
     unsigned* dev_err;
+    // passive tracer carried by the staged main pass (tr_in null: none)
+    const float* tr_in;
+    float* tr_out;
+    const float* tr_u;
+    const float* tr_v;
+    const float* tr_w;
+    const uint8_t* tr_solid;
+    float tr_diss;
 };
 
 // shifted value h = f - w_q of population q at `cell` of the input buffer

@@ -673,6 +673,12 @@ int make_fused_args(const fc_lbm_step_args* s, FusedArgs& a) {
     }
     a.cp.Cs_dx2 = s->Cs_dx2; a.cp.omega0 = s->omega0;
     a.dev_err = s->dev_err;
+    a.tr_in = s->tracer_in; a.tr_out = s->tracer_out;
+    a.tr_u = s->tracer_u; a.tr_v = s->tracer_v; a.tr_w = s->tracer_w;
+    a.tr_solid = s->tracer_solid; a.tr_diss = s->tracer_dissipation;
+    if (a.tr_in && (!a.tr_out || !a.tr_u || !a.tr_v || !a.tr_w || !a.tr_solid || a.tr_in == a.tr_out))
+        return FC_ERR_ARG;
+    if (a.tr_in && a.u && (a.tr_u == a.u || a.tr_v == a.v || a.tr_w == a.w)) return FC_ERR_ARG;
     if (!a.flags) return FC_ERR_ARG;
     if (a.n_links > 0 && (!a.link_off || !a.link_hdr || !a.link_w || a.n_link_cells <= 0)) return FC_ERR_ARG;
     return FC_OK;
@@ -753,6 +759,8 @@ int planes_dispatch(const FusedArgs& a, cudaStream_t st, const PlaneSet& ps) {
 extern "C" {
 
 int fc_abi_version(void) { return FC_ABI_VERSION; }
+
+long long fc_lbm_step_args_size(void) { return (long long)sizeof(fc_lbm_step_args); }
 
 static int check_collide_ptrs(const float* f, float* fp, float* r, float* u, float* v, float* w,
                               const uint8_t* s, long long n) {
@@ -1095,11 +1103,26 @@ int fc_lbm_fused_step(const fc_lbm_step_args* args, void* stream) {
             if (rc) return rc;
         }
         rc = FC_ERR_UNSUPPORTED;
-        if (!split && args->staging == 0 && args->cells_per_thread <= 1 && fused_tma_eligible(a, args->storage))
-            rc = launch_fused_tma(a, args->storage, args->collision, st);
+        bool tracer_done = false;
+        if (!split && args->staging == 0 && args->cells_per_thread <= 1 && fused_tma_eligible(a, args->storage)) {
+            // the staged pass reads and writes the tracer in cell pairs (8-byte words)
+            FusedArgs am = a;
+            const bool carry = a.tr_in && !((reinterpret_cast<uintptr_t>(a.tr_in) | reinterpret_cast<uintptr_t>(a.tr_out) |
+                                             reinterpret_cast<uintptr_t>(a.tr_u) | reinterpret_cast<uintptr_t>(a.tr_v) |
+                                             reinterpret_cast<uintptr_t>(a.tr_w)) & 7) &&
+                               !(reinterpret_cast<uintptr_t>(a.tr_solid) & 1);
+            if (!carry) am.tr_in = nullptr;
+            rc = launch_fused_tma(am, args->storage, args->collision, st);
+            tracer_done = rc == FC_OK && carry;
+        }
         if (rc == FC_ERR_UNSUPPORTED)
             rc = dispatch<StepLauncher>(args->storage, args->collision, a, st, split, args->cells_per_thread, 0, 0);
         if (rc) return rc;
+        if (a.tr_in && !tracer_done) {   // the direct pass does not carry the tracer
+            rc = fc_tracer_step(a.tr_in, a.tr_out, a.tr_u, a.tr_v, a.tr_w, a.tr_solid, a.g.nx, a.g.ny, a.g.nz,
+                                a.tr_diss, stream);
+            if (rc) return rc;
+        }
     }
     if (!split || !(phases & 2)) return FC_OK;
     return dispatch<LinkCellLauncher>(args->storage, args->collision, a, st, 0, 0, 0, 0);

@@ -35,6 +35,10 @@
 // whose link slice exceeds the stage's room take a path with direct global
 // loads.
 //
+// Tracer.  When the arguments carry a passive tracer, every lane also advances
+// it for its two cells (tracer_pair, all cells, solid ones included), so a step
+// with a tracer needs no tracer launch of its own.
+//
 // Every mbarrier wait is bounded.  A CTA whose wait gives up sets
 // DEV_ERR_TIMEOUT, waits (again bounded) for the copies it still has in flight
 // and returns, so a lost copy never hangs the device.
@@ -267,6 +271,47 @@ __device__ __forceinline__ Pair19 slow_lanes(const FusedArgs* ap, Pair19 p, uint
     return p;
 }
 
+// One step of the passive tracer for one cell: fc_tracer_step's arithmetic with
+// the same roundings (first-order upwind differences, clamp to [0, 1] keeping
+// NaN, dissipation, zero in flow-solid cells; tracer_patch.py:55-82).
+__device__ __forceinline__ float tracer_cell(float p, float xm, float xp, float ym, float yp, float zm, float zp,
+                                             float uc, float vc, float wc, bool solid, float diss) {
+    const float ax = uc >= 0.0f ? __fsub_rn(p, xm) : __fsub_rn(xp, p);
+    const float ay = vc >= 0.0f ? __fsub_rn(p, ym) : __fsub_rn(yp, p);
+    const float az = wc >= 0.0f ? __fsub_rn(p, zm) : __fsub_rn(zp, p);
+    const float s = __fadd_rn(__fadd_rn(__fmul_rn(uc, ax), __fmul_rn(vc, ay)), __fmul_rn(wc, az));
+    float n = __fsub_rn(p, s);
+    if (!isnan(n)) n = fminf(fmaxf(n, 0.0f), 1.0f);
+    n = __fmul_rn(n, diss);
+    return solid ? 0.0f : n;
+}
+
+// The tracer step of a lane's two cells (i, j, k) and (i, j, k + 1), k even: the
+// field and the velocity are read as 8-byte pairs, the upwind neighbours from
+// every axis with periodic wrap (the field's torch.roll), and the pair written
+// to the other tracer buffer.  Neighbour rows and planes are being read by the
+// warps and CTAs working next to this one, so most of those loads hit L2.
+__device__ __forceinline__ void tracer_pair(const FusedArgs& a, int i, int j, int k, int idx) {
+    const int nyz = a.g.nynz, nz = a.g.nz;
+    const int dxm = (i > 0 ? -1 : a.g.nx - 1) * nyz, dxp = (i + 1 < a.g.nx ? 1 : 1 - a.g.nx) * nyz;
+    const int dym = (j > 0 ? -1 : a.g.ny - 1) * nz, dyp = (j + 1 < a.g.ny ? 1 : 1 - a.g.ny) * nz;
+    const float* ph = a.tr_in;
+    const float2 p = __ldg(reinterpret_cast<const float2*>(ph + idx));
+    const float2 xm = __ldg(reinterpret_cast<const float2*>(ph + idx + dxm));
+    const float2 xp = __ldg(reinterpret_cast<const float2*>(ph + idx + dxp));
+    const float2 ym = __ldg(reinterpret_cast<const float2*>(ph + idx + dym));
+    const float2 yp = __ldg(reinterpret_cast<const float2*>(ph + idx + dyp));
+    const float zm = __ldg(ph + idx + (k > 0 ? -1 : nz - 1));        // k - 1 of cell k
+    const float zp = __ldg(ph + idx + (k + 2 < nz ? 2 : 2 - nz));    // k + 2 of cell k + 1
+    const float2 u = __ldg(reinterpret_cast<const float2*>(a.tr_u + idx));
+    const float2 v = __ldg(reinterpret_cast<const float2*>(a.tr_v + idx));
+    const float2 w = __ldg(reinterpret_cast<const float2*>(a.tr_w + idx));
+    const unsigned sd = __ldg(reinterpret_cast<const unsigned short*>(a.tr_solid + idx));
+    const float oa = tracer_cell(p.x, xm.x, xp.x, ym.x, yp.x, zm, p.y, u.x, v.x, w.x, (sd & 0xffu) != 0, a.tr_diss);
+    const float ob = tracer_cell(p.y, xm.y, xp.y, ym.y, yp.y, p.x, zp, u.y, v.y, w.y, (sd >> 8) != 0, a.tr_diss);
+    *reinterpret_cast<float2*>(a.tr_out + idx) = make_float2(oa, ob);
+}
+
 // Record of the CTA's m-th tile (from the shared cache for the first ones).
 __device__ __forceinline__ TileRec tile_rec(const FusedArgs& a, const TileRec* cache, int m, int t) {
     TileRec r;
@@ -385,8 +430,9 @@ __global__ void __launch_bounds__(TS_THREADS, ts_min_blocks<KIND>())
                                        : (unsigned)(CF_SOLID | (CF_SOLID << 8));
             const uint8_t fa = (uint8_t)(fl2 & 0xffu), fb = (uint8_t)(fl2 >> 8);
             if (!valid) continue;
-            if ((fa & fb & CF_SOLID) && !((fa | fb) & (CF_DEFER | CF_WRITE_S))) continue;
             const int idx = (i * ny + j) * nz + k;
+            if (a.tr_in) tracer_pair(a, i, j, k, idx);
+            if ((fa & fb & CF_SOLID) && !((fa | fb) & (CF_DEFER | CF_WRITE_S))) continue;
             f2 h[19];
             {
                 const int om = r * nz + (k > 0 ? k - 1 : nz - 1);        // source of cell k for c_z = +1

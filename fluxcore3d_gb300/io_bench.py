@@ -10,7 +10,9 @@
 * steps_with_snapshots: the time loop with a snapshot every 10 steps against the
   same loop without snapshots (device time per step).
 * tracer: device time of one fc_tracer_step (21 B/cell algorithmic) and of the
-  reference's tensor sequence for TracerField.step on the same fields.
+  reference's tensor sequence for TracerField.step on the same fields; and the
+  lattice step with macros written every step (what a tracer needs) alone, followed
+  by the separate tracer launch, and with the tracer carried by the main pass.
 * checkpoint: save_checkpoint / load_checkpoint wall time and size, file in /tmp.
 """
 from __future__ import annotations
@@ -145,6 +147,25 @@ def run(dev, steps=200):
     def ref():
         holder[0] = ref_step(holder[0])
     out["tracer_reference_sequence_ms"] = round(timed(ref), 4)
+    # the lattice step with the tracer after it (separate launch) and carried by the main pass
+    fc = sim._fc
+
+    def plain():
+        sim.step(do_thermal=False)
+
+    def separate():
+        sim.step(do_thermal=False)
+        tr.step()
+
+    def fused():
+        fc.tracer = tr
+        try:
+            sim.step(do_thermal=False)
+        finally:
+            fc.tracer = None
+    for name, fn in (("step_ms_macros_every_step", plain), ("step_ms_with_tracer_separate", separate),
+                     ("step_ms_with_tracer_fused", fused)):
+        out[name] = round(statistics.median([timed(fn, n=200) for _ in range(3)]), 4)
     # checkpoint
     path = os.path.join(tmp, "ck.npz")
     ts, tl = [], []

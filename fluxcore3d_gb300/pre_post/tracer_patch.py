@@ -8,6 +8,12 @@ Same fields, methods and printed lines.  `step()` is one launch of fc_tracer_ste
 `inject()` one launch of fc_tracer_inject.  The tracer reads sim.u / sim.v / sim.wv
 after every step, so attaching it makes the fused lattice engine write the macro
 fields every step (macro stride 1), as the reference's step does.
+
+On the fused lattice engine, attach_tracer(..., fuse=True) (the default) hands the
+tracer to the engine: each sim.step() then advances it inside the lattice main pass,
+reading the velocity the step exposes, instead of launching fc_tracer_step after the
+step.  The field is the same bit for bit; tracer.step() on its own (warmup) still
+launches the kernel.
 """
 from __future__ import annotations
 
@@ -85,14 +91,18 @@ class TracerField:
         return self.field.detach().cpu().numpy().astype(np.float32)
 
 
-def attach_tracer(sim, flow_dir="-Z", inject_depth=6, dissipation=0.9995):
+def attach_tracer(sim, flow_dir="-Z", inject_depth=6, dissipation=0.9995, *, fuse=True):
     tracer = TracerField(sim, flow_dir=flow_dir, inject_depth=inject_depth, dissipation=dissipation)
     fc = getattr(sim, "_fc", None)
     if fc is not None:
         fc.macro_stride = 1
+        if fuse:
+            fc.tracer = tracer
     _lbm_step = sim.step
 
     def _step_with_tracer(self_, do_thermal=False):
+        if fc is not None and fc.tracer is tracer:
+            return _lbm_step(do_thermal=do_thermal)   # the lattice pass advanced the tracer
         result = _lbm_step(do_thermal=do_thermal)
         tracer.step()
         return result

@@ -178,6 +178,7 @@ class FusedLBM:
         self.use_graphs = bool(getattr(cfg, "lbm_cuda_graph", True))
         self._graphs = {}
         self._eager_steps = 0
+        self.tracer = None  # a TracerField the main pass advances once per step (attach_tracer sets it)
         self.args = StepArgs()
         self._fill_static_args()
 
@@ -280,6 +281,19 @@ class FusedLBM:
             a.rho = a.u = a.v = a.w = None
         else:
             a.rho, a.u, a.v, a.w = (ptr(t) for t in m)
+
+    def _arm_tracer(self, tr, m):
+        """Point the step's tracer arguments at `tr`'s buffers, advected by the velocity in
+        macro set m (None clears them)."""
+        a = self.args
+        if tr is None:
+            a.tracer_in = a.tracer_out = a.tracer_u = a.tracer_v = a.tracer_w = a.tracer_solid = None
+            return
+        a.tracer_in = ptr(tr._buf[tr._cur])
+        a.tracer_out = ptr(tr._buf[1 - tr._cur])
+        a.tracer_u, a.tracer_v, a.tracer_w = (ptr(t) for t in m[1:])
+        a.tracer_solid = ptr(tr._solid_u8)
+        a.tracer_dissipation = float(tr.diss)
 
     def _expose(self, m):
         sim = self.sim
@@ -418,11 +432,22 @@ class FusedLBM:
         k = self.k + 1          # reference step number being completed
         nxt = 1 - self.cur
         write_m = (k % self.macro_stride) == 0
-        if self.use_graphs and not write_m and phase_event is None and self._eager_steps >= 1:
+        tr = self.tracer
+        if tr is not None:
+            # the tracer step that follows step k in the reference reads the macros exposed after
+            # step k: the ones the previous step wrote
+            self._arm_tracer(tr, self.M[(k - 1) % 2])
+        if self.use_graphs and not write_m and phase_event is None and self._eager_steps >= 1 and tr is None:
             self._graph(self.cur).replay()
         else:
-            self._enqueue(self.cur, self.M[k % 2] if write_m else None, phase_event)
+            try:
+                self._enqueue(self.cur, self.M[k % 2] if write_m else None, phase_event)
+            finally:
+                if tr is not None:
+                    self._arm_tracer(None, None)
             self._eager_steps += 1
+            if tr is not None:
+                tr._cur = 1 - tr._cur
         self.cur = nxt
         self.k = k
         # the reference exposes the pre-collision macros of this step's input state

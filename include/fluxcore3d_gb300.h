@@ -25,7 +25,7 @@
 extern "C" {
 #endif
 
-#define FC_ABI_VERSION 1
+#define FC_ABI_VERSION 2
 
 int fc_abi_version(void);
 
@@ -140,8 +140,9 @@ typedef struct fc_lbm_step_args {
     int32_t separate_link_pass;  /* 1: the main pass skips link cells and a second kernel runs them */
     int32_t cells_per_thread;    /* 1 or 2 (two rows per thread in the main pass); 0 is read as 1 */
     int32_t staging;             /* 0: main pass stages tiles of rows in shared memory with TMA when the
-                                    grid allows it (nz a multiple of 16 and at most 256, no separate link
-                                    pass, one cell per thread), 1: per-thread global loads always */
+                                    grid allows it (16 <= nz <= 512, nz a multiple of 16 per 256-element
+                                    row segment, no separate link pass, one cell per thread), 1: per-thread
+                                    global loads always */
     void* link_val;              /* optional scratch of n_links + 8 elements of the population storage type:
                                     when set, each step first gathers every link's interpolated bounce-back
                                     value into it in storage form (one thread per link cell, needs
@@ -162,10 +163,28 @@ typedef struct fc_lbm_step_args {
     int32_t skip_link_gather;    /* 1: fc_lbm_fused_step does not run the link gather; the caller runs
                                     fc_lbm_link_gather for this step's input beforehand (e.g. on a second
                                     stream while the previous step's plane work runs) */
+    /* Optional passive tracer carried by the main pass (tracer_in == NULL: none).  The step also
+     * performs exactly one fc_tracer_step(tracer_in -> tracer_out, tracer_u/v/w, tracer_solid,
+     * tracer_dissipation): inside the staged main pass when that pass runs, as its own launch
+     * otherwise; the field is the same bit for bit either way.  tracer_u/v/w are the velocity the
+     * tracer is advected by -- for the reference's wrapped step, the macros the lattice exposes
+     * after this step, i.e. the ones the previous step wrote -- and must not be this step's macro
+     * outputs.  Replaces the separate TracerField.step launch after each sim.step
+     * (pre_post/tracer_patch.py:55-82, 100-124). */
+    const float* tracer_in;
+    float* tracer_out;
+    const float* tracer_u;
+    const float* tracer_v;
+    const float* tracer_w;
+    const uint8_t* tracer_solid;
+    float tracer_dissipation;
 } fc_lbm_step_args;
 
 /* One full time step for every non-deferred cell. */
 int fc_lbm_fused_step(const fc_lbm_step_args* args, void* stream);
+/* sizeof(fc_lbm_step_args) as compiled, so a binding can check its mirror of the struct.
+ * No reference counterpart. */
+long long fc_lbm_step_args_size(void);
 
 /* Tiles of the TMA-staged main pass for this grid.  With records == NULL
  * returns the number of tiles (0 when the staged pass does not apply to the

@@ -1,5 +1,6 @@
 """The C-ABI library builds, loads without a GPU and exports every symbol the header declares;
 host-side logic (face roles, link tables, sponge profile, BC plan) on CPU tensors."""
+import ctypes
 import os
 import re
 import types
@@ -28,7 +29,8 @@ def test_library_exports_every_declared_symbol(native_lib):
     missing = [n for n in decl if not hasattr(native_lib, n)]
     assert not missing, missing
     assert set(_lib.SIGNATURES) >= decl
-    assert native_lib.fc_abi_version() == 1
+    assert native_lib.fc_abi_version() == _lib.ABI_VERSION
+    assert native_lib.fc_lbm_step_args_size() == ctypes.sizeof(_lib.StepArgs)
 
 
 def test_workspace_queries_without_gpu(native_lib):

@@ -75,3 +75,41 @@ def test_attach_tracer_follows_the_lattice_velocity(cuda):
         phi = ot.step(phi, u, v, w, solid)
     assert np.array_equal(bits(tr.get()), bits(phi))
     assert float(tr.field.max()) > 0.5
+
+
+@pytest.mark.parametrize("storage,collision", [("fp16", "mrt"), ("fp32", "trt")])
+def test_tracer_carried_by_the_staged_pass(cuda, storage, collision):
+    """attach_tracer hands the tracer to the lattice engine, whose staged main pass advances it:
+    the field equals the separate kernel's (fuse=False) and the oracle's step on the exposed
+    velocity, bit for bit, including injections between steps."""
+    def make(fuse):
+        sim = cases.channel_cube(device=cuda, collision=collision, storage=storage, nx=64, ny=32, nz=32, cube=8,
+                                 cube_x=20, outlet="pressure")
+        sim.cfg.macro_stride = 10
+        LBMCUDAUpgrade.patch(sim)
+        tr = attach_tracer(sim, flow_dir="+X", inject_depth=4, fuse=fuse)
+        return sim, tr
+    sim, tr = make(True)
+    ref_sim, ref_tr = make(False)
+    assert sim._fc.tracer is tr and ref_sim._fc.tracer is None
+    assert sim._fc.tile_links is not None          # the staged pass runs on this grid
+    solid = sim.solid_flow.cpu().numpy()
+    phi = None
+    for it in range(24):
+        if it % 10 == 0:
+            tr.inject()
+            ref_tr.inject()
+            phi = tr.get() if phi is None else np.where(tr._inlet.cpu().numpy(), np.float32(1.0), phi)
+        sim.step(do_thermal=False)
+        ref_sim.step(do_thermal=False)
+        u, v, w = (t.cpu().numpy() for t in (sim.u, sim.v, sim.wv))
+        phi = ot.step(phi, u, v, w, solid)
+        got = tr.get()
+        assert np.array_equal(bits(got), bits(ref_tr.get())), it
+        assert np.array_equal(bits(got), bits(phi)), it
+    assert sim._fc.check_device_error() == 0
+    assert float(tr.field.max()) > 0.5
+    # a tracer step on its own (warm-up style) still runs the kernel
+    tr.step()
+    ref_tr.step()
+    assert np.array_equal(bits(tr.get()), bits(ref_tr.get()))
