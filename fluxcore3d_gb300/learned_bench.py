@@ -143,6 +143,7 @@ def evaluate(net: UNetPreconditioner, n: int, seeds, dev, tol=1e-8, repeats=3, c
         rows.append({"seed": int(s), "plain_ms": round(plain_ms, 3), "plain_it": plain["it"],
                      "plain_res": plain["res_rel"], "learned_ms": round(learn_ms, 3), "learned_it": learn["it"],
                      "learned_res": learn["res_rel"], "learned_fell_back": learn["fell_back"],
+                     "learned_fell_back_at": learn.get("fell_back_at"),
                      "plain_bicgstab_ms": round(bicg_ms, 3), "plain_bicgstab_it": bicg["it"],
                      "plain_bicgstab_res": bicg["res_rel"]})
     return rows
@@ -197,7 +198,7 @@ def eval_large(net: UNetPreconditioner, dev, n=256, seeds=(2001, 2002), tol=1e-8
             _, info = fn()
             torch.cuda.synchronize()
             row[name] = {"ms": round((time.perf_counter() - t) * 1e3, 1), "it": info["it"], "res": info["res_rel"],
-                         "fell_back": info.get("fell_back")}
+                         "fell_back": info.get("fell_back"), "fell_back_at": info.get("fell_back_at")}
         rows.append(row)
         del mg, pc
         torch.cuda.empty_cache()

@@ -570,12 +570,14 @@ def bicgstab_mg_f64(mg_solver, b: Tensor, x0: Optional[Tensor] = None, tol: floa
 
 def fgmres_mg_f64(mg_solver, b: Tensor, x0: Optional[Tensor] = None, tol: float = 1e-8, max_it: int = 200,
                   restart: int = 30, precond: Optional[Callable] = None,
-                  stall_fallback: Optional[Callable] = None) -> Tuple[Tensor, dict]:
+                  stall_fallback: Optional[Callable] = None, stall_window: int = 1) -> Tuple[Tensor, dict]:
     """Flexible GMRES(restart) on FP64 vectors with a right preconditioner r -> z.
 
     `precond(r64, z64)` may change between applications.  When `stall_fallback`
-    is given, an inner cycle whose residual drops by less than 10 % switches the
-    remaining iterations to that preconditioner (the plain V-cycle)."""
+    is given, a residual that drops by less than 10 % over `stall_window`
+    consecutive inner iterations switches the remaining iterations to that
+    preconditioner (the plain V-cycle); `fell_back_at` in the result is the
+    iteration where that happened."""
     lv0 = mg_solver._levels[0]
     mask = lv0["mask_f"]
     V = _vec(mg_solver)
@@ -595,7 +597,9 @@ def fgmres_mg_f64(mg_solver, b: Tensor, x0: Optional[Tensor] = None, tol: float 
     total = 0
     hist = []
     fell_back = False
+    fell_back_at = None
     converged = False
+    w_stall = max(1, int(stall_window))
     while total < max_it:
         V.mop64(x, Vb[0], b=b64, mask=mask)
         beta = math.sqrt(V.dot(Vb[0], Vb[0], 1))
@@ -640,9 +644,11 @@ def fgmres_mg_f64(mg_solver, b: Tensor, x0: Optional[Tensor] = None, tol: float 
             hist.append(est)
             if est < tol or hn == 0:
                 break
-            if stall_fallback is not None and not fell_back and j >= 2 and est > 0.9 * hist[-2]:
+            if (stall_fallback is not None and not fell_back and j >= max(2, w_stall)
+                    and est > 0.9 * hist[-1 - w_stall]):
                 M = stall_fallback
                 fell_back = True
+                fell_back_at = total
         # x += Z y with H y = g
         y = [0.0] * j_done
         for i in range(j_done - 1, -1, -1):
@@ -659,4 +665,4 @@ def fgmres_mg_f64(mg_solver, b: Tensor, x0: Optional[Tensor] = None, tol: float 
                 break
     res = _true_res(V, x, b64, mask, w) / bnorm
     return x, {"converged": converged and res < tol, "it": total, "res_rel": res, "history": hist,
-               "fell_back": fell_back}
+               "fell_back": fell_back, "fell_back_at": fell_back_at}
