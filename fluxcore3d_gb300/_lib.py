@@ -84,6 +84,8 @@ class StepArgs(C.Structure):
         ("tracer_w", vp),
         ("tracer_solid", vp),
         ("tracer_dissipation", f32),
+        ("tile_order", C.c_int32),
+        ("gather_order", C.c_int32),
     ]
 
 

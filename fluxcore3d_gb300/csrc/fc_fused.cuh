@@ -97,6 +97,8 @@ struct FusedArgs {
     const float* tr_w;
     const uint8_t* tr_solid;
     float tr_diss;
+    int tile_order;     // staged pass: 0 tiles in ascending order, 1 descending
+    int gather_order;   // link gather: 0 links in ascending order, 1 descending
 };
 
 // shifted value h = f - w_q of population q at `cell` of the input buffer

@@ -473,6 +473,8 @@ __global__ void __launch_bounds__(256) k_link_gather_links(const FusedArgs a, co
                                                            long long n_subset, int skip_marked) {
     using T = typename Store<KIND>::T;
     long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (a.gather_order) t = (subset ? n_subset : a.n_links) - 1 - t;   // descending: negative past the end
+    if (t < 0) return;
     if (subset) {
         if (t >= n_subset) return;
         t = __ldg(subset + t);
@@ -676,6 +678,8 @@ int make_fused_args(const fc_lbm_step_args* s, FusedArgs& a) {
     a.tr_in = s->tracer_in; a.tr_out = s->tracer_out;
     a.tr_u = s->tracer_u; a.tr_v = s->tracer_v; a.tr_w = s->tracer_w;
     a.tr_solid = s->tracer_solid; a.tr_diss = s->tracer_dissipation;
+    a.tile_order = s->tile_order != 0;
+    a.gather_order = s->gather_order != 0;
     if (a.tr_in && (!a.tr_out || !a.tr_u || !a.tr_v || !a.tr_w || !a.tr_solid || a.tr_in == a.tr_out))
         return FC_ERR_ARG;
     if (a.tr_in && a.u && (a.tr_u == a.u || a.tr_v == a.v || a.tr_w == a.w)) return FC_ERR_ARG;

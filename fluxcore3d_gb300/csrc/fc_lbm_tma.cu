@@ -19,8 +19,10 @@
 // table saying which staged element each of them replaces.  Link cells and
 // links are stored in cell order, so a tile's links are one contiguous range;
 // fc_lbm_tile_links precomputes it with the first link of every chunk.
-// Persistent CTAs of 4 warps (4 per SM at 16-bit storage, 2 at FP32) rotate over
-// 2 shared-memory stages
+// Persistent CTAs of 4 warps (4 per SM at 16-bit storage, 2 at FP32) take the
+// tiles in ascending or, with tile_order, descending order (the step alternates,
+// so each pass starts on the planes the previous one wrote last, still in L2) and
+// rotate over 2 shared-memory stages
 // tracked by mbarriers; warps run through the tiles independently and the last
 // warp done with a stage refills it, so no CTA-wide barrier sits in the loop.
 //
@@ -312,6 +314,12 @@ __device__ __forceinline__ void tracer_pair(const FusedArgs& a, int i, int j, in
     *reinterpret_cast<float2*>(a.tr_out + idx) = make_float2(oa, ob);
 }
 
+// Tile taken at position q of the pass: q itself, or counted from the end when the
+// pass runs in descending order (every tile is computed the same either way).
+__device__ __forceinline__ int tile_at(const FusedArgs& a, const TileGeo& tg, int q) {
+    return a.tile_order ? tg.n_tiles - 1 - q : q;
+}
+
 // Record of the CTA's m-th tile (from the shared cache for the first ones).
 __device__ __forceinline__ TileRec tile_rec(const FusedArgs& a, const TileRec* cache, int m, int t) {
     TileRec r;
@@ -357,15 +365,17 @@ __global__ void __launch_bounds__(TS_THREADS, ts_min_blocks<KIND>())
     if (a.tile_links)
         for (int m = tid; m < TS_RANGE_CACHE; m += TS_THREADS) {
             const long long t = (long long)blockIdx.x + (long long)m * G;
-            if (t < tg.n_tiles) rcache[m] = tile_rec(a, rcache, TS_RANGE_CACHE, (int)t);
+            if (t < tg.n_tiles) rcache[m] = tile_rec(a, rcache, TS_RANGE_CACHE, tile_at(a, tg, (int)t));
         }
     __syncthreads();
     if (tid == 0) {
         for (int s = 0; s < S; ++s) {
-            const int t = blockIdx.x + s * G;
-            if (t < tg.n_tiles)
+            const int q = blockIdx.x + s * G;
+            if (q < tg.n_tiles) {
+                const int t = tile_at(a, tg, q);
                 issue_tile<KIND>(a, &tm_pop, &tm_flag, tg, t, tile_rec(a, rcache, s, t), stages + s * LY::STAGE,
                                  bar0 + 8 * s);
+            }
         }
     }
 
@@ -381,7 +391,7 @@ __global__ void __launch_bounds__(TS_THREADS, ts_min_blocks<KIND>())
     // (it, ch): tile iteration and chunk of this warp's current chunk, advanced by TS_WARPS chunks
     int it = warp / nch, ch = warp - (warp / nch) * nch;
     while (it < my_tiles) {
-        const int t = blockIdx.x + it * G;
+        const int t = tile_at(a, tg, blockIdx.x + it * G);
         const int s = it % S;
         const int i = t / tg.tiles_j;
         const int j0 = (t - i * tg.tiles_j) * tg.tj;
@@ -511,8 +521,9 @@ __global__ void __launch_bounds__(TS_THREADS, ts_min_blocks<KIND>())
             __threadfence_block();
             if (atomicAdd(done + s, 1) == touching - 1) {
                 done[s] = 0;
-                const int tn = t + S * G;
-                if (tn < tg.n_tiles) {
+                const int qn = blockIdx.x + (it + S) * G;
+                if (qn < tg.n_tiles) {
+                    const int tn = tile_at(a, tg, qn);
                     asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
                     issue_tile<KIND>(a, &tm_pop, &tm_flag, tg, tn, tile_rec(a, rcache, it + S, tn),
                                      stages + s * LY::STAGE, bar0 + 8 * s);

@@ -179,6 +179,7 @@ class FusedLBM:
         self._graphs = {}
         self._eager_steps = 0
         self.tracer = None  # a TracerField the main pass advances once per step (attach_tracer sets it)
+        self.alternate_order = True   # alternate the staged pass's tile order (and the gathers') per step
         self.args = StepArgs()
         self._fill_static_args()
 
@@ -384,9 +385,15 @@ class FusedLBM:
         a.pop_out = ptr(self.P[1 - cur])
         a.f32 = ptr(sim.f)
         self._set_macros(m_out)
+        # the staged pass alternates its tile order every step, and each link gather runs opposite
+        # to the pass that wrote its input, so both start on what is still in L2
+        alt = 1 if self.alternate_order else 0
+        a.tile_order = cur * alt
+        a.gather_order = cur * alt      # the in-step gather reads P[cur], written in order 1 - cur
         a.skip_link_gather = 1 if self.concurrent_gather else 0
         _lib.call("fc_lbm_fused_step", a, st)
         a.skip_link_gather = 0
+        a.gather_order = (1 - cur) * alt   # the gathers below read P[1 - cur], written in order cur
         if phase_event is not None:
             phase_event.record()
         if self.concurrent_gather:
@@ -469,6 +476,7 @@ class FusedLBM:
             for e0, e1 in ev:
                 a.pop_in = ptr(self.P[cur])
                 a.pop_out = ptr(self.P[1 - cur])
+                a.tile_order = cur if self.alternate_order else 0
                 self._set_macros(None)
                 e0.record()
                 _lib.call("fc_lbm_fused_step", a, stream_ptr())

@@ -178,6 +178,12 @@ typedef struct fc_lbm_step_args {
     const float* tracer_w;
     const uint8_t* tracer_solid;
     float tracer_dissipation;
+    /* Order in which the staged main pass takes its tiles (0: ascending cells, 1: descending) and in
+     * which the link gather takes its links.  The results do not depend on either; alternating the
+     * pass order every step and running the gather opposite to the pass that wrote its input makes
+     * both start on the cells written last, which are still in L2.  No reference counterpart. */
+    int32_t tile_order;
+    int32_t gather_order;
 } fc_lbm_step_args;
 
 /* One full time step for every non-deferred cell. */

@@ -213,6 +213,31 @@ def test_fused_planes_and_concurrent_gather_bit_identical(cuda, monkeypatch):
         assert np.array_equal(a, b)
 
 
+@pytest.mark.parametrize("concurrent", [True, False])
+def test_alternating_tile_and_gather_order_bit_identical(cuda, concurrent):
+    """The staged pass alternates its tile order every step and each link gather runs opposite to
+    the pass that wrote its input; the populations, plane states and macros are the same bits as
+    with every pass and gather in ascending order (links, sponge and inlet/outlet planes included)."""
+    out = {}
+    for alt in (True, False):
+        sim = cases.pin_fin(device=cuda, collision="mrt", storage="fp16", nx=48, ny=32, nz=48,
+                            n_pins=(3, 2), radius=3.5, height=24, base=4, sponge_length=8)
+        LBMCUDAUpgrade.patch(sim)
+        sim._fc.alternate_order = alt
+        sim._fc.concurrent_gather = concurrent and sim._fc.concurrent_gather
+        assert sim._fc.tile_links is not None
+        for _ in range(41):
+            sim.step(do_thermal=False)
+        sim.sync_f()
+        torch.cuda.synchronize()
+        assert sim._fc.check_device_error() == 0
+        P = sim._fc.P[sim._fc.cur]
+        out[alt] = (P.view(torch.uint8).cpu().numpy(), sim.f.cpu().numpy(), sim.rho.cpu().numpy(),
+                    sim.u.cpu().numpy())
+    for a, b in zip(out[True], out[False]):
+        assert np.array_equal(a, b)
+
+
 def test_bounded_mbarrier_wait_times_out_and_context_survives(cuda):
     """Failure detection without a GPU fault: the staged pass's bounded mbarrier wait gives up
     when nothing arrives and reports the timeout bit (4) to the host; with an arrival it completes;
