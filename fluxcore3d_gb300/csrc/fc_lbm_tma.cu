@@ -218,16 +218,22 @@ __device__ __forceinline__ f2 slab_pair(const unsigned char* slab, int q, int e0
     }
 }
 
-// Store population q of the pair at cells idx, idx+1 (idx even: one aligned store).
+// Store population q of the pair at cells idx, idx+1 (idx even: one aligned
+// store).  `keep` masks the packed 16-bit pair (0xffff per live cell), so a solid
+// cell stores its pinned shifted 0 without a select per value; FP32 takes the
+// values as given.
 template <int KIND>
-__device__ __forceinline__ void store_pair(const FusedArgs& a, int q, int idx, float x, float y) {
+__device__ __forceinline__ void store_pair(const FusedArgs& a, int q, int idx, float x, float y, unsigned keep) {
     if (KIND == ST_F32) {
         *reinterpret_cast<float2*>(reinterpret_cast<float*>(a.pout[q]) + idx) = make_float2(x + wq(q), y + wq(q));
     } else if (KIND == ST_F16S) {
-        *reinterpret_cast<__half2*>(reinterpret_cast<__half*>(a.pout[q]) + idx) = __floats2half2_rn(x, y);
+        const __half2 v = __floats2half2_rn(x, y);
+        *reinterpret_cast<unsigned*>(reinterpret_cast<__half*>(a.pout[q]) + idx) =
+            *reinterpret_cast<const unsigned*>(&v) & keep;
     } else {
-        *reinterpret_cast<__nv_bfloat162*>(reinterpret_cast<__nv_bfloat16*>(a.pout[q]) + idx) =
-            __floats2bfloat162_rn(x, y);
+        const __nv_bfloat162 v = __floats2bfloat162_rn(x, y);
+        *reinterpret_cast<unsigned*>(reinterpret_cast<__nv_bfloat16*>(a.pout[q]) + idx) =
+            *reinterpret_cast<const unsigned*>(&v) & keep;
     }
 }
 
@@ -503,9 +509,15 @@ __global__ void __launch_bounds__(TS_THREADS, ts_min_blocks<KIND>())
             }
             // deferred cells are stored too: the plane pass overwrites them after the BCs.
             // Solid cells get their pinned state (shifted 0, macros 1,0,0,0).
+            if constexpr (KIND == ST_F32) {
 #pragma unroll
-            for (int q = 0; q < 19; ++q)
-                store_pair<KIND>(a, q, idx, live_a ? h[q].v.x : 0.f, live_b ? h[q].v.y : 0.f);
+                for (int q = 0; q < 19; ++q)
+                    store_pair<KIND>(a, q, idx, live_a ? h[q].v.x : 0.f, live_b ? h[q].v.y : 0.f, 0u);
+            } else {
+                const unsigned keep = (live_a ? 0x0000ffffu : 0u) | (live_b ? 0xffff0000u : 0u);
+#pragma unroll
+                for (int q = 0; q < 19; ++q) store_pair<KIND>(a, q, idx, h[q].v.x, h[q].v.y, keep);
+            }
             if (a.rho) {
                 *reinterpret_cast<float2*>(a.rho + idx) =
                     make_float2(live_a ? m.rho.v.x : 1.f, live_b ? m.rho.v.y : 1.f);
