@@ -50,6 +50,21 @@ def test_argument_checks_return_status_without_gpu(native_lib):
     args.storage = 7
     assert native_lib.fc_lbm_fused_step(args, None) == 1
     assert native_lib.fc_lbm_wait_selftest(16, 0, None, None) == 1
+    # a carried tracer needs every buffer, and distinct in / out buffers and velocity / macro outputs
+    # (the step checks the argument block before it touches any pointer)
+    good = _lib.StepArgs()
+    good.nx, good.ny, good.nz = 16, 8, 16
+    good.pop_in, good.pop_out, good.cell_flags = 0x10000, 0x20000, 0x30000
+    for bad in ({"tracer_out": None}, {"tracer_solid": None}, {"tracer_out": 0x40000},
+                {"u": 0x50000, "v": 0x51000, "w": 0x52000, "rho": 0x53000}):
+        a = _lib.StepArgs.from_buffer_copy(good)
+        a.tracer_in, a.tracer_out = 0x40000, 0x41000
+        a.tracer_u, a.tracer_v, a.tracer_w, a.tracer_solid = 0x50000, 0x51000, 0x52000, 0x60000
+        assert native_lib.fc_lbm_tile_links(a, None, 0, None, 0, None, 0, None) > 0   # accepted as is
+        for k, v in bad.items():
+            setattr(a, k, v)
+        assert native_lib.fc_lbm_tile_links(a, None, 0, None, 0, None, 0, None) == -1, bad
+        assert native_lib.fc_lbm_fused_step(a, None) == 1, bad
 
 
 def test_face_roles_table():
