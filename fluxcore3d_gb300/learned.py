@@ -274,15 +274,20 @@ class LearnedPreconditioner:
 
 class LearnedCorrection:
     """Preconditioner callable (r64, z64) for fgmres_mg_f64: one plain V-cycle, then the network
-    applied to what it leaves behind,  z = v + N(r - A v)  with v = V(r).
+    applied to what it leaves behind, then `post_smooth` damped-Jacobi sweeps of the fine level:
+    z = S(v + N(r - A v)) with v = V(r).
 
     The V-cycle removes the oscillatory error; the network is trained (learned_bench,
     `correction=True` pairs) on the residual a V-cycle leaves and the exact error that goes with
     it, i.e. on the smooth, long-range part that geometric coarsening handles poorly across the
-    conductivity jumps and along the flow.  Every vector is zero on the Dirichlet rows."""
+    conductivity jumps and along the flow.  Like the coarse correction of a two-grid cycle, the
+    network's output carries some oscillatory error, which A = I + dt L (dt = 1000) turns into a
+    large residual; the sweeps after it remove that part.  Every vector is zero on the Dirichlet
+    rows."""
 
-    def __init__(self, net: UNetPreconditioner, mg_solver, k_field: torch.Tensor):
+    def __init__(self, net: UNetPreconditioner, mg_solver, k_field: torch.Tensor, post_smooth: int = 0):
         self.net = net
+        self.post_smooth = int(post_smooth)
         self.mg = mg_solver
         lv0 = mg_solver._levels[0]
         self.lv0 = lv0
@@ -311,7 +316,9 @@ class LearnedCorrection:
         _lib.call("fc_vec_convert", 1, ptr(lv0["b_buf"]), ptr(r64), n, ptr(self.mask), 1.0, st)
         r1 = self.residual_after_vcycle(lv0["b_buf"])
         y = self.net.forward(r1, self.k)
-        # x += y (masked), then z = x in FP64
+        # x += y (masked), smoothing sweeps on A x = r, then z = x in FP64
         _lib.call("fc_vec_axpby", 0, ptr(lv0["x"]), ptr(y), n, 1.0, None, None, 1.0, ptr(self.mask), st)
+        if self.post_smooth > 0:
+            self.mg._smooth_n(0, self.post_smooth)
         _lib.call("fc_vec_convert", 0, ptr(z64), ptr(lv0["x"]), n, ptr(self.mask), 1.0, st)
         self.calls += 1
