@@ -45,7 +45,7 @@ def peaks():
     if os.path.exists(p):
         with open(p) as fh:
             d = json.load(fh)
-        return float(d["hbm_gbs"]), float(d.get("bf16_tflops", 1924.8)), "measured"
+        return float(d["hbm_gbs"]), float(d.get("bf16_tflops", 1900.0)), "measured"
     return 6800.0, 1900.0, "fallback"
 
 
