@@ -134,3 +134,34 @@ def test_learned_correction_is_certified_and_measured(cuda):
     assert np.isfinite(q["vcycle_plus_net_rel_err"]) and q["vcycle_rel_err"] < 1.0
     print("learned correction:", r, q)
     assert net.check_device_error() == 0
+
+
+def test_learned_correction_post_smoothing_and_stall_window(cuda):
+    """LearnedCorrection(post_smooth=n) is the correction followed by n smoothing sweeps of the fine
+    level on the same right-hand side, bit for bit; FGMRES with a windowed stall test converges and
+    reports the iteration of its fallback (or None)."""
+    from fluxcore3d_gb300 import learned_bench as lb
+    from fluxcore3d_gb300.learned import LearnedCorrection, UNetPreconditioner
+    from fluxcore3d_gb300.solver import mg_pcg
+    dev = torch.device("cuda")
+    mg, k, solid = lb.make_problem(16, 300, dev)
+    b = lb.random_rhs(16, np.random.default_rng(3), dev, solid)
+    net = UNetPreconditioner(device=dev, seed=2)
+    lv0 = mg._levels[0]
+    mask = lv0["mask_f"]
+    r64 = (b.double() * mask.double()).contiguous()
+    z0 = torch.zeros_like(r64)
+    LearnedCorrection(net, mg, k, post_smooth=0)(r64, z0)
+    mg._smooth_n(0, 2)                       # the same sweeps, on the state the correction left
+    expect = (lv0["x"].double() * mask.double()).cpu().numpy()
+    z2 = torch.zeros_like(r64)
+    LearnedCorrection(net, mg, k, post_smooth=2)(r64, z2)
+    assert np.array_equal(z2.cpu().numpy(), expect)
+    assert not np.array_equal(z2.cpu().numpy(), z0.cpu().numpy())
+    pc = LearnedCorrection(net, mg, k, post_smooth=2)
+    _, info = mg_pcg.fgmres_mg_f64(mg, b, tol=1e-8, max_it=300, restart=30, precond=pc,
+                                   stall_fallback=mg_pcg._vcycle_pc(mg), stall_window=5)
+    assert info["converged"] and info["res_rel"] < 1e-8
+    assert info["fell_back_at"] is None or info["fell_back_at"] >= 5
+    assert info["fell_back"] == (info["fell_back_at"] is not None)
+    assert net.check_device_error() == 0
