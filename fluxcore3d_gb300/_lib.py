@@ -156,6 +156,7 @@ SIGNATURES: dict[str, tuple] = {
     "fc_bicgstab_xr": (i32, [i32, vp, vp, vp, vp, C.c_int64, vp, i32, vp, C.c_int64, vp]),
     "fc_mg_mop_f64": (i32, [vp] * 8 + [f64, i32, i32, i32, i32, i32, vp, vp, vp, vp]),
     "fc_mg_mop_f32": (i32, [vp] * 8 + [f32, i32, i32, i32, i32, i32, vp, vp, vp, vp]),
+    "fc_mg_mop_transpose_f32": (i32, [vp] * 7 + [f32, i32, i32, i32, i32, i32, vp, vp, vp]),
     # thermal
     "fc_thermal_rhs": (i32, [vp] * 7 + [f32, i64, vp]),
     "fc_thermal_reconstruct": (i32, [vp, vp, vp, i32, i32, i32, i32, i32, vp]),

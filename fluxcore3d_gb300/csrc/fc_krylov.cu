@@ -218,6 +218,39 @@ __global__ void __launch_bounds__(BLOCK) k_dot2_part(const T* __restrict__ x, co
     }
 }
 
+// y += M^T (mask * x), scattered: row r of M holds 1 + dt sum_n a_n(r) on the diagonal and
+// -dt a_n(r) at its (ghosted) neighbour n, so row r adds x_r times each entry to the column
+// it sits in.  A ghost that maps a direction onto the cell itself adds +dt a_n and -dt a_n to
+// the same column, as the row does.  y must be zero on entry.
+__global__ void __launch_bounds__(BLOCK) k_mop_transpose(const float* __restrict__ x, const float* __restrict__ aE,
+                                                         const float* __restrict__ aW, const float* __restrict__ aN,
+                                                         const float* __restrict__ aS, const float* __restrict__ aU,
+                                                         const float* __restrict__ aD, float dt, Lvl g,
+                                                         const float* __restrict__ mask, float* __restrict__ y) {
+    const long long n = (long long)g.nx * g.ny * g.nz;
+    const long long idx = (long long)blockIdx.x * BLOCK + threadIdx.x;
+    if (idx >= n) return;
+    if (mask && mask[idx] == 0.f) return;
+    const float v = x[idx];
+    if (v == 0.f) return;
+    const long long nynz = (long long)g.ny * g.nz;
+    const int i = (int)idx / (int)nynz;
+    const int rr = (int)idx - i * (int)nynz;
+    const int j = rr / g.nz, k = rr - j * g.nz;
+    const int iE = i < g.nx - 1 ? i + 1 : i - 1, iW = i > 0 ? i - 1 : lowg(g, 0);
+    const int jN = j < g.ny - 1 ? j + 1 : j - 1, jS = j > 0 ? j - 1 : lowg(g, 1);
+    const int kU = k < g.nz - 1 ? k + 1 : k - 1, kD = k > 0 ? k - 1 : lowg(g, 2);
+    const float e = aE[idx], w = aW[idx], nn = aN[idx], s = aS[idx], u = aU[idx], d = aD[idx];
+    const float dv = dt * v;
+    atomicAdd(y + idx, v + dv * (((e + w) + (nn + s)) + (u + d)));
+    atomicAdd(y + iE * nynz + (long long)j * g.nz + k, -dv * e);
+    atomicAdd(y + iW * nynz + (long long)j * g.nz + k, -dv * w);
+    atomicAdd(y + i * nynz + (long long)jN * g.nz + k, -dv * nn);
+    atomicAdd(y + i * nynz + (long long)jS * g.nz + k, -dv * s);
+    atomicAdd(y + i * nynz + (long long)j * g.nz + kU, -dv * u);
+    atomicAdd(y + i * nynz + (long long)j * g.nz + kD, -dv * d);
+}
+
 }  // namespace
 
 extern "C" {
@@ -355,6 +388,20 @@ int fc_mg_mop_f64(const double* x, const float* aE, const float* aW, const float
     Lvl g{nx, ny, nz, ax, out_idx};
     k_mop_t<double><<<grid_for((long long)nx * ny * nz), BLOCK, 0, (cudaStream_t)stream>>>(
         x, aE, aW, aN, aS, aU, aD, diagL, dt, g, b, mask, y);
+    return launch_status();
+}
+
+int fc_mg_mop_transpose_f32(const float* x, const float* aE, const float* aW, const float* aN, const float* aS,
+                            const float* aU, const float* aD, float dt, int nx, int ny, int nz, int ax,
+                            int out_idx, const float* mask, float* y, void* stream) {
+    if (!x || !y || !aE || !aW || !aN || !aS || !aU || !aD || nx < 2 || ny < 2 || nz < 2 || ax < 0 || ax > 2)
+        return FC_ERR_ARG;
+    if (x == y || (long long)nx * ny * nz >= (1LL << 31)) return FC_ERR_ARG;
+    const long long n = (long long)nx * ny * nz;
+    cudaStream_t st = (cudaStream_t)stream;
+    if (cudaMemsetAsync(y, 0, (size_t)n * sizeof(float), st) != cudaSuccess) return FC_ERR_LAUNCH;
+    Lvl g{nx, ny, nz, ax, out_idx};
+    k_mop_transpose<<<grid_for(n), BLOCK, 0, st>>>(x, aE, aW, aN, aS, aU, aD, dt, g, mask, y);
     return launch_status();
 }
 

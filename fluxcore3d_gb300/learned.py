@@ -190,6 +190,45 @@ class UNetPreconditioner:
         _lib.call("fc_nn_mse_grad", ptr(S["yj"]), 16, ptr(tn), ptr(wv), nvox, ptr(gj), ptr(ws), nb, st)
         nblk = (nvox + 255) // 256
         loss = float(ws[: nblk * 8].view(torch.float64).sum().item()) / nvox
+        return loss, self._backward(gj)
+
+    def residual_loss_and_grad(self, r, k, ops):
+        """Residual-norm loss of the correction: for sample b with operator M_b = I + dt L_b
+        (ops[b]: dict with the fine level's coefficient pointers `coef` (aE, aW, aN, aS, aU, aD,
+        diagL), `dt`, `ax`, `out_idx` and the FP32 `mask`), the normalised residual left by the
+        masked output y, rho = mask (r / rms(r) - M (mask y)), relative to the normalised
+        right-hand side: loss = mean_b ||rho||^2 / ||r / rms(r)||^2.  Its gradient with respect to y,
+        -2 mask M^T rho / ||r / rms(r)||^2, enters the output channel; fills layer.g.
+        Returns (loss, [grad per layer as [C_out, 27, C_in] FP32])."""
+        self.forward(r, k, keep=True)
+        S = self._saved
+        B, D, H, W = S["shape"]
+        st = stream_ptr()
+        gj = torch.zeros_like(S["yj"])
+        loss = 0.0
+        for b in range(B):
+            op = ops[b]
+            mask = op["mask"]
+            y = (S["yj"][b, ..., 0] * mask).contiguous()
+            rhat = (r[b] * S["inv"][b]).contiguous()
+            rho = torch.empty_like(rhat)
+            _lib.call("fc_mg_mop_f32", ptr(y), *op["coef"], float(op["dt"]), D, H, W, op["ax"], op["out_idx"],
+                      ptr(rhat), ptr(mask), ptr(rho), st)
+            den = float((rhat.double() ** 2).sum()) + 1e-30
+            loss += float((rho.double() ** 2).sum()) / den / B
+            g = torch.empty_like(rhat)
+            _lib.call("fc_mg_mop_transpose_f32", ptr(rho), *op["coef"][:6], float(op["dt"]), D, H, W, op["ax"],
+                      op["out_idx"], ptr(mask), ptr(g), st)
+            gj[b, ..., 0] = g * mask * (-2.0 / den / B)
+        return loss, self._backward(gj)
+
+    def _backward(self, gj):
+        """Back-propagate the gradient gj of the FP32 16-channel output through the saved forward
+        pass; fills layer.g and returns the per-layer gradients."""
+        S = self._saved
+        B, D, H, W = S["shape"]
+        s0, s1, s2 = (B, D, H, W), (B, D // 2, H // 2, W // 2), (B, D // 4, H // 4, W // 4)
+        st = stream_ptr()
         L = self.L
         _, gjb = self._act(gj, None, False)
         self._wgrad(S["yi"], gjb, L["j"], s0)
@@ -230,8 +269,7 @@ class UNetPreconditioner:
         g = self._dgrad(gbb, L["b"], s0)
         _, gab = self._act(g, S["ya"], True)
         self._wgrad(S["x"], gab, L["a"], s0)
-        grads = [l.g[:, :27 * l.cin].reshape(l.cout, 27, l.cin) for l in self.layers]
-        return loss, grads
+        return [l.g[:, :27 * l.cin].reshape(l.cout, 27, l.cin) for l in self.layers]
 
     def adam_step(self, lr=1e-3, beta1=0.9, beta2=0.999, eps=1e-8):
         self.step_count += 1

@@ -365,6 +365,13 @@ int fc_mg_mop_f64(const double* x, const float* aE, const float* aW, const float
 int fc_mg_mop_f32(const float* x, const float* aE, const float* aW, const float* aN, const float* aS,
                   const float* aU, const float* aD, const float* diagL, float dt, int nx, int ny, int nz, int ax,
                   int out_idx, const float* b, const float* mask, float* y, void* stream);
+/* y = M^T (mask * x): the transpose of the operator of fc_mg_mop_f32 (same coefficients and
+ * boundary ghosting), applied to the masked vector, FP32, accumulated with atomics (summation order
+ * not fixed).  For the residual-norm loss of the learned correction, whose gradient is
+ * -2 M^T (b - M y).  No reference counterpart. */
+int fc_mg_mop_transpose_f32(const float* x, const float* aE, const float* aW, const float* aN, const float* aS,
+                            const float* aU, const float* aD, float dt, int nx, int ny, int nz, int ax,
+                            int out_idx, const float* mask, float* y, void* stream);
 
 /* ---------------------------------------------------------------------------
  * Thermal pseudo-time step (the THERMAL_CUDA module surface)
