@@ -175,7 +175,6 @@ class UNetPreconditioner:
         self.forward(r, k, keep=True)
         S = self._saved
         B, D, H, W = S["shape"]
-        s0, s1, s2 = (B, D, H, W), (B, D // 2, H // 2, W // 2), (B, D // 4, H // 4, W // 4)
         st = stream_ptr()
         nvox = B * D * H * W
         tn2 = target.reshape(B, -1) * S["inv"][:, None]
